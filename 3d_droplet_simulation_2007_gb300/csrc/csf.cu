@@ -1,0 +1,142 @@
+// csf.cu -- CSF surface-tension force (csf, main.f:2363-2481): 27-point filter
+// of the volume fraction, face-normal curvature kappa = -div(n), and the face
+// forces S11/S22/S33 = sigh * (c~_i - c~_{i-1}) * kappa_i, plus bc_tensor
+// (main.f:4222-4296).
+#include "dsg_internal.cuh"
+
+namespace dsg {
+namespace {
+
+// Curvature at interior cells: six face-normal magnitudes with transverse
+// 4-point means (+1e-50 inside the root), kappa = -(d1x-d2x+d1y-d2y+d1z-d2z).
+__global__ void k_curvature(double *__restrict__ kap, const double *__restrict__ f, Dims d) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
+  const int k = blockIdx.z + 2;
+  if (i > d.nx - 1 || j > d.ny - 1) return;
+  const size_t q = d.ix(i, j, k);
+  const long sy = (long)d.sy(), sz = (long)d.sz();
+#define F(di, dj, dk) f[q + (long)(di) + (long)(dj) * sy + (long)(dk) * sz]
+  double t0, t1, t2;
+  t0 = F(1, 0, 0) - F(0, 0, 0);
+  t1 = F(0, 1, 0) - F(0, -1, 0) + F(1, 1, 0) - F(1, -1, 0);
+  t2 = F(0, 0, 1) - F(0, 0, -1) + F(1, 0, 1) - F(1, 0, -1);
+  const double nxu = sqrt(t0 * t0 + 0.0625 * (t1 * t1) + 0.0625 * (t2 * t2) + 1.e-50);
+  t0 = F(0, 0, 0) - F(-1, 0, 0);
+  t1 = F(0, 1, 0) - F(0, -1, 0) + F(-1, 1, 0) - F(-1, -1, 0);
+  t2 = F(0, 0, 1) - F(0, 0, -1) + F(-1, 0, 1) - F(-1, 0, -1);
+  const double nxd = sqrt(t0 * t0 + 0.0625 * (t1 * t1) + 0.0625 * (t2 * t2) + 1.e-50);
+  t0 = F(0, 1, 0) - F(0, 0, 0);
+  t1 = F(1, 0, 0) - F(-1, 0, 0) + F(1, 1, 0) - F(-1, 1, 0);
+  t2 = F(0, 0, 1) - F(0, 0, -1) + F(0, 1, 1) - F(0, 1, -1);
+  const double nyu = sqrt(t0 * t0 + 0.0625 * (t1 * t1) + 0.0625 * (t2 * t2) + 1.e-50);
+  t0 = F(0, 0, 0) - F(0, -1, 0);
+  t1 = F(1, 0, 0) - F(-1, 0, 0) + F(1, -1, 0) - F(-1, -1, 0);
+  t2 = F(0, 0, 1) - F(0, 0, -1) + F(0, -1, 1) - F(0, -1, -1);
+  const double nyd = sqrt(t0 * t0 + 0.0625 * (t1 * t1) + 0.0625 * (t2 * t2) + 1.e-50);
+  t0 = F(0, 0, 1) - F(0, 0, 0);
+  t1 = F(1, 0, 0) - F(-1, 0, 0) + F(1, 0, 1) - F(-1, 0, 1);
+  t2 = F(0, 1, 0) - F(0, -1, 0) + F(0, 1, 1) - F(0, -1, 1);
+  const double nzu = sqrt(t0 * t0 + 0.0625 * (t1 * t1) + 0.0625 * (t2 * t2) + 1.e-50);
+  t0 = F(0, 0, 0) - F(0, 0, -1);
+  t1 = F(1, 0, 0) - F(-1, 0, 0) + F(1, 0, -1) - F(-1, 0, -1);
+  t2 = F(0, 1, 0) - F(0, -1, 0) + F(0, 1, -1) - F(0, -1, -1);
+  const double nzd = sqrt(t0 * t0 + 0.0625 * (t1 * t1) + 0.0625 * (t2 * t2) + 1.e-50);
+  const double d1x = (F(1, 0, 0) - F(0, 0, 0)) / nxu;
+  const double d2x = (F(0, 0, 0) - F(-1, 0, 0)) / nxd;
+  const double d1y = (F(0, 1, 0) - F(0, 0, 0)) / nyu;
+  const double d2y = (F(0, 0, 0) - F(0, -1, 0)) / nyd;
+  const double d1z = (F(0, 0, 1) - F(0, 0, 0)) / nzu;
+  const double d2z = (F(0, 0, 0) - F(0, 0, -1)) / nzd;
+#undef F
+  kap[q] = -(d1x - d2x + d1y - d2y + d1z - d2z);
+}
+
+__global__ void k_csf_force(double *__restrict__ s11, double *__restrict__ s22, double *__restrict__ s33,
+                            const double *__restrict__ f, const double *__restrict__ kap, Dims d,
+                            double sigh) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
+  const int k = blockIdx.z + 2;
+  if (i > d.nx - 1 || j > d.ny - 1) return;
+  const size_t q = d.ix(i, j, k);
+  const double kq = kap[q], fq = f[q];
+  s11[q] = sigh * (fq - f[q - 1]) * kq;
+  s22[q] = sigh * (fq - f[q - d.sy()]) * kq;
+  s33[q] = sigh * (fq - f[q - d.sz()]) * kq;
+}
+
+// bc_tensor, three ordered steps.
+__global__ void k_bct_x(double *__restrict__ s11, double *__restrict__ s12, double *__restrict__ s13, Dims d) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 2;
+  const int k = blockIdx.y * blockDim.y + threadIdx.y + 2;
+  if (j > d.ny - 1 || k > d.nz - 1) return;
+  s11[d.ix(1, j, k)] = 0.0;
+  s12[d.ix(d.nx, j, k)] = 0.0;
+  s13[d.ix(d.nx, j, k)] = 0.0;
+}
+
+__global__ void k_bct_y(double *__restrict__ s22, double *__restrict__ s12, double *__restrict__ s23, Dims d) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int k = blockIdx.y * blockDim.y + threadIdx.y + 2;
+  if (i > d.nx || k > d.nz - 1) return;
+  s22[d.ix(i, 1, k)] = s22[d.ix(i, 2, k)];
+  s12[d.ix(i, d.ny, k)] = 0.0;
+  s23[d.ix(i, d.ny, k)] = 0.0;
+}
+
+__global__ void k_bct_z(double *__restrict__ s33, double *__restrict__ s13, double *__restrict__ s23, Dims d) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (i > d.nx || j > d.ny) return;
+  s33[d.ix(i, j, 1)] = 0.0;
+  s13[d.ix(i, j, 2)] = 0.0;
+  s13[d.ix(i, j, d.nz)] = 0.0;
+  s23[d.ix(i, j, 2)] = 0.0;
+  s23[d.ix(i, j, d.nz)] = 0.0;
+}
+
+const dim3 kBlk(32, 4, 1);
+
+}  // namespace
+
+cudaError_t bc_tensor(double *const S[6], Dims d, cudaStream_t st) {
+  // S = {S11, S22, S33, S12, S13, S23}
+  const dim3 b2(32, 8);
+  DSG_COUNT k_bct_x<<<dim3((d.ny + 31) / 32, (d.nz + 7) / 8), b2, 0, st>>>(S[0], S[3], S[4], d);
+  DSG_COUNT k_bct_y<<<dim3((d.nx + 31) / 32, (d.nz + 7) / 8), b2, 0, st>>>(S[1], S[3], S[5], d);
+  DSG_COUNT k_bct_z<<<dim3((d.nx + 31) / 32, (d.ny + 7) / 8), b2, 0, st>>>(S[2], S[4], S[5], d);
+  return cudaGetLastError();
+}
+
+// csf with the reference's scratch aliasing: w11 = pressure array, w22 = fine
+// residual array, w33 = fine rhs array; ccf is the routine's local array.
+cudaError_t csf(const double *ccc, double *w11, double *w22, double *w33, double *ccf, double *const S[6],
+                Dims d, double tau, double sigma, double h, cudaStream_t st) {
+  const size_t bytes = d.count() * sizeof(double);
+  // copy(ccf,ccc); filterc27(ccf,w22); copy(ccf,w22): filtering ccf == filtering ccc
+  cudaError_t e = filterc27(ccc, w22, d, st);
+  if (e != cudaSuccess) return e;
+  e = cudaMemcpyAsync(ccf, w22, bytes, cudaMemcpyDeviceToDevice, st);
+  if (e != cudaSuccess) return e;
+  e = bc_out(ccf, d, st);
+  if (e != cudaSuccess) return e;
+  if (sigma == 0.0) {
+    for (int m = 0; m < 6; m++) {
+      e = cudaMemsetAsync(S[m], 0, bytes, st);
+      if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+  }
+  const double sigh = 0.5 * (tau * tau) * sigma / (h * h * h);
+  DSG_COUNT k_curvature<<<interior_grid(d, kBlk), kBlk, 0, st>>>(w11, ccf, d);
+  e = bc_out(w11, d, st);
+  if (e != cudaSuccess) return e;
+  DSG_COUNT k_csf_force<<<interior_grid(d, kBlk), kBlk, 0, st>>>(S[0], S[1], S[2], ccf, w11, d, sigh);
+  if ((e = cudaMemcpyAsync(w11, S[0], bytes, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyAsync(w22, S[1], bytes, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyAsync(w33, S[2], bytes, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
+  return bc_tensor(S, d, st);
+}
+
+}  // namespace dsg

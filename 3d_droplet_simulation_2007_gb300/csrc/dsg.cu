@@ -1,0 +1,603 @@
+// dsg.cu -- context, device arena and host orchestration of the time step:
+// readinput/memoryaloc/nondim (main.f:185-446), the main.f:19-73 loop body,
+// solvelpres (main.f:3236-3439) and the FMG driver mglin (main.f:3645-3763).
+// Everything runs on one CUDA stream; the only host reads inside a step are the
+// CFL maximum of checktime, the residual norm of the tol modes (once per
+// V-cycle) and the divergence maximum of the relaxation-count adaptivity
+// (every 10 steps).
+#include <math.h>
+#include <stdarg.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <vector>
+
+#include "dsg_internal.cuh"
+
+static std::string g_last_error;
+
+namespace dsg {
+
+std::atomic<long long> g_launches{0};
+
+int set_error(dsg_ctx *ctx, int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (ctx) ctx->err = buf;
+  g_last_error = buf;
+  return code;
+}
+
+int cuda_fail(dsg_ctx *ctx, cudaError_t e, const char *where) {
+  return set_error(ctx, e == cudaErrorMemoryAllocation ? DSG_E_NOMEM : DSG_E_CUDA, "CUDA error %d (%s) at %s",
+                   (int)e, cudaGetErrorString(e), where);
+}
+
+}  // namespace dsg
+
+using dsg::Dims;
+
+namespace {
+
+// nondim, main.f:341-446 (drop case).  Host arithmetic keeps the reference's
+// operation order; this translation unit is built without FP contraction.
+void nondim(dsg_ctx *ctx) {
+  const dsg_config &in = ctx->cfg;
+  dsg_scalars &s = ctx->s;
+  s.lengthscale = in.length_si;
+  const double dx = in.xvel1_si - in.xvel2_si, dy = in.yvel1_si - in.yvel2_si, dz = in.zvel1_si - in.zvel2_si;
+  double vscale = sqrt(dx * dx + dy * dy + dz * dz);
+  if (vscale == 0.0) vscale = 1.0;
+  s.vscale = vscale;
+  const double timescale = s.lengthscale / vscale;
+  s.lengthsize = in.length_si / s.lengthscale;
+  s.h = s.lengthsize / (ctx->nx - 2);
+  s.time = 0.0;
+  const double tau_si = in.maxcfl * (double)0.8f * (in.length_si / (ctx->nx - 2)) / vscale;
+  s.tau = tau_si / timescale;
+  s.tauh = s.tau / s.h;
+  s.tauh2 = (int)(s.tau / (s.h * s.h));
+  s.tswap = 0;
+  s.radius = in.radius_si / s.lengthscale;
+  s.xvel1 = in.xvel1_si / vscale;
+  s.yvel1 = in.yvel1_si / vscale;
+  s.zvel1 = in.zvel1_si / vscale;
+  s.xvel2 = in.xvel2_si / vscale;
+  s.yvel2 = in.yvel2_si / vscale;
+  s.zvel2 = in.zvel2_si / vscale;
+  s.y0 = (ctx->ny - 2) * s.h / 2;
+  s.z0 = (ctx->nz - 2) * s.h / 2;
+  s.rho1 = 1.0;
+  s.rho2 = in.rho2_si / in.rho1_si;
+  const double L = s.lengthscale;
+  double denom = in.rho1_si * (L * L) / timescale;
+  s.mu1 = in.visc1_si / denom;
+  s.mu2 = in.visc2_si / denom;
+  denom = in.rho1_si * (L * L * L) / (timescale * timescale);
+  s.sigma = in.sigma_si / denom;
+  denom = L / (timescale * timescale);
+  s.g = in.grav_si / denom;
+  s.g1 = in.grav1_si / denom;
+}
+
+inline double *S6(dsg_ctx *c, int m) { return c->f[DSG_F_S11 + m]; }
+
+struct Tensor {
+  double *p[6];
+  explicit Tensor(dsg_ctx *c) {
+    for (int m = 0; m < 6; m++) p[m] = S6(c, m);
+  }
+};
+
+int read_device(dsg_ctx *ctx, int n) {
+  DSG_CK(ctx, cudaMemcpyAsync(ctx->red_host, ctx->red_out, n * sizeof(double), cudaMemcpyDeviceToHost,
+                              ctx->stream));
+  DSG_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  return DSG_OK;
+}
+
+// relax_n on level jj; the finest level is timed with an event pair when the
+// live profile is on.
+cudaError_t relax_level(dsg_ctx *ctx, int n, int jj, double ls) {
+  double **L = ctx->lv[jj];
+  const Dims d = ctx->level(jj);
+  const bool timed = ctx->prof && jj == ctx->ng && n > 0;
+  if (timed) {
+    if (ctx->prof_used + 2 > ctx->prof_ev.size()) {
+      for (int q = 0; q < 256; q++) {
+        cudaEvent_t e;
+        cudaError_t r = cudaEventCreate(&e);
+        if (r != cudaSuccess) return r;
+        ctx->prof_ev.push_back(e);
+      }
+    }
+    cudaError_t r = cudaEventRecord(ctx->prof_ev[ctx->prof_used], ctx->stream);
+    if (r != cudaSuccess) return r;
+  }
+  cudaError_t e = dsg::relax_n(n, L[1], ls, L[3], L[4], L[5], L[6], L[7], d, ctx->cfg.omega, ctx->stream);
+  if (timed) {
+    cudaError_t r = cudaEventRecord(ctx->prof_ev[ctx->prof_used + 1], ctx->stream);
+    if (r != cudaSuccess) return r;
+    ctx->prof_used += 2;
+    ctx->prof_relax_calls += n;
+    ctx->prof_relax_bytes += (double)n * 6.0 * sizeof(double) * (double)d.count();
+  }
+  return e;
+}
+
+// One V-cycle from level j down to 1 and back (main.f:3705-3759).
+int vcycle(dsg_ctx *ctx, int j) {
+  const double ls = ctx->s.lengthsize;
+  cudaStream_t st = ctx->stream;
+  for (int jj = j; jj >= 2; jj--) {
+    double **L = ctx->lv[jj];
+    const Dims d = ctx->level(jj);
+    DSG_CK(ctx, relax_level(ctx, ctx->s.npre, jj, ls));
+    DSG_CK(ctx, dsg::resid(ls, L[2], L[1], L[3], L[4], L[5], L[6], d, st));
+    const Dims dc = ctx->level(jj - 1);
+    DSG_CK(ctx, dsg::rstrct(ctx->lv[jj - 1][3], L[2], dc, st));
+    DSG_CK(ctx, dsg::fill_zero(ctx->lv[jj - 1][1], dc.count(), st));
+  }
+  DSG_CK(ctx, relax_level(ctx, ctx->s.ntop, 1, ls));
+  for (int jj = 2; jj <= j; jj++) {
+    double **L = ctx->lv[jj];
+    const Dims d = ctx->level(jj);
+    DSG_CK(ctx, dsg::addint(L[1], ctx->lv[jj - 1][1], L[2], d, st));
+    DSG_CK(ctx, relax_level(ctx, ctx->s.npost, jj, ls));
+  }
+  return DSG_OK;
+}
+
+int relres_host(dsg_ctx *ctx, double *out) {
+  double **L = ctx->lv[ctx->ng];
+  DSG_CK(ctx, dsg::relres_sums(ctx->red_out, ctx->red_partials, ctx->s.lengthsize, L[1], L[3], L[4], L[5],
+                               L[6], ctx->fine(), ctx->stream));
+  int rc = read_device(ctx, 2);
+  if (rc) return rc;
+  const double rr = ctx->red_host[0], bb = ctx->red_host[1];
+  if (!isfinite(rr) || !isfinite(bb))
+    return dsg::set_error(ctx, DSG_E_NONFINITE, "non-finite residual norm (%g, %g)", rr, bb);
+  *out = bb > 0.0 ? sqrt(rr) / sqrt(bb) : sqrt(rr);
+  return DSG_OK;
+}
+
+int mglin(dsg_ctx *ctx, dsg_mg_stats *stats) {
+  const int ng = ctx->ng;
+  const double om = ctx->cfg.omega;
+  cudaStream_t st = ctx->stream;
+  int fine_sweeps = 0;
+  for (int g = ng - 1; g >= 1; g--) {
+    const Dims dc = ctx->level(g);
+    DSG_CK(ctx, dsg::rstrct(ctx->lv[g][3], ctx->lv[g + 1][3], dc, st));
+    DSG_CK(ctx, dsg::acfromac(ctx->lv[g][4], ctx->lv[g][5], ctx->lv[g][6], ctx->lv[g][7], ctx->lv[g + 1][4],
+                              ctx->lv[g + 1][5], ctx->lv[g + 1][6], dc, st));
+  }
+  double **L1 = ctx->lv[1];
+  DSG_CK(ctx, dsg::fill_zero(L1[1], ctx->level(1).count(), st));
+  // First coarse solve with lengthscale in place of lengthsize (main.f:3686-3689).
+  DSG_CK(ctx, dsg::relax_n(ctx->s.ntop, L1[1], ctx->s.lengthscale, L1[3], L1[4], L1[5], L1[6], L1[7],
+                           ctx->level(1), om, st));
+  for (int j = 2; j <= ng; j++) {
+    DSG_CK(ctx, dsg::interp(ctx->lv[j][1], ctx->lv[j - 1][1], ctx->level(j), st));
+    for (int c = 0; c < ctx->cfg.cycles; c++) {
+      int rc = vcycle(ctx, j);
+      if (rc) return rc;
+      if (j == ng) fine_sweeps += ctx->s.npre + ctx->s.npost;
+    }
+  }
+  dsg_mg_stats s;
+  memset(&s, 0, sizeof s);
+  s.mode = ctx->cfg.mode;
+  s.relres = -1.0;
+  s.relres_init = -1.0;
+  s.epsdiv = -1.0;
+  ctx->s.last_vcycles = 0;
+  ctx->s.last_relres = -1.0;
+  ctx->s.last_relres_fmg = -1.0;
+  if (ctx->cfg.mode == DSG_MODE_TOL_FP64) {
+    double r;
+    int rc = relres_host(ctx, &r);
+    if (rc) return rc;
+    s.relres_init = r;
+    int n = 0;
+    while (r >= ctx->cfg.tol && n < ctx->cfg.max_vcycles) {
+      rc = vcycle(ctx, ng);
+      if (rc) return rc;
+      fine_sweeps += ctx->s.npre + ctx->s.npost;
+      n++;
+      rc = relres_host(ctx, &r);
+      if (rc) return rc;
+    }
+    s.vcycles = n;
+    s.relres = r;
+    s.converged = r < ctx->cfg.tol;
+    ctx->s.last_vcycles = n;
+    ctx->s.last_relres = r;
+    ctx->s.last_relres_fmg = s.relres_init;
+  } else if (ctx->cfg.mode != DSG_MODE_REF_EXACT) {
+    return dsg::set_error(ctx, DSG_E_ARG, "pressure mode %d is not available in this build", ctx->cfg.mode);
+  }
+  s.fine_sweeps = fine_sweeps;
+  if (stats) *stats = s;
+  if (ctx->cfg.mode == DSG_MODE_TOL_FP64 && !s.converged)
+    return dsg::set_error(ctx, DSG_E_NOT_CONVERGED, "multigrid reached %d V-cycles at relres %.3e > tol %.3e",
+                          s.vcycles, s.relres, ctx->cfg.tol);
+  return DSG_OK;
+}
+
+}  // namespace
+
+// ============================================================================
+// C ABI
+// ============================================================================
+extern "C" {
+
+const char *dsg_last_error(const dsg_ctx *ctx) { return ctx ? ctx->err.c_str() : g_last_error.c_str(); }
+
+int dsg_create(const dsg_config *cfg, dsg_ctx **out) {
+  if (!cfg || !out) return dsg::set_error(nullptr, DSG_E_ARG, "null argument");
+  *out = nullptr;
+  if (cfg->nx < 4 || cfg->ny < 4 || cfg->nz < 4)
+    return dsg::set_error(nullptr, DSG_E_ARG, "grid %dx%dx%d too small", cfg->nx, cfg->ny, cfg->nz);
+  if (cfg->mode < 0 || cfg->mode > DSG_MODE_LEARNED)
+    return dsg::set_error(nullptr, DSG_E_ARG, "unknown mode %d", cfg->mode);
+  // memoryaloc, main.f:284-298
+  int nn = cfg->nx < cfg->ny ? cfg->nx : cfg->ny;
+  nn = nn < cfg->nz ? nn : cfg->nz;
+  int j = nn - 2, ng = 1;
+  while (j > 2) {
+    j /= 2;
+    ng++;
+  }
+  if ((1 << ng) + 2 != nn || ng > 30)
+    return dsg::set_error(nullptr, DSG_E_ARG, "STOP: nn .ne. 2**ng + 2 (%d vs %d)", nn, (1 << ng) + 2);
+  dsg_ctx *ctx = new dsg_ctx();
+  ctx->cfg = *cfg;
+  ctx->nx = cfg->nx;
+  ctx->ny = cfg->ny;
+  ctx->nz = cfg->nz;
+  ctx->ng = ng;
+  memset(&ctx->s, 0, sizeof ctx->s);
+  int nnx = cfg->nx, nny = cfg->ny, nnz = cfg->nz;
+  size_t total = 0;
+  auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  for (int l = ng; l >= 1; l--) {
+    ctx->lnx[l] = nnx;
+    ctx->lny[l] = nny;
+    ctx->lnz[l] = nnz;
+    total += 8 * up((size_t)nnx * nny * nnz * sizeof(double));
+    nnx = nnx / 2 + 1;
+    nny = nny / 2 + 1;
+    nnz = nnz / 2 + 1;
+  }
+  const size_t fine = up((size_t)cfg->nx * cfg->ny * cfg->nz * sizeof(double));
+  const int nextra = DSG_NFIELDS - 8 + 1;  // fine fields beyond the level arrays + ccf
+  total += nextra * fine;
+  total += up(dsg::kRedBlocks * 4 * sizeof(double)) + up(16 * sizeof(double));
+  cudaError_t e = cudaMalloc(&ctx->arena, total);
+  if (e != cudaSuccess) {
+    int rc = dsg::cuda_fail(ctx, e, "cudaMalloc(arena)");
+    g_last_error = ctx->err;
+    delete ctx;
+    return rc;
+  }
+  ctx->arena_bytes = total;
+  char *p = (char *)ctx->arena;
+  for (int l = ng; l >= 1; l--)
+    for (int f = 0; f < 8; f++) {
+      ctx->lv[l][f] = (double *)p;
+      p += up((size_t)ctx->lnx[l] * ctx->lny[l] * ctx->lnz[l] * sizeof(double));
+    }
+  for (int f = 0; f < 8; f++) ctx->f[f] = ctx->lv[ng][f];
+  for (int f = 8; f < DSG_NFIELDS; f++) {
+    ctx->f[f] = (double *)p;
+    p += fine;
+  }
+  ctx->ccf = (double *)p;
+  p += fine;
+  ctx->red_partials = (double *)p;
+  p += up(dsg::kRedBlocks * 4 * sizeof(double));
+  ctx->red_out = (double *)p;
+  e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMallocHost(&ctx->red_host, 16 * sizeof(double));
+  if (e == cudaSuccess) e = cudaMemsetAsync(ctx->arena, 0, total, ctx->own_stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->own_stream);
+  if (e != cudaSuccess) {
+    int rc = dsg::cuda_fail(ctx, e, "context setup");
+    g_last_error = ctx->err;
+    dsg_destroy(ctx);
+    return rc;
+  }
+  ctx->stream = ctx->own_stream;
+  ctx->s.npre = cfg->npre;
+  ctx->s.npost = cfg->npost;
+  ctx->s.ntop = cfg->ntop;
+  ctx->s.cycles = cfg->cycles;
+  ctx->s.ng = ng;
+  ctx->s.last_epsdiv = -1.0;
+  nondim(ctx);
+  *out = ctx;
+  return DSG_OK;
+}
+
+void dsg_destroy(dsg_ctx *ctx) {
+  if (!ctx) return;
+  if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
+  for (cudaEvent_t e : ctx->prof_ev) cudaEventDestroy(e);
+  if (ctx->arena) cudaFree(ctx->arena);
+  if (ctx->red_host) cudaFreeHost(ctx->red_host);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+  delete ctx;
+}
+
+int dsg_set_stream(dsg_ctx *ctx, void *stream) {
+  if (!ctx) return DSG_E_ARG;
+  ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+  return DSG_OK;
+}
+
+int dsg_synchronize(dsg_ctx *ctx) {
+  if (!ctx) return DSG_E_ARG;
+  DSG_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  return DSG_OK;
+}
+
+int64_t dsg_device_bytes(const dsg_ctx *ctx) { return ctx ? (int64_t)ctx->arena_bytes : 0; }
+
+int dsg_upload(dsg_ctx *ctx, int field, const double *host) {
+  if (!ctx || !host || field < 0 || field >= DSG_NFIELDS) return dsg::set_error(ctx, DSG_E_ARG, "bad upload");
+  DSG_CK(ctx, cudaMemcpyAsync(ctx->f[field], host, ctx->fine().count() * sizeof(double), cudaMemcpyHostToDevice,
+                              ctx->stream));
+  DSG_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  return DSG_OK;
+}
+
+int dsg_download(dsg_ctx *ctx, int field, double *host) {
+  if (!ctx || !host || field < 0 || field >= DSG_NFIELDS) return dsg::set_error(ctx, DSG_E_ARG, "bad download");
+  DSG_CK(ctx, cudaMemcpyAsync(host, ctx->f[field], ctx->fine().count() * sizeof(double), cudaMemcpyDeviceToHost,
+                              ctx->stream));
+  DSG_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  return DSG_OK;
+}
+
+int dsg_level_ptr(dsg_ctx *ctx, int field, int level, double **dev, int *nx, int *ny, int *nz) {
+  if (!ctx || field < 0 || field > 7 || level < 1 || level > ctx->ng || !dev)
+    return dsg::set_error(ctx, DSG_E_ARG, "bad level field");
+  *dev = ctx->lv[level][field];
+  if (nx) *nx = ctx->lnx[level];
+  if (ny) *ny = ctx->lny[level];
+  if (nz) *nz = ctx->lnz[level];
+  return DSG_OK;
+}
+
+int dsg_field_ptr(dsg_ctx *ctx, int field, double **dev) {
+  if (!ctx || field < 0 || field >= DSG_NFIELDS || !dev) return dsg::set_error(ctx, DSG_E_ARG, "bad field");
+  *dev = ctx->f[field];
+  return DSG_OK;
+}
+
+int dsg_get_scalars(const dsg_ctx *ctx, dsg_scalars *out) {
+  if (!ctx || !out) return DSG_E_ARG;
+  *out = ctx->s;
+  return DSG_OK;
+}
+
+int dsg_set_scalars(dsg_ctx *ctx, const dsg_scalars *in) {
+  if (!ctx || !in) return DSG_E_ARG;
+  const int ng = ctx->s.ng;
+  ctx->s = *in;
+  ctx->s.ng = ng;
+  return DSG_OK;
+}
+
+int dsg_init_drop(dsg_ctx *ctx) {
+  if (!ctx) return DSG_E_ARG;
+  dsg_scalars &s = ctx->s;
+  const Dims d = ctx->fine();
+  // smooth2 geometry (main.f:5684-5691)
+  const double x0 = (ctx->nx - 2) * s.h / 4.0;
+  if (ctx->cfg.z0_si != 1000.0) s.z0 = ctx->cfg.z0_si / ctx->cfg.length_si;
+  if (ctx->cfg.y0_si != 1000.0) s.y0 = ctx->cfg.y0_si / ctx->cfg.length_si;
+  s.y0 = s.y0 + s.h / 2.0;
+  const double amp = ctx->cfg.noise_si / s.vscale;
+  DSG_CK(ctx, dsg::init_drop(ctx->f[DSG_F_CC], ctx->f[DSG_F_U], ctx->f[DSG_F_V], ctx->f[DSG_F_W], d, s.h, x0,
+                             s.y0, s.z0, s.radius, s.yvel1, s.yvel2, s.zvel1, s.zvel2, amp, ctx->cfg.noise_seed,
+                             ctx->stream));
+  DSG_CK(ctx, dsg::bc_c(ctx->f[DSG_F_CC], d, ctx->stream));
+  DSG_CK(ctx, dsg::bc_v(ctx->f[DSG_F_U], ctx->f[DSG_F_V], ctx->f[DSG_F_W], ctx->red_partials, d, s.xvel2,
+                        ctx->stream));
+  DSG_CK(ctx, dsg::calcrho(ctx->f[DSG_F_RHON], ctx->f[DSG_F_MUN], ctx->f[DSG_F_CC], d, s.rho1, s.rho2, s.mu1,
+                           s.mu2, ctx->stream));
+  DSG_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  return DSG_OK;
+}
+
+int dsg_vofmethod(dsg_ctx *ctx) {
+  if (!ctx) return DSG_E_ARG;
+  dsg_scalars &s = ctx->s;
+  const Dims d = ctx->fine();
+  double *cc = ctx->f[DSG_F_CC], *s1 = ctx->f[DSG_F_EI], *s2 = ctx->f[DSG_F_RES], *s3 = ctx->f[DSG_F_RHS];
+  double *vel[4] = {nullptr, ctx->f[DSG_F_U], ctx->f[DSG_F_V], ctx->f[DSG_F_W]};
+  s.tswap = s.tswap + 1;
+  if (s.tswap > 3) s.tswap = 1;
+  int order[3];
+  if (s.tswap % 3 == 0) { order[0] = 3; order[1] = 1; order[2] = 2; }
+  else if (s.tswap % 2 == 0) { order[0] = 2; order[1] = 3; order[2] = 1; }
+  else { order[0] = 1; order[1] = 2; order[2] = 3; }
+  for (int q = 0; q < 3; q++)
+    DSG_CK(ctx, dsg::swp(vel[order[q]], cc, s1, s2, s3, order[q], d, s.tauh, ctx->stream));
+  DSG_CK(ctx, dsg::bc_c(cc, d, ctx->stream));
+  DSG_CK(ctx, dsg::calcrho(ctx->f[DSG_F_RHON], ctx->f[DSG_F_MUN], cc, d, s.rho1, s.rho2, s.mu1, s.mu2,
+                           ctx->stream));
+  return DSG_OK;
+}
+
+int dsg_checktime(dsg_ctx *ctx) {
+  if (!ctx) return DSG_E_ARG;
+  dsg_scalars &s = ctx->s;
+  DSG_CK(ctx, dsg::absmax3(ctx->red_out, ctx->red_partials, ctx->f[DSG_F_U], ctx->f[DSG_F_V], ctx->f[DSG_F_W],
+                           ctx->fine(), ctx->stream));
+  int rc = read_device(ctx, 1);
+  if (rc) return rc;
+  double cfl1 = ctx->red_host[0] * s.tauh;
+  if (!isfinite(cfl1)) return dsg::set_error(ctx, DSG_E_NONFINITE, "non-finite velocity in CFL");
+  const double maxcfl = ctx->cfg.maxcfl;
+  if (cfl1 > maxcfl) {
+    s.tau = s.tau * (maxcfl * (double)0.8f) / cfl1;
+    s.tauh = s.tau / s.h;
+    s.tauh2 = (int)(s.tau / (s.h * s.h));
+  }
+  if (cfl1 <= maxcfl * (double)0.25f) {
+    cfl1 = maxcfl * (double)0.5f;
+    s.tau = s.tau * (maxcfl * (double)0.5f) / cfl1;
+    s.tauh = s.tau / s.h;
+    s.tauh2 = (int)(s.tau / (s.h * s.h));
+  }
+  s.time = s.time + s.tau;
+  return DSG_OK;
+}
+
+int dsg_csf(dsg_ctx *ctx) {
+  if (!ctx) return DSG_E_ARG;
+  Tensor S(ctx);
+  DSG_CK(ctx, dsg::csf(ctx->f[DSG_F_CC], ctx->f[DSG_F_P], ctx->f[DSG_F_RES], ctx->f[DSG_F_RHS], ctx->ccf, S.p,
+                       ctx->fine(), ctx->s.tau, ctx->s.sigma, ctx->s.h, ctx->stream));
+  return DSG_OK;
+}
+
+int dsg_mglin(dsg_ctx *ctx, dsg_mg_stats *stats) {
+  if (!ctx) return DSG_E_ARG;
+  return mglin(ctx, stats);
+}
+
+int dsg_solvelpres(dsg_ctx *ctx, int t, dsg_mg_stats *stats) {
+  if (!ctx) return DSG_E_ARG;
+  dsg_scalars &s = ctx->s;
+  const Dims d = ctx->fine();
+  cudaStream_t st = ctx->stream;
+  double *cc = ctx->f[DSG_F_CC], *w1 = ctx->f[DSG_F_P], *w2 = ctx->f[DSG_F_RES], *w3 = ctx->f[DSG_F_RHS];
+  double *a = ctx->f[DSG_F_A], *b = ctx->f[DSG_F_B], *c = ctx->f[DSG_F_C], *ei = ctx->f[DSG_F_EI];
+  double *u = ctx->f[DSG_F_U], *v = ctx->f[DSG_F_V], *w = ctx->f[DSG_F_W];
+  Tensor S(ctx);
+  const double tauh2 = (double)s.tauh2, mu1 = s.mu1, mu2 = s.mu2;
+  const double r20 = tauh2 * mu2;
+  const double r10 = 0.25 * tauh2 * (mu1 - mu2);
+  double r1 = 2.0 * tauh2 * (mu1 - mu2);
+  double r2 = 2.0 * tauh2 * mu2;
+  const double stdgrav = s.g * (s.tau * s.tau) / s.h;
+  const double horgrav = s.g1 * (s.tau * s.tau) / s.h;
+  DSG_CK(ctx, dsg::stress(S.p, u, v, w, cc, d, r1, r2, r10, r20, st));
+  DSG_CK(ctx, dsg::bc_tensor(S.p, d, st));
+  r2 = s.rho2;
+  r1 = 0.5 * (s.rho1 - s.rho2);
+  DSG_CK(ctx, dsg::abcei(a, b, c, ei, cc, r1, r2, d, st));
+  DSG_CK(ctx, dsg::predictor(w1, w2, w3, u, v, w, a, b, c, S.p, d, horgrav, stdgrav, st));
+  DSG_CK(ctx, dsg::bc_w(w1, w2, w3, u, v, w, ctx->red_partials, d, st));
+  DSG_CK(ctx, dsg::convective(u, v, w, w1, w2, w3, d, s.tauh, ctx->cfg.convectype, st));
+  DSG_CK(ctx, dsg::bc_v(u, v, w, ctx->red_partials, d, s.xvel2, st));
+  const double hi2 = 1.0 / (s.h * s.h);
+  DSG_CK(ctx, dsg::divergence(w3, u, v, w, d, hi2, st));
+  dsg_mg_stats ms;
+  memset(&ms, 0, sizeof ms);
+  int rc = mglin(ctx, &ms);
+  if (rc && rc != DSG_E_NOT_CONVERGED) return rc;
+  const int mg_rc = rc;
+  DSG_CK(ctx, cudaMemcpyAsync(ctx->f[DSG_F_PPREV], w1, d.count() * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  DSG_CK(ctx, dsg::project(u, v, w, w1, a, b, c, d, st));
+  DSG_CK(ctx, dsg::bc_v(u, v, w, ctx->red_partials, d, s.xvel2, st));
+  ms.epsdiv = -1.0;
+  s.last_epsdiv = -1.0;
+  if (t <= 1 || t % 10 == 0) {
+    // relaxation-count adaptivity, main.f:3389-3416
+    DSG_CK(ctx, dsg::divergence(w3, u, v, w, d, hi2, st));
+    DSG_CK(ctx, dsg::absmax3(ctx->red_out, ctx->red_partials, w3, nullptr, nullptr, d, st));
+    rc = read_device(ctx, 1);
+    if (rc) return rc;
+    const double epsdiv = s.h * ctx->red_host[0];
+    ms.epsdiv = epsdiv;
+    s.last_epsdiv = epsdiv;
+    if (epsdiv > 25.0 && s.ntop < 30) {
+      s.ntop += 2;
+      s.npre += 2;
+      s.npost += 2;
+    } else if (epsdiv < 2.5 && s.ntop > 4) {
+      s.npre -= 1;
+      s.ntop -= 1;
+      s.npost -= 1;
+    }
+  }
+  if (ctx->cfg.tprint > 0 && t % ctx->cfg.tprint == 0) DSG_CK(ctx, dsg::divergence(w3, u, v, w, d, hi2, st));
+  if (stats) *stats = ms;
+  return mg_rc;
+}
+
+int dsg_step(dsg_ctx *ctx, int t, dsg_mg_stats *stats) {
+  if (!ctx) return DSG_E_ARG;
+  int rc = dsg_vofmethod(ctx);
+  if (rc) return rc;
+  rc = dsg_checktime(ctx);
+  if (rc) return rc;
+  rc = dsg_csf(ctx);
+  if (rc) return rc;
+  return dsg_solvelpres(ctx, t, stats);
+}
+
+int dsg_liquid_volume(dsg_ctx *ctx, double *out) {
+  if (!ctx || !out) return DSG_E_ARG;
+  DSG_CK(ctx, dsg::sumfield(ctx->red_out, ctx->red_partials, ctx->f[DSG_F_CC], ctx->fine(), ctx->stream));
+  int rc = read_device(ctx, 1);
+  if (rc) return rc;
+  *out = ctx->red_host[0];
+  if (!isfinite(*out)) return dsg::set_error(ctx, DSG_E_NONFINITE, "non-finite liquid volume");
+  return DSG_OK;
+}
+
+int dsg_max_divergence(dsg_ctx *ctx, double *out) {
+  if (!ctx || !out) return DSG_E_ARG;
+  const double hi2 = 1.0 / (ctx->s.h * ctx->s.h);
+  DSG_CK(ctx, dsg::divmax(ctx->red_out, ctx->red_partials, ctx->f[DSG_F_U], ctx->f[DSG_F_V], ctx->f[DSG_F_W], hi2,
+                          ctx->fine(), ctx->stream));
+  int rc = read_device(ctx, 1);
+  if (rc) return rc;
+  *out = ctx->s.h * ctx->red_host[0];
+  return DSG_OK;
+}
+
+int dsg_relres(dsg_ctx *ctx, double *out) {
+  if (!ctx || !out) return DSG_E_ARG;
+  return relres_host(ctx, out);
+}
+
+int dsg_profile_enable(dsg_ctx *ctx, int on) {
+  if (!ctx) return DSG_E_ARG;
+  DSG_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  ctx->prof = on != 0;
+  ctx->prof_used = 0;
+  ctx->prof_relax_calls = 0;
+  ctx->prof_relax_bytes = 0.0;
+  ctx->prof_launch0 = dsg::g_launches.load();
+  return DSG_OK;
+}
+
+int dsg_profile_read(dsg_ctx *ctx, dsg_profile *out) {
+  if (!ctx || !out) return DSG_E_ARG;
+  DSG_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  double ms = 0.0;
+  for (size_t q = 0; q + 1 < ctx->prof_used; q += 2) {
+    float x = 0.f;
+    DSG_CK(ctx, cudaEventElapsedTime(&x, ctx->prof_ev[q], ctx->prof_ev[q + 1]));
+    ms += x;
+  }
+  out->launches = dsg::g_launches.load() - ctx->prof_launch0;
+  out->relax_calls = ctx->prof_relax_calls;
+  out->relax_ms = ms;
+  out->relax_bytes = ctx->prof_relax_bytes;
+  return DSG_OK;
+}
+
+int64_t dsg_launch_count(void) { return dsg::g_launches.load(); }
+
+}  // extern "C"

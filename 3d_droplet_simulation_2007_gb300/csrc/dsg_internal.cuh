@@ -1,0 +1,151 @@
+// dsg_internal.cuh -- shared device helpers, launch helpers and the context
+// structure of the GB300 projection hot path.  Not part of the public ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include <atomic>
+#include <string>
+#include <vector>
+
+#include "../../include/dsg.h"
+
+namespace dsg {
+
+// Every kernel launch of the library goes through DSG_COUNT so that the
+// number of launches in a timed region can be reported.
+extern std::atomic<long long> g_launches;
+#define DSG_COUNT dsg::g_launches.fetch_add(1, std::memory_order_relaxed),
+
+// Column-major, 1-based (i,j,k) -> linear offset of an (nx,ny,nz) array.
+struct Dims {
+  int nx, ny, nz;
+  __host__ __device__ __forceinline__ size_t ix(int i, int j, int k) const {
+    return (size_t)(i - 1) + (size_t)nx * ((size_t)(j - 1) + (size_t)ny * (size_t)(k - 1));
+  }
+  __host__ __device__ __forceinline__ size_t count() const { return (size_t)nx * ny * nz; }
+  __host__ __device__ __forceinline__ int sx() const { return 1; }
+  __host__ __device__ __forceinline__ int sy() const { return nx; }
+  __host__ __device__ __forceinline__ size_t sz() const { return (size_t)nx * ny; }
+};
+
+__device__ __forceinline__ double dmax1(double a, double b) { return a >= b ? a : b; }
+__device__ __forceinline__ double dmin1(double a, double b) { return a <= b ? a : b; }
+
+// Grid over the interior (2..n-1)^3 with 32 x 4 thread blocks, one z plane per
+// grid row in z.
+inline dim3 interior_grid(const Dims &d, dim3 blk) {
+  return dim3((unsigned)((d.nx - 2 + blk.x - 1) / blk.x), (unsigned)((d.ny - 2 + blk.y - 1) / blk.y),
+              (unsigned)(d.nz - 2));
+}
+
+// Number of blocks of the deterministic reductions (fixed so that results do
+// not depend on the device).
+constexpr int kRedBlocks = 1216;  // 8 x 152 SMs
+constexpr int kRedThreads = 256;
+
+// ---- host-side launch helpers (implemented in the kernel .cu files) -------
+// All return cudaGetLastError() of the launches.
+cudaError_t bc_scalar(double *s, Dims d, cudaStream_t st);
+cudaError_t bc_resid(double *s, Dims d, cudaStream_t st);
+cudaError_t bc_out(double *s, Dims d, cudaStream_t st);
+cudaError_t relax(double *u, double lengthsize, const double *rhs, const double *a, const double *b,
+                  const double *c, const double *ei, Dims d, double omega, cudaStream_t st);
+cudaError_t relax_n(int n, double *u, double lengthsize, const double *rhs, const double *a,
+                    const double *b, const double *c, const double *ei, Dims d, double omega,
+                    cudaStream_t st);
+cudaError_t resid(double lengthsize, double *res, const double *u, const double *rhs, const double *a,
+                  const double *b, const double *c, Dims d, cudaStream_t st);
+cudaError_t rstrct(double *uc, const double *uf, Dims dc, cudaStream_t st);
+cudaError_t interp(double *uf, const double *uc, Dims df, cudaStream_t st);
+cudaError_t addint(double *uf, const double *uc, double *res, Dims df, cudaStream_t st);
+cudaError_t acfromac(double *a, double *b, double *c, double *ei, const double *a2, const double *b2,
+                     const double *c2, Dims dc, cudaStream_t st);
+cudaError_t abcei(double *a, double *b, double *c, double *ei, const double *cc, double r1, double r2,
+                  Dims d, cudaStream_t st);
+cudaError_t filterc27(const double *cc, double *cf, Dims d, cudaStream_t st);
+// relres partial sums: out[0] = sum r^2, out[1] = sum rhs^2 (device, 2 doubles)
+cudaError_t relres_sums(double *out, double *partials, double lengthsize, const double *u,
+                        const double *rhs, const double *a, const double *b, const double *c, Dims d,
+                        cudaStream_t st);
+// out[0] = interior sum of f (SUMFIELD order-independent tree sum)
+cudaError_t sumfield(double *out, double *partials, const double *f, Dims d, cudaStream_t st);
+// out[0] = max |f| over the interior
+cudaError_t absmax3(double *out, double *partials, const double *f0, const double *f1,
+                    const double *f2, Dims d, cudaStream_t st);
+// out[0] = max |div u| * hi2 over the interior (FMODMAX of the divergence)
+cudaError_t divmax(double *out, double *partials, const double *u, const double *v, const double *w,
+                   double hi2, Dims d, cudaStream_t st);
+cudaError_t fill_zero(double *f, size_t n, cudaStream_t st);
+
+// vof.cu
+cudaError_t bc_c(double *cc, Dims d, cudaStream_t st);
+cudaError_t swp(const double *us, double *cc, double *vof1, double *vof2, double *vof3, int dir, Dims d,
+                double tauh, cudaStream_t st);
+cudaError_t calcrho(double *rhon, double *mun, const double *cc, Dims d, double rho1, double rho2,
+                    double mu1, double mu2, cudaStream_t st);
+// csf.cu (S = {S11,S22,S33,S12,S13,S23})
+cudaError_t bc_tensor(double *const S[6], Dims d, cudaStream_t st);
+cudaError_t csf(const double *ccc, double *w11, double *w22, double *w33, double *ccf, double *const S[6],
+                Dims d, double tau, double sigma, double h, cudaStream_t st);
+// momentum.cu
+cudaError_t bc_v(double *u, double *v, double *w, double *partials, Dims d, double xvel2, cudaStream_t st);
+cudaError_t bc_w(double *w1, double *w2, double *w3, const double *u, const double *v, const double *w,
+                 double *partials, Dims d, cudaStream_t st);
+cudaError_t stress(double *const S[6], const double *u, const double *v, const double *w, const double *cc,
+                   Dims d, double r1, double r2, double r10, double r20, cudaStream_t st);
+cudaError_t predictor(double *w1, double *w2, double *w3, const double *u, const double *v, const double *w,
+                      const double *a, const double *b, const double *c, double *const S[6], Dims d,
+                      double horgrav, double stdgrav, cudaStream_t st);
+cudaError_t convective(double *u, double *v, double *w, const double *w1, const double *w2, const double *w3,
+                       Dims d, double tauh, int convectype, cudaStream_t st);
+cudaError_t divergence(double *out, const double *u, const double *v, const double *w, Dims d, double hi2,
+                       cudaStream_t st);
+cudaError_t project(double *u, double *v, double *w, const double *p, const double *a, const double *b,
+                    const double *c, Dims d, cudaStream_t st);
+// init.cu
+cudaError_t init_drop(double *cc, double *u, double *v, double *w, Dims d, double h, double x0, double y0,
+                      double z0, double radius, double yvel1, double yvel2, double zvel1, double zvel2,
+                      double noise_amp, uint64_t seed, cudaStream_t st);
+
+}  // namespace dsg
+
+// ---- context ---------------------------------------------------------------
+struct dsg_ctx {
+  dsg_config cfg;
+  dsg_scalars s;
+  int nx, ny, nz, ng;
+  int lnx[32], lny[32], lnz[32];
+  double *lv[32][8];          // [level][CC,P,RES,RHS,A,B,C,EI], level 1..ng
+  double *f[DSG_NFIELDS];     // fine fields; 0..7 alias lv[ng]
+  double *ccf;                // csf filtered volume fraction (local array of csf)
+  double *red_partials;       // reduction partials (kRedBlocks * 4 doubles)
+  double *red_out;            // device reduction results (8 doubles)
+  double *red_host;           // pinned host mirror of red_out
+  void *arena;
+  size_t arena_bytes;
+  cudaStream_t stream;
+  cudaStream_t own_stream;
+  std::string err;
+  // live profile of the finest-level relaxation (CUDA events on ctx->stream)
+  bool prof = false;
+  long long prof_launch0 = 0;
+  std::vector<cudaEvent_t> prof_ev;
+  size_t prof_used = 0;
+  long long prof_relax_calls = 0;
+  double prof_relax_bytes = 0.0;
+  dsg::Dims fine() const { return dsg::Dims{nx, ny, nz}; }
+  dsg::Dims level(int l) const { return dsg::Dims{lnx[l], lny[l], lnz[l]}; }
+};
+
+namespace dsg {
+int set_error(dsg_ctx *ctx, int code, const char *fmt, ...);
+int cuda_fail(dsg_ctx *ctx, cudaError_t e, const char *where);
+}  // namespace dsg
+
+#define DSG_CK(ctx, expr)                                   \
+  do {                                                      \
+    cudaError_t _e = (expr);                                \
+    if (_e != cudaSuccess) return dsg::cuda_fail((ctx), _e, #expr); \
+  } while (0)

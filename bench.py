@@ -1,0 +1,311 @@
+#!/usr/bin/env python
+"""Benchmark: time-steps/s of the droplet projection hot path at 256^3.
+
+Workload: the splash-on-wall case, 256^3 interior cells (258^3 nodes), 3 m/s
+impact, 4 pre/4 post red-black sweeps, laminar (k-epsilon is not part of this
+build), pressure solved to 1e-8 relative residual.  A "step" is one body of the
+main.f time loop (VOF advection, CFL check, CSF force, momentum + pressure
+projection) with every field resident in HBM.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Prints one JSON line.  With N>1 (torchrun) every rank advances its own
+independent droplet replica (weak scaling, no collective on the data path).
+``--impl reference`` times the CPU reference restatement (the oracle: plain
+FP64 multigrid to the same tolerance, single thread) on the same workload.
+"""
+import argparse
+import importlib
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+PKG = "3d_droplet_simulation_2007_gb300"
+
+METRIC = "time-steps/s at 256^3, plain FP64 MG vs FP32-refined+learned warm-start, 1e-8 resid"
+UNIT = "time-steps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=256, help="interior cells per side")
+    ap.add_argument("--mode", default="best", help="best|tol_fp64|tol_mixed|learned|ref_exact")
+    ap.add_argument("--tol", type=float, default=1e-8)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def workload(dsg, n, mode, tol):
+    cfg = dsg.config
+    return cfg.droplet(n, steps=1000, impact_speed=3.0, noise_si=1e-4, mode=mode, tol=tol,
+                       npre=4, npost=4, ntop=4)
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs"), "measured"
+    return 6800.0, "fallback"
+
+
+def committed_traffic(kernel, n):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, or None."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    e = d.get("%s@%d" % (kernel, n))
+    return None if e is None else e.get("dram_bytes_per_launch")
+
+
+class Clocks:
+    """nvidia-smi sampler over the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as f:
+            for ln in f:
+                parts = [x.strip() for x in ln.split(",")]
+                if len(parts) >= 8:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = sorted(float(r[0]) for r in rows if r[0].replace(".", "").isdigit())
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for nm, v in zip(names, r[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None,
+                "sm_max_mhz": float(rows[0][1]) if rows[0][1].replace(".", "").isdigit() else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def cpu_baseline(dsg, n, tol, steps=1):
+    """Single-threaded oracle (plain FP64 MG to tol) on a bounded sample."""
+    from oracle import Oracle
+    inp = workload(dsg, n, dsg.config.MODE_TOL_FP64, tol)
+    ora = Oracle(inp.as_dict())
+    t0 = time.perf_counter()
+    for t in range(1, steps + 1):
+        ora.step(t)
+    dt = time.perf_counter() - t0
+    return {"value": steps / dt, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": "%d time step(s) of the %d^3 workload from its initial condition, C oracle "
+                      "(plain FP64 FMG + V-cycles to %.0e), 1 thread, %.1f s" % (steps, n, tol, dt)}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    dsg = importlib.import_module(PKG)
+    steps = max(1, min(args.steps, 3))
+    cb = cpu_baseline(dsg, args.n, args.tol, steps=steps)
+    line = {"metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
+            "warmup": 0, "ms_per_step": 1e3 / cb["value"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "splash-on-wall droplet %d^3, 3 m/s, laminar, plain FP64 MG to %.0e"
+                                   % (args.n, args.tol)},
+            "impl": "reference", "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def mode_of(dsg, name):
+    names = dsg.config.MODE_NAMES
+    if name == "best":
+        return names["tol_fp64"]
+    return names[name]
+
+
+def time_steps(torch, solver, k, t0):
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    stats = []
+    for t in range(t0, t0 + k):
+        stats.append(solver.step(t))
+    e1.record(st)
+    e1.synchronize()
+    return e0.elapsed_time(e1), stats
+
+
+def run_gb300(args):
+    import numpy as np
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dsg = importlib.import_module(PKG)
+    dsg.load()
+    mode = mode_of(dsg, args.mode)
+    inp = workload(dsg, args.n, mode, args.tol)
+    solver = dsg.Solver(inp)
+    solver.set_stream(torch.cuda.current_stream().cuda_stream)
+    for t in range(1, args.warmup + 1):
+        solver.step(t)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    solver.profile_enable(True)
+    ms, stats = time_steps(torch, solver, args.steps, args.warmup + 1)
+    prof = solver.profile_read()
+    solver.profile_enable(False)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    ms_max = ms
+    if dist:
+        tt = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms_max = float(tt.item())
+    value = ws * args.steps / (ms_max / 1e3)
+    vcycles = [s["vcycles"] for s in stats]
+
+    # plain FP64 reference point of the metric (same replica, continued)
+    plain = None
+    if mode != dsg.config.MODE_TOL_FP64:
+        p_inp = workload(dsg, args.n, dsg.config.MODE_TOL_FP64, args.tol)
+        ps = dsg.Solver(p_inp)
+        ps.set_stream(torch.cuda.current_stream().cuda_stream)
+        for t in range(1, args.warmup + 1):
+            ps.step(t)
+        pms, pst = time_steps(torch, ps, args.steps, args.warmup + 1)
+        plain = {"value": args.steps / (pms / 1e3), "vcycles": [s["vcycles"] for s in pst]}
+        ps.close()
+
+    # end to end through the public API: pinned host state in, results out
+    e2e = None
+    if not args.no_e2e:
+        n_cells = inp.nx * inp.ny * inp.nz
+        ins = ["cc", "u", "v", "w", "s12", "s13", "s23"]
+        outs = ["p", "cc", "u", "v", "w"]
+        host = {}
+        for nm in set(ins + outs):
+            host[nm] = torch.empty(n_cells, dtype=torch.float64, pin_memory=True).numpy()
+        for nm in ins:
+            solver.download_into(nm, host[nm])
+        k2 = max(1, args.e2e_steps)
+        torch.cuda.synchronize()
+        t_start = time.perf_counter()
+        t = args.warmup + args.steps
+        for _ in range(k2):
+            t += 1
+            for nm in ins:
+                solver.upload(nm, host[nm])
+            solver.step(t)
+            for nm in outs:
+                solver.download_into(nm, host[nm])
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t_start
+        e2e = {"value": ws * k2 / el, "unit": UNIT, "h2d_bytes_per_step": len(ins) * n_cells * 8,
+               "d2h_bytes_per_step": len(outs) * n_cells * 8}
+    solver.close()
+
+    if rank == 0:
+        peak, peak_kind = measured_peaks()
+        achieved = None
+        if prof["relax_calls"]:
+            per_call_ms = prof["relax_ms"] / prof["relax_calls"]
+            per_call_bytes = prof["relax_bytes"] / prof["relax_calls"]
+            achieved = per_call_bytes / (per_call_ms / 1e3) / 1e9
+        traffic = committed_traffic("relax_fp64", args.n)
+        roof = {"bound": "hbm", "kernel": "finest-level relax (2 red-black colour passes, FP64)",
+                "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                "peak_kind": peak_kind,
+                "bytes_per_launch": (prof["relax_bytes"] / prof["relax_calls"]) if prof["relax_calls"] else None,
+                "share_of_step": (prof["relax_ms"] / ms) if ms else None}
+        cb = None
+        if ws == 1 and not args.no_cpu_baseline:
+            cb = cpu_baseline(dsg, args.n, args.tol, steps=1)
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": "splash-on-wall droplet %d^3 cells (%d^3 nodes), 3 m/s, laminar, "
+                                       "4/4 RBGS sweeps, pressure to %.0e relative residual"
+                                       % (args.n, args.n + 2, args.tol),
+                           "mode": [k for k, v in dsg.config.MODE_NAMES.items() if v == mode][0],
+                           "l2": "per-step working set %.1f GB >> 129 MB L2 (no flush needed)"
+                                 % (solver_bytes_estimate(inp) / 1e9),
+                           "parallelism": "replicas" if ws > 1 else "single"},
+                "vcycles_per_step": vcycles, "gpu_launches": prof["launches"], "roofline": roof,
+                "cpu_baseline": cb, "e2e": e2e, "clocks": clk}
+        if plain:
+            line["plain_fp64"] = plain
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def solver_bytes_estimate(inp):
+    return 20.0 * inp.nx * inp.ny * inp.nz * 8
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,194 @@
+/*
+ * dsg.h -- C ABI of the GB300-native projection hot path of the 3D VOF
+ * droplet solver (farzan-t/3D_Droplet_simulation_2007).
+ *
+ * Two layers of entry points, both plain C (no C++ or torch types):
+ *
+ *  1. Resident-state API (dsg_create ... dsg_step).  A context owns every
+ *     field of the reference COMMON blocks in HBM (one device arena) and runs
+ *     the routines of main.f's time loop on one CUDA stream.  This is what the
+ *     Fortran driver binds through ISO_C_BINDING in place of VOFmethod, csf,
+ *     solvelpres and mglin.
+ *  2. Array-level kernels (dsg_relax ... dsg_filterc27) with the argument
+ *     lists of the reference subroutines, operating on caller-owned DEVICE
+ *     arrays on a caller-given stream.
+ *
+ * Arrays: Fortran column-major A(nx,ny,nz), FP64 unless stated, one ghost layer
+ * on every side (interior 2..n-1), exactly the layout of main.f.  Every function
+ * returns DSG_OK (0) or a negative DSG_E* code and never aborts the process;
+ * dsg_last_error() gives the message.  A context is not re-entrant: one host
+ * thread per context.  Several contexts may coexist.
+ */
+#ifndef DSG_H
+#define DSG_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DSG_OK 0
+#define DSG_E_ARG (-1)          /* invalid argument / size */
+#define DSG_E_CUDA (-2)         /* CUDA runtime error */
+#define DSG_E_NOMEM (-3)        /* device allocation failed */
+#define DSG_E_NOT_CONVERGED (-4) /* multigrid hit its V-cycle cap before tol */
+#define DSG_E_NONFINITE (-5)    /* NaN/Inf found in a residual or volume reduction */
+#define DSG_E_STATE (-6)        /* call out of order (e.g. no net loaded) */
+
+/* Pressure solver modes. */
+#define DSG_MODE_REF_EXACT 0 /* mglin as the reference: FMG, fixed `cycles`, no residual test */
+#define DSG_MODE_TOL_FP64 1  /* the same FMG, then FP64 V-cycles until relres < tol */
+#define DSG_MODE_TOL_MIXED 2 /* FP64 defect correction around FP32 V-cycles, to tol */
+#define DSG_MODE_LEARNED 3   /* TOL_MIXED, initial guess from the learned net (guarded) */
+
+/* Fine-level field identifiers (memoryaloc main.f:300-317 order, then the
+ * COMMON /surfcom/ and /PHYSICS/ arrays of input.h:31-36, 84-90). */
+enum {
+  DSG_F_CC = 0,  /* z(icc(ng)): volume fraction */
+  DSG_F_P = 1,   /* z(iu(ng)): pressure (also scratch of csf/solvelpres, as in the reference) */
+  DSG_F_RES = 2, /* z(ires(ng)) */
+  DSG_F_RHS = 3, /* z(irhs(ng)) */
+  DSG_F_A = 4, DSG_F_B = 5, DSG_F_C = 6, DSG_F_EI = 7,
+  DSG_F_U = 8, DSG_F_V = 9, DSG_F_W = 10,
+  DSG_F_S11 = 11, DSG_F_S22 = 12, DSG_F_S33 = 13, DSG_F_S12 = 14, DSG_F_S13 = 15, DSG_F_S23 = 16,
+  DSG_F_RHON = 17, DSG_F_MUN = 18,
+  DSG_F_PPREV = 19, /* previous-step pressure (build addition: the reference keeps none) */
+  DSG_NFIELDS = 20
+};
+
+/* The 38 positional values of inputdata.in (main.f:188-234) in file order,
+ * then additions with no reference counterpart. */
+typedef struct dsg_config {
+  int nx, ny, nz, tmax, nfilter, cycles;
+  double omega;
+  int npre, ntop, npost, restart;
+  double maxcfl;
+  int iturb, convectype, hswitch;
+  double xvel1_si, yvel1_si, zvel1_si, xvel2_si, yvel2_si, zvel2_si;
+  double rho2_si, rho1_si, sigma_si, visc2_si, visc1_si, grav_si, grav1_si;
+  int icase, ibc;
+  double length_si, radius_si, y0_si, z0_si;
+  int tprint, ntecplot, tsave, surfacet;
+  /* additions */
+  int mode;            /* DSG_MODE_* */
+  double tol;          /* relative residual target of the tol modes */
+  int max_vcycles;     /* V-cycle / defect-correction cap of the tol modes */
+  double noise_si;     /* half-width of the seeded uniform velocity noise [m/s] */
+  uint64_t noise_seed; /* seed of the counter-based noise */
+} dsg_config;
+
+/* Non-dimensional scalars and adaptive counters (COMMON /PHYSICS/, /DIFF/,
+ * /CYCLING/, /dinem/). */
+typedef struct dsg_scalars {
+  double tau, tauh, time, h, rho1, rho2, mu1, mu2, sigma, g, g1;
+  double lengthsize, lengthscale, vscale, radius, y0, z0;
+  double xvel1, yvel1, zvel1, xvel2, yvel2, zvel2;
+  int tauh2; /* INTEGER in input.h:53-55: tau/h^2 truncated */
+  int npre, npost, ntop, cycles, tswap, ng;
+  int last_vcycles;
+  double last_relres, last_relres_fmg, last_epsdiv;
+} dsg_scalars;
+
+/* Result of one pressure solve. */
+typedef struct dsg_mg_stats {
+  int mode;           /* mode actually used (a fallback can lower it) */
+  int vcycles;        /* V-cycles (fp64 modes) or defect-correction sweeps (mixed) after the initial guess */
+  int fine_sweeps;    /* relax calls on the finest level */
+  double relres_init; /* relative residual of the initial guess (FMG or learned) */
+  double relres;      /* final relative residual (-1 in ref_exact mode) */
+  int converged;      /* 1 if relres < tol (tol modes) */
+  int fallback;       /* 1 if the learned guess was rejected for the previous-step pressure */
+  double epsdiv;      /* h*max|div| of the adaptivity check, -1 if not run this step */
+} dsg_mg_stats;
+
+typedef struct dsg_ctx dsg_ctx;
+
+/* ---- lifecycle ---------------------------------------------------------- */
+/* readinput + memoryaloc + nondim (main.f:185-446).  Allocates the device
+ * arena; requires min(nx,ny,nz) = 2^ng+2 (memoryaloc main.f:295-298). */
+int dsg_create(const dsg_config *cfg, dsg_ctx **out);
+void dsg_destroy(dsg_ctx *ctx);
+const char *dsg_last_error(const dsg_ctx *ctx); /* ctx may be NULL: last global error */
+int dsg_set_stream(dsg_ctx *ctx, void *cuda_stream); /* NULL = the context's own stream */
+int dsg_synchronize(dsg_ctx *ctx);
+/* Device bytes held by the context arena. */
+int64_t dsg_device_bytes(const dsg_ctx *ctx);
+
+/* ---- state transfer ----------------------------------------------------- */
+/* Copy a fine field (nx*ny*nz doubles, column-major) host <-> device. */
+int dsg_upload(dsg_ctx *ctx, int field, const double *host);
+int dsg_download(dsg_ctx *ctx, int field, double *host);
+/* Device pointer of a level array (field DSG_F_CC..DSG_F_EI, level 1..ng). */
+int dsg_level_ptr(dsg_ctx *ctx, int field, int level, double **dev_ptr, int *nx, int *ny, int *nz);
+int dsg_field_ptr(dsg_ctx *ctx, int field, double **dev_ptr);
+int dsg_get_scalars(const dsg_ctx *ctx, dsg_scalars *out);
+int dsg_set_scalars(dsg_ctx *ctx, const dsg_scalars *in);
+
+/* ---- time-step routines (main.f time loop, main.f:19-73) ----------------- */
+/* initialize, restart=0 drop case: smooth2 (+ seeded noise) + bc_c + bc_v +
+ * calcrho (main.f:159-178, 5678-5752). */
+int dsg_init_drop(dsg_ctx *ctx);
+/* VOFmethod(t) main.f:795-824 */
+int dsg_vofmethod(dsg_ctx *ctx);
+/* checktime(t) main.f:2152-2171 (one device max-reduction, one host read) */
+int dsg_checktime(dsg_ctx *ctx);
+/* csf(ccc,w11,w22,w33) main.f:2363-2481 */
+int dsg_csf(dsg_ctx *ctx);
+/* solvelpres(cc,w1..w3,a,b,c,ei,t) main.f:3236-3439, pressure solve per mode */
+int dsg_solvelpres(dsg_ctx *ctx, int t, dsg_mg_stats *stats);
+/* mglin(r1,r2) main.f:3645-3763 on the resident fine rhs and coefficients */
+int dsg_mglin(dsg_ctx *ctx, dsg_mg_stats *stats);
+/* One body of the main.f:19-73 loop with surfacet=2 (CSF), hswitch=0, laminar. */
+int dsg_step(dsg_ctx *ctx, int t, dsg_mg_stats *stats);
+/* SUMFIELD(cc) main.f:4783-4801: liquid volume (FP64, deterministic order) */
+int dsg_liquid_volume(dsg_ctx *ctx, double *out);
+/* h * FMODMAX(div u) on the resident velocity (main.f:3389-3398) */
+int dsg_max_divergence(dsg_ctx *ctx, double *out);
+/* ||rhs - L p||_2 / ||rhs||_2 on the fine interior (new: the reference has no norm) */
+int dsg_relres(dsg_ctx *ctx, double *out);
+
+/* ---- instrumentation ----------------------------------------------------- */
+typedef struct dsg_profile {
+  int64_t launches;    /* library kernel launches since dsg_profile_enable */
+  int64_t relax_calls; /* finest-level relax calls timed with CUDA events */
+  double relax_ms;     /* summed event time of those calls */
+  double relax_bytes;  /* their algorithmic bytes: 6 words (u r+w, a, b, c, rhs) per cell */
+} dsg_profile;
+/* Start (on=1, counters reset) or stop live profiling of the context. */
+int dsg_profile_enable(dsg_ctx *ctx, int on);
+/* Synchronize the context stream and report the counters. */
+int dsg_profile_read(dsg_ctx *ctx, dsg_profile *out);
+/* Total kernel launches made by the library in this process. */
+int64_t dsg_launch_count(void);
+
+/* ---- array-level kernels (device pointers, reference argument lists) ----
+ * `stream` is a cudaStream_t (NULL = legacy default stream). */
+/* relax main.f:3956-3997 */
+int dsg_relax(double *u, double lengthsize, const double *rhs, const double *a, const double *b,
+              const double *c, const double *ei, int nx, int ny, int nz, double omega, void *stream);
+/* resid main.f:3902-3931 (with bc_resid) */
+int dsg_resid(double lengthsize, double *res, const double *u, const double *rhs, const double *a,
+              const double *b, const double *c, int nx, int ny, int nz, void *stream);
+/* rstrct main.f:3765-3791: uc(ncx,ncy,ncz) from uf(2ncx-2, 2ncy-2, 2ncz-2) */
+int dsg_rstrct(double *uc, const double *uf, int ncx, int ncy, int ncz, void *stream);
+/* interp main.f:3866-3900: uf(nfx,nfy,nfz) from uc(nfx/2+1, ...) */
+int dsg_interp(double *uf, const double *uc, int nfx, int nfy, int nfz, void *stream);
+/* addint main.f:3934-3954 (res is scratch, as in the reference) */
+int dsg_addint(double *uf, const double *uc, double *res, int nfx, int nfy, int nfz, void *stream);
+/* acfromac main.f:3793-3844: coarse a,b,c,ei (nx,ny,nz) from fine a2,b2,c2 */
+int dsg_acfromac(double *a, double *b, double *c, double *ei, const double *a2, const double *b2,
+                 const double *c2, int nx, int ny, int nz, void *stream);
+/* abcei main.f:3582-3615 with bc_coef main.f:4465-4494 */
+int dsg_abcei(double *a, double *b, double *c, double *ei, const double *cc, double r1, double r2,
+              int nx, int ny, int nz, void *stream);
+/* bc_scalar main.f:4298-4329, bc_resid 4432-4463, bc_out 4399-4430 */
+int dsg_bc_scalar(double *s, int nx, int ny, int nz, void *stream);
+int dsg_bc_resid(double *s, int nx, int ny, int nz, void *stream);
+int dsg_bc_out(double *s, int nx, int ny, int nz, void *stream);
+/* filterc27 main.f:5473-5511 */
+int dsg_filterc27(const double *cc, double *cf, int nx, int ny, int nz, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
