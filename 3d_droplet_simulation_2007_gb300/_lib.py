@@ -64,7 +64,7 @@ class DsgScalars(C.Structure):
 class DsgProfile(C.Structure):
     """struct dsg_profile."""
     _fields_ = [("launches", C.c_int64), ("relax_calls", C.c_int64), ("relax_ms", C.c_double),
-                ("relax_bytes", C.c_double)]
+                ("relax_bytes", C.c_double), ("relax_bits", C.c_int)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}

@@ -17,6 +17,16 @@ __global__ void k_curvature(double *__restrict__ kap, const double *__restrict__
   const size_t q = d.ix(i, j, k);
   const long sy = (long)d.sy(), sz = (long)d.sz();
 #define F(di, dj, dk) f[q + (long)(di) + (long)(dj) * sy + (long)(dk) * sz]
+  // Uniform 19-point neighbourhood (bulk liquid or gas): every difference is
+  // +0, every d is 0/sqrt(1e-50) = +0 and kappa = -(+0) = -0 exactly.
+  const double f0 = F(0, 0, 0);
+  if (F(1, 0, 0) == f0 && F(-1, 0, 0) == f0 && F(0, 1, 0) == f0 && F(0, -1, 0) == f0 && F(0, 0, 1) == f0 &&
+      F(0, 0, -1) == f0 && F(1, 1, 0) == f0 && F(1, -1, 0) == f0 && F(-1, 1, 0) == f0 && F(-1, -1, 0) == f0 &&
+      F(1, 0, 1) == f0 && F(1, 0, -1) == f0 && F(-1, 0, 1) == f0 && F(-1, 0, -1) == f0 && F(0, 1, 1) == f0 &&
+      F(0, 1, -1) == f0 && F(0, -1, 1) == f0 && F(0, -1, -1) == f0) {
+    kap[q] = -0.0;
+    return;
+  }
   double t0, t1, t2;
   t0 = F(1, 0, 0) - F(0, 0, 0);
   t1 = F(0, 1, 0) - F(0, -1, 0) + F(1, 1, 0) - F(1, -1, 0);

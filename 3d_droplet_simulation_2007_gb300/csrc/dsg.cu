@@ -124,6 +124,7 @@ cudaError_t relax_level(dsg_ctx *ctx, int n, int jj, double ls) {
     ctx->prof_used += 2;
     ctx->prof_relax_calls += n;
     ctx->prof_relax_bytes += (double)n * 6.0 * sizeof(double) * (double)d.count();
+    ctx->prof_relax_bits = 64;
   }
   return e;
 }
@@ -164,11 +165,222 @@ int relres_host(dsg_ctx *ctx, double *out) {
   return DSG_OK;
 }
 
+// ---- mixed precision: FP32 V-cycles inside FP64 defect correction ---------
+enum { U32 = 0, RHS32 = 1, A32 = 2, B32 = 3, C32 = 4, EI32 = 5 };
+
+inline float level_h2(dsg_ctx *ctx, int l) {
+  const double h1 = ctx->s.lengthsize / (ctx->lnx[l] - 2);
+  return (float)(h1 * h1);
+}
+
+// Finest-level colour-split FP32 arrays: {even, odd} halves of U and RHS.
+struct FineSplit {
+  float *u[2];
+  float *r[2];
+};
+
+inline FineSplit fine_split(dsg_ctx *ctx) {
+  float **L = ctx->lv32[ctx->ng];
+  const dsg::Dims d = ctx->fine();
+  const size_t half = (size_t)((d.nx - 2) >> 1) * (d.ny - 2) * (d.nz - 2);
+  return FineSplit{{L[U32], L[U32] + half}, {L[RHS32], L[RHS32] + half}};
+}
+
+inline size_t fine_split_bytes(dsg_ctx *ctx) {
+  const dsg::Dims d = ctx->fine();
+  return 2 * (size_t)((d.nx - 2) >> 1) * (d.ny - 2) * (d.nz - 2) * sizeof(float);
+}
+
+inline void phase_coefs(dsg_ctx *ctx, float *r1, float *r2) {
+  *r1 = (float)(0.5 * (ctx->s.rho1 - ctx->s.rho2));
+  *r2 = (float)ctx->s.rho2;
+}
+
+cudaError_t relax32_level(dsg_ctx *ctx, int n, int l) {
+  float **L = ctx->lv32[l];
+  const Dims d = ctx->level(l);
+  const bool fine = l == ctx->ng;
+  const bool timed = ctx->prof && fine && n > 0;
+  if (timed) {
+    if (ctx->prof_used + 2 > ctx->prof_ev.size()) {
+      for (int q = 0; q < 256; q++) {
+        cudaEvent_t e;
+        cudaError_t r = cudaEventCreate(&e);
+        if (r != cudaSuccess) return r;
+        ctx->prof_ev.push_back(e);
+      }
+    }
+    cudaError_t r = cudaEventRecord(ctx->prof_ev[ctx->prof_used], ctx->stream);
+    if (r != cudaSuccess) return r;
+  }
+  cudaError_t e;
+  if (fine) {
+    FineSplit f = fine_split(ctx);
+    float r1, r2;
+    phase_coefs(ctx, &r1, &r2);
+    e = dsg::relax32_split_n(n, f.u, f.r, L[A32], d, level_h2(ctx, l), (float)ctx->cfg.omega, r1, r2, ctx->stream);
+  } else {
+    e = dsg::relax32_n(n, L[U32], level_h2(ctx, l), L[RHS32], L[A32], L[B32], L[C32], L[EI32], d,
+                       (float)ctx->cfg.omega, ctx->stream);
+  }
+  if (timed) {
+    cudaError_t r = cudaEventRecord(ctx->prof_ev[ctx->prof_used + 1], ctx->stream);
+    if (r != cudaSuccess) return r;
+    ctx->prof_used += 2;
+    ctx->prof_relax_calls += n;
+    // colour-split sweep: per colour pass the other colour (half), own colour
+    // read+write (half each), own rhs (half) and cc (full): 6 FP32 words per cell
+    ctx->prof_relax_bytes += (double)n * 6.0 * sizeof(float) * (double)d.count();
+    ctx->prof_relax_bits = 32;
+  }
+  return e;
+}
+
+int vcycle32(dsg_ctx *ctx, int j) {
+  cudaStream_t st = ctx->stream;
+  const int ng = ctx->ng;
+  float r1, r2;
+  phase_coefs(ctx, &r1, &r2);
+  for (int jj = j; jj >= 2; jj--) {
+    float **L = ctx->lv32[jj];
+    DSG_CK(ctx, relax32_level(ctx, ctx->s.npre, jj));
+    if (jj == ng) {
+      FineSplit f = fine_split(ctx);
+      DSG_CK(ctx, dsg::resid_restrict32_split(ctx->lv32[jj - 1][RHS32], f.u, f.r, L[A32], ctx->level(jj),
+                                              1.0f / level_h2(ctx, jj), r1, r2, st));
+    } else {
+      DSG_CK(ctx, dsg::resid_restrict32(ctx->lv32[jj - 1][RHS32], L[U32], L[RHS32], L[A32], L[B32], L[C32],
+                                        ctx->level(jj), 1.0f / level_h2(ctx, jj), st));
+    }
+    DSG_CK(ctx, cudaMemsetAsync(ctx->lv32[jj - 1][U32], 0, ctx->level(jj - 1).count() * sizeof(float), st));
+  }
+  DSG_CK(ctx, relax32_level(ctx, ctx->s.ntop, 1));
+  for (int jj = 2; jj <= j; jj++) {
+    if (jj == ng) {
+      FineSplit f = fine_split(ctx);
+      DSG_CK(ctx, dsg::prolong32_split(f.u, ctx->lv32[jj - 1][U32], ctx->level(jj), 1, st));
+    } else {
+      DSG_CK(ctx, dsg::addint32(ctx->lv32[jj][U32], ctx->lv32[jj - 1][U32], ctx->level(jj), st));
+    }
+    DSG_CK(ctx, relax32_level(ctx, ctx->s.npost, jj));
+  }
+  return DSG_OK;
+}
+
+int defect_host(dsg_ctx *ctx, double *relres) {
+  double **L = ctx->lv[ctx->ng];
+  FineSplit f = fine_split(ctx);
+  DSG_CK(ctx, dsg::defect64(f.r, ctx->red_out, ctx->red_partials, L[1], L[3], L[4], L[5], L[6], ctx->fine(),
+                            ctx->s.lengthsize, ctx->stream));
+  int rc = read_device(ctx, 2);
+  if (rc) return rc;
+  const double rr = ctx->red_host[0], bb = ctx->red_host[1];
+  if (!isfinite(rr) || !isfinite(bb))
+    return dsg::set_error(ctx, DSG_E_NONFINITE, "non-finite defect norm (%g, %g)", rr, bb);
+  *relres = bb > 0.0 ? sqrt(rr) / sqrt(bb) : sqrt(rr);
+  return DSG_OK;
+}
+
+// FP32 hierarchy: cc in FP32 on the finest level (its relax forms the face
+// coefficients itself), coarse coefficients by acfromac from the FP64 fine
+// coefficients of abcei.
+int coef_hierarchy32(dsg_ctx *ctx) {
+  const int ng = ctx->ng;
+  cudaStream_t st = ctx->stream;
+  double **F = ctx->lv[ng];
+  DSG_CK(ctx, dsg::to32(ctx->lv32[ng][A32], F[0], ctx->fine().count(), st));
+  if (ng >= 2) {
+    float **C = ctx->lv32[ng - 1];
+    DSG_CK(ctx, dsg::acfromac64to32(C[A32], C[B32], C[C32], C[EI32], F[4], F[5], F[6], ctx->level(ng - 1), st));
+  }
+  for (int g = ng - 2; g >= 1; g--) {
+    float **C = ctx->lv32[g], **Fi = ctx->lv32[g + 1];
+    DSG_CK(ctx, dsg::acfromac32(C[A32], C[B32], C[C32], C[EI32], Fi[A32], Fi[B32], Fi[C32], ctx->level(g), st));
+  }
+  return DSG_OK;
+}
+
+// Initial guess by an FP32 full-multigrid pass (the mglin schedule in FP32).
+int fmg32(dsg_ctx *ctx) {
+  const int ng = ctx->ng;
+  cudaStream_t st = ctx->stream;
+  FineSplit f = fine_split(ctx);
+  DSG_CK(ctx, dsg::split_from64(f.r, ctx->lv[ng][3], ctx->fine(), st));
+  if (ng >= 2) DSG_CK(ctx, dsg::restrict32_split(ctx->lv32[ng - 1][RHS32], f.r, ctx->level(ng - 1), st));
+  for (int g = ng - 2; g >= 1; g--)
+    DSG_CK(ctx, dsg::restrict32(ctx->lv32[g][RHS32], ctx->lv32[g + 1][RHS32], ctx->level(g), st));
+  DSG_CK(ctx, cudaMemsetAsync(ctx->lv32[1][U32], 0, ctx->level(1).count() * sizeof(float), st));
+  DSG_CK(ctx, relax32_level(ctx, ctx->s.ntop, 1));
+  for (int j = 2; j <= ng; j++) {
+    if (j == ng)
+      DSG_CK(ctx, dsg::prolong32_split(f.u, ctx->lv32[j - 1][U32], ctx->level(j), 0, st));
+    else
+      DSG_CK(ctx, dsg::interp32(ctx->lv32[j][U32], ctx->lv32[j - 1][U32], ctx->level(j), st));
+    for (int c = 0; c < ctx->cfg.cycles; c++) {
+      int rc = vcycle32(ctx, j);
+      if (rc) return rc;
+    }
+  }
+  DSG_CK(ctx, dsg::correct64(ctx->lv[ng][1], f.u, ctx->fine(), 1, st));
+  return DSG_OK;
+}
+
+int mixed_solve(dsg_ctx *ctx, dsg_mg_stats *s) {
+  const int ng = ctx->ng;
+  cudaStream_t st = ctx->stream;
+  if ((ctx->nx - 2) & 1)
+    return dsg::set_error(ctx, DSG_E_ARG, "mixed mode needs an even number of interior cells along x (%d)",
+                          ctx->nx - 2);
+  int rc = coef_hierarchy32(ctx);
+  if (rc) return rc;
+  rc = fmg32(ctx);
+  if (rc) return rc;
+  double r;
+  rc = defect_host(ctx, &r);
+  if (rc) return rc;
+  s->relres_init = r;
+  int n = 0;
+  while (r >= ctx->cfg.tol && n < ctx->cfg.max_vcycles) {
+    FineSplit f = fine_split(ctx);
+    DSG_CK(ctx, cudaMemsetAsync(f.u[0], 0, fine_split_bytes(ctx), st));
+    rc = vcycle32(ctx, ng);
+    if (rc) return rc;
+    DSG_CK(ctx, dsg::correct64(ctx->lv[ng][1], f.u, ctx->fine(), 0, st));
+    s->fine_sweeps += ctx->s.npre + ctx->s.npost;
+    n++;
+    rc = defect_host(ctx, &r);
+    if (rc) return rc;
+  }
+  DSG_CK(ctx, dsg::bc_scalar(ctx->lv[ng][1], ctx->fine(), st));
+  s->vcycles = n;
+  s->relres = r;
+  s->converged = r < ctx->cfg.tol;
+  return DSG_OK;
+}
+
 int mglin(dsg_ctx *ctx, dsg_mg_stats *stats) {
   const int ng = ctx->ng;
   const double om = ctx->cfg.omega;
   cudaStream_t st = ctx->stream;
   int fine_sweeps = 0;
+  if (ctx->cfg.mode == DSG_MODE_TOL_MIXED) {
+    dsg_mg_stats s;
+    memset(&s, 0, sizeof s);
+    s.mode = ctx->cfg.mode;
+    s.relres = -1.0;
+    s.relres_init = -1.0;
+    s.epsdiv = -1.0;
+    int rc = mixed_solve(ctx, &s);
+    if (rc) return rc;
+    ctx->s.last_vcycles = s.vcycles;
+    ctx->s.last_relres = s.relres;
+    ctx->s.last_relres_fmg = s.relres_init;
+    if (stats) *stats = s;
+    if (!s.converged)
+      return dsg::set_error(ctx, DSG_E_NOT_CONVERGED, "mixed multigrid reached %d cycles at relres %.3e > tol %.3e",
+                            s.vcycles, s.relres, ctx->cfg.tol);
+    return DSG_OK;
+  }
   for (int g = ng - 1; g >= 1; g--) {
     const Dims dc = ctx->level(g);
     DSG_CK(ctx, dsg::rstrct(ctx->lv[g][3], ctx->lv[g + 1][3], dc, st));
@@ -217,7 +429,7 @@ int mglin(dsg_ctx *ctx, dsg_mg_stats *stats) {
     ctx->s.last_vcycles = n;
     ctx->s.last_relres = r;
     ctx->s.last_relres_fmg = s.relres_init;
-  } else if (ctx->cfg.mode != DSG_MODE_REF_EXACT) {
+  } else if (ctx->cfg.mode != DSG_MODE_REF_EXACT && ctx->cfg.mode != DSG_MODE_TOL_MIXED) {
     return dsg::set_error(ctx, DSG_E_ARG, "pressure mode %d is not available in this build", ctx->cfg.mode);
   }
   s.fine_sweeps = fine_sweeps;
@@ -273,6 +485,8 @@ int dsg_create(const dsg_config *cfg, dsg_ctx **out) {
     nny = nny / 2 + 1;
     nnz = nnz / 2 + 1;
   }
+  for (int l = ng; l >= 1; l--)
+    total += 6 * up((size_t)ctx->lnx[l] * ctx->lny[l] * ctx->lnz[l] * sizeof(float));
   const size_t fine = up((size_t)cfg->nx * cfg->ny * cfg->nz * sizeof(double));
   const int nextra = DSG_NFIELDS - 8 + 1;  // fine fields beyond the level arrays + ccf
   total += nextra * fine;
@@ -290,6 +504,11 @@ int dsg_create(const dsg_config *cfg, dsg_ctx **out) {
     for (int f = 0; f < 8; f++) {
       ctx->lv[l][f] = (double *)p;
       p += up((size_t)ctx->lnx[l] * ctx->lny[l] * ctx->lnz[l] * sizeof(double));
+    }
+  for (int l = ng; l >= 1; l--)
+    for (int f = 0; f < 6; f++) {
+      ctx->lv32[l][f] = (float *)p;
+      p += up((size_t)ctx->lnx[l] * ctx->lny[l] * ctx->lnz[l] * sizeof(float));
     }
   for (int f = 0; f < 8; f++) ctx->f[f] = ctx->lv[ng][f];
   for (int f = 8; f < DSG_NFIELDS; f++) {
@@ -595,6 +814,7 @@ int dsg_profile_read(dsg_ctx *ctx, dsg_profile *out) {
   out->relax_calls = ctx->prof_relax_calls;
   out->relax_ms = ms;
   out->relax_bytes = ctx->prof_relax_bytes;
+  out->relax_bits = ctx->prof_relax_bits;
   return DSG_OK;
 }
 

@@ -104,6 +104,31 @@ cudaError_t divergence(double *out, const double *u, const double *v, const doub
                        cudaStream_t st);
 cudaError_t project(double *u, double *v, double *w, const double *p, const double *a, const double *b,
                     const double *c, Dims d, cudaStream_t st);
+// mg32.cu (mixed precision)
+cudaError_t relax32_n(int n, float *u, float h2, const float *rhs, const float *a, const float *b, const float *c,
+                      const float *ei, Dims d, float omega, cudaStream_t st);
+cudaError_t resid_restrict32(float *rhs_c, const float *u, const float *rhs, const float *a, const float *b,
+                             const float *c, Dims df, float h2i, cudaStream_t st);
+cudaError_t addint32(float *uf, const float *uc, Dims df, cudaStream_t st);
+cudaError_t interp32(float *uf, const float *uc, Dims df, cudaStream_t st);
+cudaError_t restrict32(float *uc, const float *uf, Dims dc, cudaStream_t st);
+cudaError_t acfromac32(float *a, float *b, float *c, float *ei, const float *a2, const float *b2, const float *c2,
+                       Dims dc, cudaStream_t st);
+cudaError_t acfromac64to32(float *a, float *b, float *c, float *ei, const double *a2, const double *b2,
+                           const double *c2, Dims dc, cudaStream_t st);
+// finest level in colour-split storage ({even, odd} arrays of (nx-2)/2 x (ny-2) x (nz-2))
+cudaError_t relax32_split_n(int n, float *const u[2], float *const rhs[2], const float *cc, Dims d, float h2,
+                            float omega, float r1, float r2, cudaStream_t st);
+cudaError_t resid_restrict32_split(float *rhs_c, float *const u[2], float *const rhs[2], const float *cc, Dims df,
+                                   float h2i, float r1, float r2, cudaStream_t st);
+cudaError_t prolong32_split(float *const u[2], const float *uc, Dims df, int add, cudaStream_t st);
+cudaError_t restrict32_split(float *uc, float *const rhs[2], Dims dc, cudaStream_t st);
+cudaError_t split_from64(float *const dst[2], const double *src, Dims d, cudaStream_t st);
+cudaError_t defect64(float *const r32[2], double *out2, double *partials, const double *p, const double *rhs,
+                     const double *a, const double *b, const double *c, Dims d, double lengthsize,
+                     cudaStream_t st);
+cudaError_t correct64(double *p, float *const e[2], Dims d, int init, cudaStream_t st);
+cudaError_t to32(float *dst, const double *src, size_t n, cudaStream_t st);
 // init.cu
 cudaError_t init_drop(double *cc, double *u, double *v, double *w, Dims d, double h, double x0, double y0,
                       double z0, double radius, double yvel1, double yvel2, double zvel1, double zvel2,
@@ -118,6 +143,9 @@ struct dsg_ctx {
   int nx, ny, nz, ng;
   int lnx[32], lny[32], lnz[32];
   double *lv[32][8];          // [level][CC,P,RES,RHS,A,B,C,EI], level 1..ng
+  float *lv32[32][6];         // FP32 hierarchy [level][U,RHS,A,B,C,EI] of the mixed mode;
+                              // on the finest level U and RHS are colour-split (even half, odd
+                              // half) and A holds cc in FP32
   double *f[DSG_NFIELDS];     // fine fields; 0..7 alias lv[ng]
   double *ccf;                // csf filtered volume fraction (local array of csf)
   double *red_partials;       // reduction partials (kRedBlocks * 4 doubles)
@@ -135,6 +163,7 @@ struct dsg_ctx {
   size_t prof_used = 0;
   long long prof_relax_calls = 0;
   double prof_relax_bytes = 0.0;
+  int prof_relax_bits = 64;
   dsg::Dims fine() const { return dsg::Dims{nx, ny, nz}; }
   dsg::Dims level(int l) const { return dsg::Dims{lnx[l], lny[l], lnz[l]}; }
 };

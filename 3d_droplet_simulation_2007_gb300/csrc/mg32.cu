@@ -1,0 +1,541 @@
+// mg32.cu -- FP32 multigrid bulk and the FP64 defect-correction kernels of the
+// mixed-precision pressure solve (no reference counterpart: the reference
+// solves in FP64 only).
+//
+// The V-cycle follows mglin's structure (main.f:3703-3759): red-black relax
+// (main.f:3956-3997), 8-cell restriction of the residual, piecewise-constant
+// prolong-and-add, NTOP sweeps on the coarsest grid, on the same operator with
+// face coefficients coarsened as acfromac does (main.f:3793-3844).  It runs in
+// FP32 on the correction equation L e = r, where r is the FP64 residual of the
+// current FP64 pressure; the correction is accumulated in FP64.
+//
+// Differences from the FP64 kernels of mg64.cu, chosen for bandwidth:
+//  * every kernel reads bc_scalar's ghost values virtually (own value / 0), so
+//    no ghost-refresh launches exist in the FP32 cycle;
+//  * the residual is never stored: one kernel forms the 8 fine residuals of a
+//    coarse cell and writes their mean as the coarse right-hand side;
+//  * this file is compiled with FMA contraction.
+#include "dsg_internal.cuh"
+
+namespace dsg {
+namespace {
+
+// Virtual-ghost neighbour reads of bc_scalar semantics on level dims d.
+struct Nb {
+  float xp, xm, yp, ym, zp, zm;
+};
+
+__device__ __forceinline__ Nb neighbours(const float *__restrict__ u, size_t q, int i, int j, int k, Dims d,
+                                         float uc) {
+  Nb n;
+  const size_t sy = d.sy(), sz = d.sz();
+  n.xp = (i + 1 == d.nx) ? 0.f : u[q + 1];
+  n.xm = (i - 1 == 1) ? uc : u[q - 1];
+  n.yp = (j + 1 == d.ny) ? uc : u[q + sy];
+  n.ym = (j - 1 == 1) ? uc : u[q - sy];
+  n.zp = (k + 1 == d.nz) ? uc : u[q + sz];
+  n.zm = (k - 1 == 1) ? uc : u[q - sz];
+  return n;
+}
+
+// ---- finest level: colour-split storage --------------------------------------
+//
+// On the finest level the FP32 correction u and right-hand side are stored
+// split by colour: cells with i+j+k even (the first pass of relax) in one
+// array, odd in another, each (nx-2)/2 x (ny-2) x (nz-2) over the interior
+// only (ghosts are virtual).  In row (j,k) the colour-c cells are
+// i = 2 + 2m + p with p = (j+k+c) & 1.  A colour pass then reads the other
+// colour, reads and writes its own colour and reads cc for the face
+// coefficients, all with full 32-byte sectors: 24 bytes per cell per relax.
+// Face coefficients are formed from the FP32 volume fraction as abcei does,
+// a = 1/(r1*(c_i+c_{i+1}) + r2), with bc_coef's a(1) = a(2).
+struct Split {
+  int hx, ny2, nz2;  // (nx-2)/2, ny-2, nz-2
+  __host__ __device__ __forceinline__ size_t at(int m, int j, int k) const {
+    return (size_t)m + (size_t)hx * ((size_t)(j - 2) + (size_t)ny2 * (size_t)(k - 2));
+  }
+  __host__ __device__ __forceinline__ size_t count() const { return (size_t)hx * ny2 * nz2; }
+};
+
+__device__ __forceinline__ Split split_of(Dims d) { return Split{(d.nx - 2) >> 1, d.ny - 2, d.nz - 2}; }
+
+// Single-instruction reciprocal (MUFU): the FP32 V-cycle is a preconditioner
+// of the FP64 defect correction, so an approximate 1/x is sufficient.
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+__device__ __forceinline__ float face_coef(float x, float y, float r1, float r2) {
+  return rcp_approx(r1 * (x + y) + r2);
+}
+
+// Value of cell (i,j,k) of a colour-split pair {even, odd}.
+__device__ __forceinline__ float split_get(const float *__restrict__ ev, const float *__restrict__ od, Split sp,
+                                           int i, int j, int k) {
+  const size_t q = sp.at((i - 2) >> 1, j, k);
+  return ((i + j + k) & 1) ? od[q] : ev[q];
+}
+
+// One colour pass on the finest level: colour c (0 = i+j+k even).
+__global__ void k_relax32_split(float *__restrict__ self, const float *__restrict__ other,
+                                const float *__restrict__ rhs_self, const float *__restrict__ cc, Dims d, Split sp,
+                                int c, float h2, float omega, float r1, float r2) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
+  const int k = blockIdx.z + 2;
+  if (m >= sp.hx || j > d.ny - 1) return;
+  const int p = (j + k + c) & 1;
+  const int i = 2 + 2 * m + p;
+  const size_t qs = sp.at(m, j, k);
+  const size_t rowstride = (size_t)sp.hx, planestride = (size_t)sp.hx * sp.ny2;
+  const float uc = self[qs];
+  const float xm = (m == 0 && p == 0) ? uc : other[qs - 1 + p];
+  const float xp = (m == sp.hx - 1 && p == 1) ? 0.f : other[qs + p];
+  const float ym = (j == 2) ? uc : other[qs - rowstride];
+  const float yp = (j == d.ny - 1) ? uc : other[qs + rowstride];
+  const float zm = (k == 2) ? uc : other[qs - planestride];
+  const float zp = (k == d.nz - 1) ? uc : other[qs + planestride];
+  const size_t q = d.ix(i, j, k);
+  const float c0 = cc[q];
+  const float ae = face_coef(c0, cc[q + 1], r1, r2);
+  const float aw = (i == 2) ? ae : face_coef(cc[q - 1], c0, r1, r2);
+  const float bn = face_coef(c0, cc[q + d.sy()], r1, r2);
+  const float bs = face_coef(cc[q - d.sy()], c0, r1, r2);
+  const float ct = face_coef(c0, cc[q + d.sz()], r1, r2);
+  const float cb = face_coef(cc[q - d.sz()], c0, r1, r2);
+  const float ei = rcp_approx(ae + aw + bn + bs + ct + cb);
+  const float temp = (ae * xp + aw * xm + bn * yp + bs * ym + ct * zp + cb * zm - h2 * rhs_self[qs]) * ei;
+  self[qs] = omega * temp + (1.f - omega) * uc;
+}
+
+// Finest-level residual (cc-derived operator, virtual ghosts) restricted to the
+// coarse rhs: mean of the 8 fine residuals of each coarse cell.
+__global__ void k_resid_restrict32_split(float *__restrict__ rhs_c, const float *__restrict__ ue,
+                                         const float *__restrict__ uo, const float *__restrict__ re,
+                                         const float *__restrict__ ro, const float *__restrict__ cc, Dims df,
+                                         Split sp, Dims dc, float h2i, float r1, float r2) {
+  const int ic = blockIdx.x * blockDim.x + threadIdx.x + 2;
+  const int jc = blockIdx.y * blockDim.y + threadIdx.y + 2;
+  const int kc = blockIdx.z + 2;
+  if (ic > dc.nx - 1 || jc > dc.ny - 1) return;
+  float acc = 0.f;
+#pragma unroll
+  for (int dk = 0; dk < 2; dk++)
+#pragma unroll
+    for (int dj = 0; dj < 2; dj++)
+#pragma unroll
+      for (int di = 0; di < 2; di++) {
+        const int i = 2 * ic - 2 + di, j = 2 * jc - 2 + dj, k = 2 * kc - 2 + dk;
+        const float uc = split_get(ue, uo, sp, i, j, k);
+        const float xp = (i + 1 == df.nx) ? 0.f : split_get(ue, uo, sp, i + 1, j, k);
+        const float xm = (i == 2) ? uc : split_get(ue, uo, sp, i - 1, j, k);
+        const float yp = (j + 1 == df.ny) ? uc : split_get(ue, uo, sp, i, j + 1, k);
+        const float ym = (j == 2) ? uc : split_get(ue, uo, sp, i, j - 1, k);
+        const float zp = (k + 1 == df.nz) ? uc : split_get(ue, uo, sp, i, j, k + 1);
+        const float zm = (k == 2) ? uc : split_get(ue, uo, sp, i, j, k - 1);
+        const size_t q = df.ix(i, j, k);
+        const float c0 = cc[q];
+        const float ae = face_coef(c0, cc[q + 1], r1, r2);
+        const float aw = (i == 2) ? ae : face_coef(cc[q - 1], c0, r1, r2);
+        const float bn = face_coef(c0, cc[q + df.sy()], r1, r2);
+        const float bs = face_coef(cc[q - df.sy()], c0, r1, r2);
+        const float ct = face_coef(c0, cc[q + df.sz()], r1, r2);
+        const float cb = face_coef(cc[q - df.sz()], c0, r1, r2);
+        const float lap = ae * (xp - uc) + aw * (xm - uc) + bn * (yp - uc) + bs * (ym - uc) + ct * (zp - uc) +
+                          cb * (zm - uc);
+        acc += split_get(re, ro, sp, i, j, k) - h2i * lap;
+      }
+  rhs_c[dc.ix(ic, jc, kc)] = 0.125f * acc;
+}
+
+// Fine (split) u = or += injection of the coarse correction.
+__global__ void k_prolong32_split(float *__restrict__ ue, float *__restrict__ uo, const float *__restrict__ uc,
+                                  Dims df, Split sp, Dims dc, int add) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
+  const int k = blockIdx.z + 2;
+  if (i > df.nx - 1 || j > df.ny - 1) return;
+  const float v = uc[dc.ix((i >> 1) + 1, (j >> 1) + 1, (k >> 1) + 1)];
+  float *dst = ((i + j + k) & 1) ? uo : ue;
+  const size_t q = sp.at((i - 2) >> 1, j, k);
+  dst[q] = add ? dst[q] + v : v;
+}
+
+// 8-cell mean of the split fine rhs into the coarse interior (rstrct).
+__global__ void k_restrict32_split(float *__restrict__ uc, const float *__restrict__ re,
+                                   const float *__restrict__ ro, Dims dc, Split sp) {
+  const int ic = blockIdx.x * blockDim.x + threadIdx.x + 2;
+  const int jc = blockIdx.y * blockDim.y + threadIdx.y + 2;
+  const int kc = blockIdx.z + 2;
+  if (ic > dc.nx - 1 || jc > dc.ny - 1) return;
+  float acc = 0.f;
+#pragma unroll
+  for (int dk = 0; dk < 2; dk++)
+#pragma unroll
+    for (int dj = 0; dj < 2; dj++)
+#pragma unroll
+      for (int di = 0; di < 2; di++)
+        acc += split_get(re, ro, sp, 2 * ic - 2 + di, 2 * jc - 2 + dj, 2 * kc - 2 + dk);
+  uc[dc.ix(ic, jc, kc)] = 0.125f * acc;
+}
+
+// FP64 -> split FP32 (the fine rhs of the FMG start).
+__global__ void k_split_from64(float *__restrict__ ev, float *__restrict__ od, const double *__restrict__ src,
+                               Dims d, Split sp) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
+  const int k = blockIdx.z + 2;
+  if (i > d.nx - 1 || j > d.ny - 1) return;
+  float *dst = ((i + j + k) & 1) ? od : ev;
+  dst[sp.at((i - 2) >> 1, j, k)] = (float)src[d.ix(i, j, k)];
+}
+
+__global__ void k_relax32(float *__restrict__ u, const float *__restrict__ rhs, const float *__restrict__ a,
+                          const float *__restrict__ b, const float *__restrict__ c, const float *__restrict__ ei,
+                          Dims d, float h2, float omega, int colour) {
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
+  const int k = blockIdx.z + 2;
+  if (j > d.ny - 1) return;
+  const int i = 2 + ((j + k + colour) & 1) + 2 * (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (i > d.nx - 1) return;
+  const size_t q = d.ix(i, j, k);
+  const size_t sy = d.sy(), sz = d.sz();
+  const float uc = u[q];
+  const Nb n = neighbours(u, q, i, j, k, d, uc);
+  const float s = a[q] * n.xp + a[q - 1] * n.xm + b[q] * n.yp + b[q - sy] * n.ym + c[q] * n.zp + c[q - sz] * n.zm -
+                  h2 * rhs[q];
+  u[q] = omega * (s * ei[q]) + (1.f - omega) * uc;
+}
+
+// Coarse rhs = mean of the 8 fine residuals (resid + rstrct, main.f:3718-3725).
+__global__ void k_resid_restrict32(float *__restrict__ rhs_c, const float *__restrict__ u,
+                                   const float *__restrict__ rhs, const float *__restrict__ a,
+                                   const float *__restrict__ b, const float *__restrict__ c, Dims df, Dims dc,
+                                   float h2i) {
+  const int ic = blockIdx.x * blockDim.x + threadIdx.x + 2;
+  const int jc = blockIdx.y * blockDim.y + threadIdx.y + 2;
+  const int kc = blockIdx.z + 2;
+  if (ic > dc.nx - 1 || jc > dc.ny - 1) return;
+  const size_t sy = df.sy(), sz = df.sz();
+  float acc = 0.f;
+#pragma unroll
+  for (int dk = 0; dk < 2; dk++)
+#pragma unroll
+    for (int dj = 0; dj < 2; dj++)
+#pragma unroll
+      for (int di = 0; di < 2; di++) {
+        const int i = 2 * ic - 2 + di, j = 2 * jc - 2 + dj, k = 2 * kc - 2 + dk;
+        const size_t q = df.ix(i, j, k);
+        const float uc = u[q];
+        const Nb n = neighbours(u, q, i, j, k, df, uc);
+        const float lap = a[q] * (n.xp - uc) + a[q - 1] * (n.xm - uc) + b[q] * (n.yp - uc) +
+                          b[q - sy] * (n.ym - uc) + c[q] * (n.zp - uc) + c[q - sz] * (n.zm - uc);
+        acc += rhs[q] - h2i * lap;
+      }
+  rhs_c[dc.ix(ic, jc, kc)] = 0.125f * acc;
+}
+
+// u += injection of the coarse correction (addint, main.f:3934-3954), interior.
+__global__ void k_addint32(float *__restrict__ uf, const float *__restrict__ uc, Dims df, Dims dc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
+  const int k = blockIdx.z + 2;
+  if (i > df.nx - 1 || j > df.ny - 1) return;
+  uf[df.ix(i, j, k)] += uc[dc.ix((i >> 1) + 1, (j >> 1) + 1, (k >> 1) + 1)];
+}
+
+// Interior injection (interp, main.f:3866-3900) for the FMG start.
+__global__ void k_interp32(float *__restrict__ uf, const float *__restrict__ uc, Dims df, Dims dc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
+  const int k = blockIdx.z + 2;
+  if (i > df.nx - 1 || j > df.ny - 1) return;
+  uf[df.ix(i, j, k)] = uc[dc.ix((i >> 1) + 1, (j >> 1) + 1, (k >> 1) + 1)];
+}
+
+// 8-cell mean of a fine interior field into the coarse interior (rstrct).
+__global__ void k_restrict32(float *__restrict__ uc, const float *__restrict__ uf, Dims dc, Dims df) {
+  const int ic = blockIdx.x * blockDim.x + threadIdx.x + 2;
+  const int jc = blockIdx.y * blockDim.y + threadIdx.y + 2;
+  const int kc = blockIdx.z + 2;
+  if (ic > dc.nx - 1 || jc > dc.ny - 1) return;
+  const size_t f = df.ix(2 * ic - 2, 2 * jc - 2, 2 * kc - 2);
+  const size_t sy = df.sy(), sz = df.sz();
+  uc[dc.ix(ic, jc, kc)] = 0.125f * (uf[f] + uf[f + 1] + uf[f + sy] + uf[f + 1 + sy] + uf[f + sz] + uf[f + 1 + sz] +
+                                    uf[f + sy + sz] + uf[f + 1 + sy + sz]);
+}
+
+__device__ __forceinline__ float acf(const float *a2, Dims df, int i1, int j1, int k1, int i2, int j2, int k2,
+                                     int i3, int j3, int k3, int i4, int j4, int k4) {
+  return 0.25f * (a2[df.ix(i1, j1, k1)] + a2[df.ix(i2, j2, k2)] + a2[df.ix(i3, j3, k3)] + a2[df.ix(i4, j4, k4)]);
+}
+
+// acfromac in FP32 (main.f:3793-3844).
+__global__ void k_acfromac32(float *__restrict__ a, float *__restrict__ b, float *__restrict__ c,
+                             float *__restrict__ ei, const float *__restrict__ a2, const float *__restrict__ b2,
+                             const float *__restrict__ c2, Dims dc, Dims df) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int k = blockIdx.z + 1;
+  if (i > dc.nx || j > dc.ny) return;
+  const bool ii = i >= 2 && i <= dc.nx - 1, ji = j >= 2 && j <= dc.ny - 1, ki = k >= 2 && k <= dc.nz - 1;
+  const size_t q = dc.ix(i, j, k);
+#define AA(i, j, k) acf(a2, df, 2 * (i) - 1, 2 * (j) - 1, 2 * (k) - 1, 2 * (i) - 1, 2 * (j) - 2, 2 * (k) - 1, \
+                        2 * (i) - 1, 2 * (j) - 1, 2 * (k) - 2, 2 * (i) - 1, 2 * (j) - 2, 2 * (k) - 2)
+#define BB(i, j, k) acf(b2, df, 2 * (i) - 1, 2 * (j) - 1, 2 * (k) - 1, 2 * (i) - 2, 2 * (j) - 1, 2 * (k) - 1, \
+                        2 * (i) - 1, 2 * (j) - 1, 2 * (k) - 2, 2 * (i) - 2, 2 * (j) - 1, 2 * (k) - 2)
+#define CC(i, j, k) acf(c2, df, 2 * (i) - 1, 2 * (j) - 1, 2 * (k) - 1, 2 * (i) - 2, 2 * (j) - 1, 2 * (k) - 1, \
+                        2 * (i) - 1, 2 * (j) - 2, 2 * (k) - 1, 2 * (i) - 2, 2 * (j) - 2, 2 * (k) - 1)
+  float va = 0.f, vb = 0.f, vc = 0.f;
+  if (i <= dc.nx - 1 && ji && ki) { va = AA(i, j, k); a[q] = va; }
+  if (j <= dc.ny - 1 && ii && ki) { vb = BB(i, j, k); b[q] = vb; }
+  if (k <= dc.nz - 1 && ii && ji) { vc = CC(i, j, k); c[q] = vc; }
+  if (ii && ji && ki) ei[q] = 1.f / (va + AA(i - 1, j, k) + vb + BB(i, j - 1, k) + vc + CC(i, j, k - 1));
+#undef AA
+#undef BB
+#undef CC
+}
+
+// ---- FP64 defect-correction kernels ----------------------------------------
+// r = rhs - L p in FP64 over the interior (the expression of resid,
+// main.f:3912-3925, with bc_scalar ghosts read virtually); writes (float)r as
+// the FP32 fine rhs and per-block partial sums of r^2 and rhs^2.
+__global__ void k_defect64(float *__restrict__ r_ev, float *__restrict__ r_od, Split sp,
+                           double *__restrict__ partials, const double *__restrict__ p,
+                           const double *__restrict__ rhs, const double *__restrict__ a,
+                           const double *__restrict__ b, const double *__restrict__ c, Dims d, double h2i) {
+  const size_t n = (size_t)(d.nx - 2) * (d.ny - 2) * (d.nz - 2);
+  const size_t sy = d.sy(), sz = d.sz();
+  double rr = 0.0, bb = 0.0;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    const size_t ni = (size_t)(d.nx - 2), nj = (size_t)(d.ny - 2);
+    const int i = (int)(t % ni) + 2;
+    const size_t rem = t / ni;
+    const int j = (int)(rem % nj) + 2, k = (int)(rem / nj) + 2;
+    const size_t q = d.ix(i, j, k);
+    const double uc = p[q];
+    const double xp = (i + 1 == d.nx) ? 0.0 : p[q + 1];
+    const double xm = (i - 1 == 1) ? uc : p[q - 1];
+    const double yp = (j + 1 == d.ny) ? uc : p[q + sy];
+    const double ym = (j - 1 == 1) ? uc : p[q - sy];
+    const double zp = (k + 1 == d.nz) ? uc : p[q + sz];
+    const double zm = (k - 1 == 1) ? uc : p[q - sz];
+    const double f = rhs[q];
+    const double r = -h2i * (a[q] * (xp - uc) + a[q - 1] * (xm - uc) + b[q] * (yp - uc) + b[q - sy] * (ym - uc) +
+                             c[q] * (zp - uc) + c[q - sz] * (zm - uc)) +
+                     f;
+    (((i + j + k) & 1) ? r_od : r_ev)[sp.at((i - 2) >> 1, j, k)] = (float)r;
+    rr += r * r;
+    bb += f * f;
+  }
+  __shared__ double s0[kRedThreads], s1[kRedThreads];
+  s0[threadIdx.x] = rr;
+  s1[threadIdx.x] = bb;
+  __syncthreads();
+  for (int s = kRedThreads / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      s0[threadIdx.x] += s0[threadIdx.x + s];
+      s1[threadIdx.x] += s1[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    partials[2 * blockIdx.x] = s0[0];
+    partials[2 * blockIdx.x + 1] = s1[0];
+  }
+}
+
+__global__ void k_fold2(const double *__restrict__ partials, double *__restrict__ out) {
+  __shared__ double s0[kRedThreads], s1[kRedThreads];
+  double a0 = 0.0, a1 = 0.0;
+  for (int b = threadIdx.x; b < kRedBlocks; b += kRedThreads) {
+    a0 += partials[2 * b];
+    a1 += partials[2 * b + 1];
+  }
+  s0[threadIdx.x] = a0;
+  s1[threadIdx.x] = a1;
+  __syncthreads();
+  for (int s = kRedThreads / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      s0[threadIdx.x] += s0[threadIdx.x + s];
+      s1[threadIdx.x] += s1[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[0] = s0[0];
+    out[1] = s1[0];
+  }
+}
+
+// p += e (FP64 accumulation of the split FP32 correction), interior; `init`
+// sets p = e.
+__global__ void k_correct64(double *__restrict__ p, const float *__restrict__ ev, const float *__restrict__ od,
+                            Dims d, Split sp, int init) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
+  const int k = blockIdx.z + 2;
+  if (i > d.nx - 1 || j > d.ny - 1) return;
+  const size_t q = d.ix(i, j, k);
+  const double e = (double)split_get(ev, od, sp, i, j, k);
+  p[q] = init ? e : p[q] + e;
+}
+
+__global__ void k_to32(float *__restrict__ dst, const double *__restrict__ src, size_t n) {
+  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+    dst[q] = (float)src[q];
+}
+
+// Coarse FP32 coefficients (acfromac) straight from the FP64 fine ones.
+__global__ void k_acfromac64to32(float *__restrict__ a, float *__restrict__ b, float *__restrict__ c,
+                                 float *__restrict__ ei, const double *__restrict__ a2,
+                                 const double *__restrict__ b2, const double *__restrict__ c2, Dims dc, Dims df) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int k = blockIdx.z + 1;
+  if (i > dc.nx || j > dc.ny) return;
+  const bool ii = i >= 2 && i <= dc.nx - 1, ji = j >= 2 && j <= dc.ny - 1, ki = k >= 2 && k <= dc.nz - 1;
+  const size_t q = dc.ix(i, j, k);
+#define FA(i, j, k) (0.25 * (a2[df.ix(2 * (i) - 1, 2 * (j) - 1, 2 * (k) - 1)] + a2[df.ix(2 * (i) - 1, 2 * (j) - 2, 2 * (k) - 1)] + \
+                             a2[df.ix(2 * (i) - 1, 2 * (j) - 1, 2 * (k) - 2)] + a2[df.ix(2 * (i) - 1, 2 * (j) - 2, 2 * (k) - 2)]))
+#define FB(i, j, k) (0.25 * (b2[df.ix(2 * (i) - 1, 2 * (j) - 1, 2 * (k) - 1)] + b2[df.ix(2 * (i) - 2, 2 * (j) - 1, 2 * (k) - 1)] + \
+                             b2[df.ix(2 * (i) - 1, 2 * (j) - 1, 2 * (k) - 2)] + b2[df.ix(2 * (i) - 2, 2 * (j) - 1, 2 * (k) - 2)]))
+#define FC(i, j, k) (0.25 * (c2[df.ix(2 * (i) - 1, 2 * (j) - 1, 2 * (k) - 1)] + c2[df.ix(2 * (i) - 2, 2 * (j) - 1, 2 * (k) - 1)] + \
+                             c2[df.ix(2 * (i) - 1, 2 * (j) - 2, 2 * (k) - 1)] + c2[df.ix(2 * (i) - 2, 2 * (j) - 2, 2 * (k) - 1)]))
+  double va = 0.0, vb = 0.0, vc = 0.0;
+  if (i <= dc.nx - 1 && ji && ki) { va = FA(i, j, k); a[q] = (float)va; }
+  if (j <= dc.ny - 1 && ii && ki) { vb = FB(i, j, k); b[q] = (float)vb; }
+  if (k <= dc.nz - 1 && ii && ji) { vc = FC(i, j, k); c[q] = (float)vc; }
+  if (ii && ji && ki) ei[q] = (float)(1.0 / (va + FA(i - 1, j, k) + vb + FB(i, j - 1, k) + vc + FC(i, j, k - 1)));
+#undef FA
+#undef FB
+#undef FC
+}
+
+const dim3 kBlk(32, 4, 1);
+
+inline int flat_blocks(size_t n) { return (int)((n + 255) / 256 < 8192 ? (n + 255) / 256 : 8192); }
+
+}  // namespace
+
+cudaError_t relax32_n(int n, float *u, float h2, const float *rhs, const float *a, const float *b, const float *c,
+                      const float *ei, Dims d, float omega, cudaStream_t st) {
+  const int half = (d.nx - 2 + 1) / 2;
+  const dim3 grid((unsigned)((half + kBlk.x - 1) / kBlk.x), (unsigned)((d.ny - 2 + kBlk.y - 1) / kBlk.y),
+                  (unsigned)(d.nz - 2));
+  for (int q = 0; q < n; q++) {
+    DSG_COUNT k_relax32<<<grid, kBlk, 0, st>>>(u, rhs, a, b, c, ei, d, h2, omega, 0);
+    DSG_COUNT k_relax32<<<grid, kBlk, 0, st>>>(u, rhs, a, b, c, ei, d, h2, omega, 1);
+  }
+  return cudaGetLastError();
+}
+
+// Finest level, colour-split storage: u = {even, odd}, rhs = {even, odd}.
+cudaError_t relax32_split_n(int n, float *const u[2], float *const rhs[2], const float *cc, Dims d, float h2,
+                            float omega, float r1, float r2, cudaStream_t st) {
+  const Split sp{(d.nx - 2) >> 1, d.ny - 2, d.nz - 2};
+  const dim3 blk(64, 4, 1);
+  const dim3 grid((unsigned)((sp.hx + 63) / 64), (unsigned)((d.ny - 2 + 3) / 4), (unsigned)(d.nz - 2));
+  for (int q = 0; q < n; q++)
+    for (int c = 0; c < 2; c++)
+      DSG_COUNT k_relax32_split<<<grid, blk, 0, st>>>(u[c], u[1 - c], rhs[c], cc, d, sp, c, h2, omega, r1, r2);
+  return cudaGetLastError();
+}
+
+cudaError_t resid_restrict32_split(float *rhs_c, float *const u[2], float *const rhs[2], const float *cc, Dims df,
+                                   float h2i, float r1, float r2, cudaStream_t st) {
+  const Dims dc{df.nx / 2 + 1, df.ny / 2 + 1, df.nz / 2 + 1};
+  const Split sp{(df.nx - 2) >> 1, df.ny - 2, df.nz - 2};
+  DSG_COUNT k_resid_restrict32_split<<<interior_grid(dc, kBlk), kBlk, 0, st>>>(rhs_c, u[0], u[1], rhs[0], rhs[1], cc,
+                                                                            df, sp, dc, h2i, r1, r2);
+  return cudaGetLastError();
+}
+
+cudaError_t prolong32_split(float *const u[2], const float *uc, Dims df, int add, cudaStream_t st) {
+  const Dims dc{df.nx / 2 + 1, df.ny / 2 + 1, df.nz / 2 + 1};
+  const Split sp{(df.nx - 2) >> 1, df.ny - 2, df.nz - 2};
+  DSG_COUNT k_prolong32_split<<<interior_grid(df, kBlk), kBlk, 0, st>>>(u[0], u[1], uc, df, sp, dc, add);
+  return cudaGetLastError();
+}
+
+cudaError_t restrict32_split(float *uc, float *const rhs[2], Dims dc, cudaStream_t st) {
+  const Dims df{2 * dc.nx - 2, 2 * dc.ny - 2, 2 * dc.nz - 2};
+  const Split sp{(df.nx - 2) >> 1, df.ny - 2, df.nz - 2};
+  DSG_COUNT k_restrict32_split<<<interior_grid(dc, kBlk), kBlk, 0, st>>>(uc, rhs[0], rhs[1], dc, sp);
+  return cudaGetLastError();
+}
+
+cudaError_t split_from64(float *const dst[2], const double *src, Dims d, cudaStream_t st) {
+  const Split sp{(d.nx - 2) >> 1, d.ny - 2, d.nz - 2};
+  DSG_COUNT k_split_from64<<<interior_grid(d, kBlk), kBlk, 0, st>>>(dst[0], dst[1], src, d, sp);
+  return cudaGetLastError();
+}
+
+cudaError_t resid_restrict32(float *rhs_c, const float *u, const float *rhs, const float *a, const float *b,
+                             const float *c, Dims df, float h2i, cudaStream_t st) {
+  const Dims dc{df.nx / 2 + 1, df.ny / 2 + 1, df.nz / 2 + 1};
+  DSG_COUNT k_resid_restrict32<<<interior_grid(dc, kBlk), kBlk, 0, st>>>(rhs_c, u, rhs, a, b, c, df, dc, h2i);
+  return cudaGetLastError();
+}
+
+cudaError_t addint32(float *uf, const float *uc, Dims df, cudaStream_t st) {
+  const Dims dc{df.nx / 2 + 1, df.ny / 2 + 1, df.nz / 2 + 1};
+  DSG_COUNT k_addint32<<<interior_grid(df, kBlk), kBlk, 0, st>>>(uf, uc, df, dc);
+  return cudaGetLastError();
+}
+
+cudaError_t interp32(float *uf, const float *uc, Dims df, cudaStream_t st) {
+  const Dims dc{df.nx / 2 + 1, df.ny / 2 + 1, df.nz / 2 + 1};
+  DSG_COUNT k_interp32<<<interior_grid(df, kBlk), kBlk, 0, st>>>(uf, uc, df, dc);
+  return cudaGetLastError();
+}
+
+cudaError_t restrict32(float *uc, const float *uf, Dims dc, cudaStream_t st) {
+  const Dims df{2 * dc.nx - 2, 2 * dc.ny - 2, 2 * dc.nz - 2};
+  DSG_COUNT k_restrict32<<<interior_grid(dc, kBlk), kBlk, 0, st>>>(uc, uf, dc, df);
+  return cudaGetLastError();
+}
+
+cudaError_t acfromac32(float *a, float *b, float *c, float *ei, const float *a2, const float *b2, const float *c2,
+                       Dims dc, cudaStream_t st) {
+  const Dims df{2 * dc.nx - 2, 2 * dc.ny - 2, 2 * dc.nz - 2};
+  const dim3 grid((unsigned)((dc.nx + kBlk.x - 1) / kBlk.x), (unsigned)((dc.ny + kBlk.y - 1) / kBlk.y),
+                  (unsigned)dc.nz);
+  DSG_COUNT k_acfromac32<<<grid, kBlk, 0, st>>>(a, b, c, ei, a2, b2, c2, dc, df);
+  return cudaGetLastError();
+}
+
+cudaError_t acfromac64to32(float *a, float *b, float *c, float *ei, const double *a2, const double *b2,
+                           const double *c2, Dims dc, cudaStream_t st) {
+  const Dims df{2 * dc.nx - 2, 2 * dc.ny - 2, 2 * dc.nz - 2};
+  const dim3 grid((unsigned)((dc.nx + kBlk.x - 1) / kBlk.x), (unsigned)((dc.ny + kBlk.y - 1) / kBlk.y),
+                  (unsigned)dc.nz);
+  DSG_COUNT k_acfromac64to32<<<grid, kBlk, 0, st>>>(a, b, c, ei, a2, b2, c2, dc, df);
+  return cudaGetLastError();
+}
+
+cudaError_t defect64(float *const r32[2], double *out2, double *partials, const double *p, const double *rhs,
+                     const double *a, const double *b, const double *c, Dims d, double lengthsize,
+                     cudaStream_t st) {
+  const double h1 = lengthsize / (d.nx - 2);
+  const double h2i = 1.0 / (h1 * h1);
+  const Split sp{(d.nx - 2) >> 1, d.ny - 2, d.nz - 2};
+  DSG_COUNT k_defect64<<<kRedBlocks, kRedThreads, 0, st>>>(r32[0], r32[1], sp, partials, p, rhs, a, b, c, d, h2i);
+  DSG_COUNT k_fold2<<<1, kRedThreads, 0, st>>>(partials, out2);
+  return cudaGetLastError();
+}
+
+cudaError_t correct64(double *p, float *const e[2], Dims d, int init, cudaStream_t st) {
+  const Split sp{(d.nx - 2) >> 1, d.ny - 2, d.nz - 2};
+  DSG_COUNT k_correct64<<<interior_grid(d, kBlk), kBlk, 0, st>>>(p, e[0], e[1], d, sp, init);
+  return cudaGetLastError();
+}
+
+cudaError_t to32(float *dst, const double *src, size_t n, cudaStream_t st) {
+  DSG_COUNT k_to32<<<flat_blocks(n), 256, 0, st>>>(dst, src, n);
+  return cudaGetLastError();
+}
+
+}  // namespace dsg

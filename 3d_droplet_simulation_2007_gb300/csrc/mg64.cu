@@ -221,16 +221,20 @@ __global__ void k_acfromac(double *__restrict__ a, double *__restrict__ b, doubl
 
 // ---- abcei (main.f:3582-3615) and bc_coef (main.f:4465-4494) --------------
 __global__ void k_abc(double *__restrict__ a, double *__restrict__ b, double *__restrict__ c,
-                      const double *__restrict__ cc, double r1, double r2, Dims d) {
+                      const double *__restrict__ cc, double r1, double r2, double k_gas, double k_liq, Dims d) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
   const int k = blockIdx.z + 2;
   if (i > d.nx - 1 || j > d.ny - 1) return;
   const size_t q = d.ix(i, j, k);
-  const double c0 = cc[q];
-  a[q] = 1.0 / (r1 * (c0 + cc[q + 1]) + r2);
-  b[q] = 1.0 / (r1 * (c0 + cc[q + d.sy()]) + r2);
-  c[q] = 1.0 / (r1 * (c0 + cc[q + d.sz()]) + r2);
+  const double c0 = cc[q], cx = cc[q + 1], cy = cc[q + d.sy()], cz = cc[q + d.sz()];
+  // Faces between two bulk cells of the same phase take the precomputed
+  // 1/(r1*(c+c)+r2) (same operations, evaluated once on the host).
+  const bool bulk = (c0 == 0.0 || c0 == 1.0);
+  const double kb = c0 == 0.0 ? k_gas : k_liq;
+  a[q] = (bulk && cx == c0) ? kb : 1.0 / (r1 * (c0 + cx) + r2);
+  b[q] = (bulk && cy == c0) ? kb : 1.0 / (r1 * (c0 + cy) + r2);
+  c[q] = (bulk && cz == c0) ? kb : 1.0 / (r1 * (c0 + cz) + r2);
 }
 
 // bc_coef: face 0 = a x-faces (all j,k), 1 = b(i,1,k) (i,k interior),
@@ -254,13 +258,20 @@ __global__ void k_bc_coef(double *__restrict__ a, double *__restrict__ b, double
 }
 
 __global__ void k_ei(double *__restrict__ ei, const double *__restrict__ a, const double *__restrict__ b,
-                     const double *__restrict__ c, Dims d) {
+                     const double *__restrict__ c, Dims d, double k_gas, double k_liq, double e_gas,
+                     double e_liq) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
   const int k = blockIdx.z + 2;
   if (i > d.nx - 1 || j > d.ny - 1) return;
   const size_t q = d.ix(i, j, k);
-  ei[q] = 1.0 / (a[q] + a[q - 1] + b[q] + b[q - d.sy()] + c[q] + c[q - d.sz()]);
+  const double s0 = a[q], s1 = a[q - 1], s2 = b[q], s3 = b[q - d.sy()], s4 = c[q], s5 = c[q - d.sz()];
+  // Six equal bulk faces: the precomputed 1/(k+k+k+k+k+k).
+  if (s0 == s1 && s0 == s2 && s0 == s3 && s0 == s4 && s0 == s5 && (s0 == k_gas || s0 == k_liq)) {
+    ei[q] = s0 == k_gas ? e_gas : e_liq;
+    return;
+  }
+  ei[q] = 1.0 / (s0 + s1 + s2 + s3 + s4 + s5);
 }
 
 // ---- filterc27 (main.f:5473-5511), default-REAL weights -------------------
@@ -273,6 +284,24 @@ __global__ void k_filterc27(const double *__restrict__ cc, double *__restrict__ 
   const size_t q = d.ix(i, j, k);
   const long sy = (long)d.sy(), sz = (long)d.sz();
 #define C(di, dj, dk) cc[q + (long)(di) + (long)(dj) * sy + (long)(dk) * sz]
+  // Uniform 27-point neighbourhood of 0 or 1: the partial sums are exact
+  // multiples of the value, so the weighted sum equals the precomputed one.
+  const double c0 = C(0, 0, 0);
+  if (c0 == 0.0 || c0 == 1.0) {
+    bool uni = true;
+#pragma unroll
+    for (int dk = -1; dk <= 1; dk++)
+#pragma unroll
+      for (int dj = -1; dj <= 1; dj++)
+#pragma unroll
+        for (int di = -1; di <= 1; di++) uni = uni && (C(di, dj, dk) == c0);
+    if (uni) {
+      double x = c0 == 0.0 ? 0.0 : w0 * 1.0 + w1 * 6.0 + w2 * 12.0 + w3 * 8.0;
+      if (x > 1.0) x = 1.0;
+      cf[q] = x;
+      return;
+    }
+  }
   const double s6 = C(-1, 0, 0) + C(1, 0, 0) + C(0, -1, 0) + C(0, 1, 0) + C(0, 0, 1) + C(0, 0, -1);
   const double s12 = C(-1, -1, 0) + C(-1, 1, 0) + C(1, -1, 0) + C(1, 1, 0) + C(0, 1, 1) + C(0, -1, 1) +
                      C(1, 0, 1) + C(-1, 0, 1) + C(0, 1, -1) + C(0, -1, -1) + C(1, 0, -1) + C(-1, 0, -1);
@@ -524,10 +553,14 @@ cudaError_t acfromac(double *a, double *b, double *c, double *ei, const double *
 
 cudaError_t abcei(double *a, double *b, double *c, double *ei, const double *cc, double r1, double r2,
                   Dims d, cudaStream_t st) {
-  DSG_COUNT k_abc<<<interior_grid(d, kBlk), kBlk, 0, st>>>(a, b, c, cc, r1, r2, d);
+  // bulk-face constants, same operation order as the kernels
+  const double k_gas = 1.0 / (r1 * (0.0 + 0.0) + r2), k_liq = 1.0 / (r1 * (1.0 + 1.0) + r2);
+  const double e_gas = 1.0 / (k_gas + k_gas + k_gas + k_gas + k_gas + k_gas);
+  const double e_liq = 1.0 / (k_liq + k_liq + k_liq + k_liq + k_liq + k_liq);
+  DSG_COUNT k_abc<<<interior_grid(d, kBlk), kBlk, 0, st>>>(a, b, c, cc, r1, r2, k_gas, k_liq, d);
   const dim3 blk(32, 8);
   DSG_COUNT k_bc_coef<<<face_grid(d, blk), blk, 0, st>>>(a, b, c, cc, r1, r2, d);
-  DSG_COUNT k_ei<<<interior_grid(d, kBlk), kBlk, 0, st>>>(ei, a, b, c, d);
+  DSG_COUNT k_ei<<<interior_grid(d, kBlk), kBlk, 0, st>>>(ei, a, b, c, d, k_gas, k_liq, e_gas, e_liq);
   return cudaGetLastError();
 }
 

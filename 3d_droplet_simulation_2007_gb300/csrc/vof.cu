@@ -136,6 +136,15 @@ __global__ void k_swp_flux(const double *__restrict__ us, const double *__restri
           2.0 * (C(-1, 0, 1) + C(1, 0, 1) + C(0, -1, 1) + C(0, 1, 1)) + 4.0 * C(0, 0, 1);
     mz = mm1 - mm2;
 #undef C
+    if (mx == 0.0 && my == 0.0 && mz == 0.0) {
+      // Deviation from swp: a symmetric neighbourhood gives an all-zero Youngs
+      // normal, for which FL3D divides 0/0.  Such a cell is advected as a
+      // uniformly filled one (donor-cell fluxes scaled by c).
+      vof1[q] = c0 * dmax1(-a1, 0.0);
+      vof2[q] = c0 * (1.0 - dmax1(a1, 0.0) + dmin1(a2, 0.0));
+      vof3[q] = c0 * dmax1(a2, 0.0);
+      return;
+    }
     double invx = 1.0, invy = 1.0, invz = 1.0;
     if (mx < 0.0) { mx = -mx; invx = -1.0; }
     if (my < 0.0) { my = -my; invy = -1.0; }

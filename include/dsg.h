@@ -153,6 +153,7 @@ typedef struct dsg_profile {
   int64_t relax_calls; /* finest-level relax calls timed with CUDA events */
   double relax_ms;     /* summed event time of those calls */
   double relax_bytes;  /* their algorithmic bytes: 6 words (u r+w, a, b, c, rhs) per cell */
+  int relax_bits;      /* word size of the timed relax: 64 (FP64 modes) or 32 (mixed modes) */
 } dsg_profile;
 /* Start (on=1, counters reset) or stop live profiling of the context. */
 int dsg_profile_enable(dsg_ctx *ctx, int on);

@@ -706,6 +706,16 @@ void ora_swp(ora_state *st, const double *us, double *cc, double *vof1, double *
                 2.0 * (C(-1, 0, 1) + C(1, 0, 1) + C(0, -1, 1) + C(0, 1, 1)) + 4.0 * C(0, 0, 1);
           mz = mm1 - mm2;
 #undef C
+          if (mx == 0.0 && my == 0.0 && mz == 0.0) {
+            /* DEVIATION (documented): a symmetric 27-point neighbourhood gives
+             * an all-zero Youngs normal; AL3D then returns 0 and FL3D divides
+             * 0/0 (NaN in the reference too).  The cell is advected as a
+             * uniformly filled cell: donor-cell fluxes scaled by c. */
+            vof1[q] = c0 * dmax1(-a1, 0.0);
+            vof2[q] = c0 * (1.0 - dmax1(a1, 0.0) + dmin1(a2, 0.0));
+            vof3[q] = c0 * dmax1(a2, 0.0);
+            continue;
+          }
           int invx = 1, invy = 1, invz = 1;
           if (mx < 0.0) { mx = -mx; invx = -1; }
           if (my < 0.0) { my = -my; invy = -1; }

@@ -59,3 +59,26 @@ def test_noncubic_step(gpu_lib):
         gpu.step(t)
     for name in ["cc", "u", "v", "w", "p"]:
         assert relerr(gpu.field(name), ora.field(name)) <= FIELD_TOL, name
+
+
+def test_isolated_interface_cell(gpu_lib):
+    """An isolated partial cell has an all-zero Youngs normal (FL3D would
+    divide 0/0); GPU and oracle both advect it as a uniformly filled cell."""
+    dsg = gpu_lib
+    from oracle import Oracle
+    inp = dsg.config.droplet(16, noise_si=0.0)
+    ora, gpu = Oracle(inp.as_dict()), dsg.Solver(inp, init=False)
+    shape = ora.shape
+    rng = np.random.default_rng(7)
+    cc = np.zeros(shape)
+    cc[8, 8, 8] = 0.3
+    cc[4, 12, 9] = 0.7
+    for name, val in (("cc", cc), ("u", rng.uniform(-1, 1, shape)), ("v", rng.uniform(-1, 1, shape)),
+                      ("w", rng.uniform(-1, 1, shape))):
+        ora.field(name)[:] = val
+        gpu.set_field(name, val)
+    ora.vofmethod()
+    gpu.vofmethod()
+    g, o = gpu.field("cc"), ora.field("cc")
+    assert np.all(np.isfinite(o)) and np.all(np.isfinite(g))
+    assert relerr(g, o) <= FIELD_TOL
