@@ -82,3 +82,29 @@ def test_isolated_interface_cell(gpu_lib):
     g, o = gpu.field("cc"), ora.field("cc")
     assert np.all(np.isfinite(o)) and np.all(np.isfinite(g))
     assert relerr(g, o) <= FIELD_TOL
+
+
+def test_step_against_golden_fixture(gpu_lib):
+    """The CUDA path reproduces the committed oracle fixture of a 16^3 droplet
+    (3 steps) within 1e-10 of each field's max-norm."""
+    import json
+    import os
+    dsg = gpu_lib
+    from golden.make_golden import FIELDS, droplet16, field_digest
+    with open(os.path.join(os.path.dirname(__file__), "golden", "step16.json")) as f:
+        ref = json.load(f)["values"]
+    gpu = dsg.Solver(droplet16())
+    for t in (1, 2, 3):
+        gpu.step(t)
+        for name in FIELDS:
+            a = gpu.field(name)
+            n = a.size
+            got = [float.fromhex(x) for x in field_digest(a)]
+            exp = [float.fromhex(x) for x in ref["t%d_%s" % (t, name)]]
+            scale = max(exp[2], 1e-300)
+            tols = [1e-10 * scale * n, 1e-10 * scale * scale * n] + [1e-10 * scale] * (len(exp) - 2)
+            for g, e, tol in zip(got, exp, tols):
+                assert abs(g - e) <= tol, (t, name, g, e)
+        vol = float.fromhex(ref["t%d_volume" % t])
+        assert abs(gpu.liquid_volume() - vol) <= 1e-12 * vol
+        assert gpu.scalars().tau == float.fromhex(ref["t%d_tau" % t])
