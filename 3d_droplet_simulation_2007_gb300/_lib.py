@@ -122,6 +122,7 @@ SIGNATURES = [
     ("dsg_bc_resid", _i, [_dp, _i, _i, _i, _vp]),
     ("dsg_bc_out", _i, [_dp, _i, _i, _i, _vp]),
     ("dsg_filterc27", _i, [_dp, _dp, _i, _i, _i, _vp]),
+    ("dsg_mglin_noalloc", _i, [_dp] * 6 + [_i] * 7 + [_d] * 3 + [_vp]),
 ]
 
 _LIB = None

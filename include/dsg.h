@@ -189,6 +189,25 @@ int dsg_bc_out(double *s, int nx, int ny, int nz, void *stream);
 /* filterc27 main.f:5473-5511 */
 int dsg_filterc27(const double *cc, double *cf, int nx, int ny, int nz, void *stream);
 
+/* ---- allocation-free pressure solve -------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory when they solve (a host that owns its device arrays under an
+ * allocator that forbids cudaMalloc after set-up, or a solve inside a region
+ * where an allocation would synchronize the device): the fixed-cycle FMG of
+ * mglin (main.f:3645-3763, same kernels and result as dsg_mglin in
+ * DSG_MODE_REF_EXACT) on caller-owned device arrays p (in/out: overwritten,
+ * ghosts included), rhs, a, b, c, ei of size nx*ny*nz.  Coarse levels and the
+ * finest residual live in one static device array sized for grids up to
+ * 66x66x66 nodes (about 5.3 MB, held on every device that loads the library
+ * until exit); larger grids return DSG_E_ARG.  Nothing is allocated.  Calls
+ * share that array: each call clears it first, but calls that overlap on the
+ * GPU race and must be serialized.  The first call on a device looks up the
+ * array's address with that device current; make it before any stream
+ * capture. */
+int dsg_mglin_noalloc(double *p, const double *rhs, const double *a, const double *b, const double *c,
+                      const double *ei, int nx, int ny, int nz, int cycles, int npre, int npost, int ntop,
+                      double omega, double lengthsize, double lengthscale, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
