@@ -43,6 +43,7 @@ class DsgConfig(C.Structure):
         ("tsave", C.c_int), ("surfacet", C.c_int),
         ("mode", C.c_int), ("tol", C.c_double), ("max_vcycles", C.c_int),
         ("noise_si", C.c_double), ("noise_seed", C.c_uint64),
+        ("inner_vcycles", C.c_int), ("use_graphs", C.c_int),
     ]
 
 
@@ -64,10 +65,14 @@ class DsgScalars(C.Structure):
 class DsgProfile(C.Structure):
     """struct dsg_profile."""
     _fields_ = [("launches", C.c_int64), ("relax_calls", C.c_int64), ("relax_ms", C.c_double),
-                ("relax_bytes", C.c_double), ("relax_bits", C.c_int)]
+                ("relax_bytes", C.c_double), ("relax_bits", C.c_int), ("phase_ms", C.c_double * 6)]
+
+    PHASES = ("vof", "cfl", "csf", "momentum", "pressure", "projection")
 
     def as_dict(self):
-        return {n: getattr(self, n) for n, _ in self._fields_}
+        d = {n: getattr(self, n) for n, _ in self._fields_ if n != "phase_ms"}
+        d["phase_ms"] = dict(zip(self.PHASES, list(self.phase_ms)))
+        return d
 
 
 class DsgMgStats(C.Structure):

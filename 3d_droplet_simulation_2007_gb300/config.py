@@ -81,6 +81,8 @@ class InputData:
     max_vcycles: int = 200
     noise_si: float = 0.0
     noise_seed: int = 0
+    inner_vcycles: int = 2
+    use_graphs: int = 1
 
     def as_dict(self):
         return asdict(self)

@@ -99,6 +99,22 @@ int read_device(dsg_ctx *ctx, int n) {
   return DSG_OK;
 }
 
+// Phase marker of the live profile: the phase `id` starts here (-1: the step ends).
+cudaError_t phase_mark(dsg_ctx *ctx, int id) {
+  if (!ctx->prof) return cudaSuccess;
+  if (ctx->phase_used >= ctx->phase_ev.size()) {
+    for (int q = 0; q < 64; q++) {
+      cudaEvent_t e;
+      cudaError_t r = cudaEventCreate(&e);
+      if (r != cudaSuccess) return r;
+      ctx->phase_ev.push_back(e);
+      ctx->phase_id.push_back(-1);
+    }
+  }
+  ctx->phase_id[ctx->phase_used] = id;
+  return cudaEventRecord(ctx->phase_ev[ctx->phase_used++], ctx->stream);
+}
+
 // relax_n on level jj; the finest level is timed with an event pair when the
 // live profile is on.
 cudaError_t relax_level(dsg_ctx *ctx, int n, int jj, double ls) {
@@ -201,6 +217,28 @@ cudaError_t relax32_level(dsg_ctx *ctx, int n, int l) {
   const Dims d = ctx->level(l);
   const bool fine = l == ctx->ng;
   const bool timed = ctx->prof && fine && n > 0;
+  if (timed && ctx->cap) {
+    // inside a graph capture: the event pair becomes two record nodes, read
+    // back after every replay (graph_run)
+    cudaEvent_t e0, e1;
+    cudaError_t r = cudaEventCreate(&e0);
+    if (r == cudaSuccess) r = cudaEventCreate(&e1);
+    if (r != cudaSuccess) return r;
+    ctx->cap->ev.push_back(e0);
+    ctx->cap->ev.push_back(e1);
+    ctx->cap->ev_n.push_back(n);
+    // External records become event-record nodes that run on every replay
+    // (a plain record during capture only marks a dependency).
+    r = cudaEventRecordWithFlags(e0, ctx->stream, cudaEventRecordExternal);
+    if (r != cudaSuccess) return r;
+    FineSplit f = fine_split(ctx);
+    float r1, r2;
+    phase_coefs(ctx, &r1, &r2);
+    cudaError_t e =
+        dsg::relax32_split_n(n, f.u, f.r, L[A32], d, level_h2(ctx, l), (float)ctx->cfg.omega, r1, r2, ctx->stream);
+    if (e != cudaSuccess) return e;
+    return cudaEventRecordWithFlags(e1, ctx->stream, cudaEventRecordExternal);
+  }
   if (timed) {
     if (ctx->prof_used + 2 > ctx->prof_ev.size()) {
       for (int q = 0; q < 256; q++) {
@@ -267,18 +305,100 @@ int vcycle32(dsg_ctx *ctx, int j) {
   return DSG_OK;
 }
 
-int defect_host(dsg_ctx *ctx, double *relres) {
+// FP64 defect into the FP32 finest rhs, its norms copied to the pinned host
+// buffer (no synchronization: capturable).
+int defect_launch(dsg_ctx *ctx) {
   double **L = ctx->lv[ctx->ng];
   FineSplit f = fine_split(ctx);
   DSG_CK(ctx, dsg::defect64(f.r, ctx->red_out, ctx->red_partials, L[1], L[3], L[4], L[5], L[6], ctx->fine(),
                             ctx->s.lengthsize, ctx->stream));
-  int rc = read_device(ctx, 2);
-  if (rc) return rc;
+  DSG_CK(ctx, cudaMemcpyAsync(ctx->red_host, ctx->red_out, 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                              ctx->stream));
+  return DSG_OK;
+}
+
+// Relative residual from the norms of the last defect (after a synchronization).
+int defect_read(dsg_ctx *ctx, double *relres) {
   const double rr = ctx->red_host[0], bb = ctx->red_host[1];
   if (!isfinite(rr) || !isfinite(bb))
     return dsg::set_error(ctx, DSG_E_NONFINITE, "non-finite defect norm (%g, %g)", rr, bb);
   *relres = bb > 0.0 ? sqrt(rr) / sqrt(bb) : sqrt(rr);
   return DSG_OK;
+}
+
+int defect_host(dsg_ctx *ctx, double *relres) {
+  int rc = defect_launch(ctx);
+  if (rc) return rc;
+  DSG_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  return defect_read(ctx, relres);
+}
+
+void graph_release(GraphRec &g) {
+  if (g.exec) cudaGraphExecDestroy(g.exec);
+  g.exec = nullptr;
+  for (cudaEvent_t e : g.ev) cudaEventDestroy(e);
+  g.ev.clear();
+  g.ev_n.clear();
+  for (int q = 0; q < 6; q++) g.key[q] = -1;
+}
+
+// Capture `body` (a sequence of launches on ctx->stream) into g; returns 1 if
+// the stream cannot be captured (the caller then launches directly).
+template <class F>
+int graph_capture(dsg_ctx *ctx, GraphRec &g, const int key[6], F body) {
+  graph_release(g);
+  if (cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+    cudaGetLastError();
+    return 1;
+  }
+  ctx->cap = &g;
+  const long long launches0 = dsg::g_launches.load();
+  int rc = body();
+  // launches made while capturing became graph nodes: count them per replay
+  g.kernels = dsg::g_launches.load() - launches0;
+  dsg::g_launches.fetch_sub(g.kernels);
+  ctx->cap = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+  if (rc || e != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    graph_release(g);
+    if (rc) return rc;
+    return dsg::cuda_fail(ctx, e, "cudaStreamEndCapture");
+  }
+  e = cudaGraphInstantiate(&g.exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    graph_release(g);
+    return dsg::cuda_fail(ctx, e, "cudaGraphInstantiate");
+  }
+  for (int q = 0; q < 6; q++) g.key[q] = key[q];
+  return DSG_OK;
+}
+
+// Replay g and wait for it; accumulate the relax times recorded inside it.
+int graph_run(dsg_ctx *ctx, GraphRec &g) {
+  DSG_CK(ctx, cudaGraphLaunch(g.exec, ctx->stream));
+  dsg::g_launches.fetch_add(g.kernels);
+  DSG_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  if (ctx->prof) {
+    for (size_t q = 0; q < g.ev_n.size(); q++) {
+      float x = 0.f;
+      DSG_CK(ctx, cudaEventElapsedTime(&x, g.ev[2 * q], g.ev[2 * q + 1]));
+      ctx->prof_graph_relax_ms += x;
+      ctx->prof_relax_calls += g.ev_n[q];
+      ctx->prof_relax_bytes += (double)g.ev_n[q] * 6.0 * sizeof(float) * (double)ctx->fine().count();
+      ctx->prof_relax_bits = 32;
+    }
+  }
+  return DSG_OK;
+}
+
+bool graph_matches(const GraphRec &g, const int key[6]) {
+  if (!g.exec) return false;
+  for (int q = 0; q < 6; q++)
+    if (g.key[q] != key[q]) return false;
+  return true;
 }
 
 // FP32 hierarchy: cc in FP32 on the finest level (its relax forms the face
@@ -331,24 +451,61 @@ int mixed_solve(dsg_ctx *ctx, dsg_mg_stats *s) {
   if ((ctx->nx - 2) & 1)
     return dsg::set_error(ctx, DSG_E_ARG, "mixed mode needs an even number of interior cells along x (%d)",
                           ctx->nx - 2);
-  int rc = coef_hierarchy32(ctx);
-  if (rc) return rc;
-  rc = fmg32(ctx);
+  const int inner = ctx->cfg.inner_vcycles > 0 ? ctx->cfg.inner_vcycles : 1;
+  const int key[6] = {ctx->s.npre, ctx->s.npost, ctx->s.ntop, ctx->cfg.cycles, inner, ctx->prof ? 1 : 0};
+  // start: FP32 coefficient hierarchy, FP32 FMG guess, first FP64 defect
+  auto first = [&]() -> int {
+    int q = coef_hierarchy32(ctx);
+    if (q) return q;
+    q = fmg32(ctx);
+    if (q) return q;
+    return defect_launch(ctx);
+  };
+  // one outer iteration: `inner` FP32 V-cycles on the correction equation,
+  // FP64 accumulation, FP64 defect and its norms
+  auto iterate = [&]() -> int {
+    FineSplit f = fine_split(ctx);
+    DSG_CK(ctx, cudaMemsetAsync(f.u[0], 0, fine_split_bytes(ctx), st));
+    for (int q = 0; q < inner; q++) {
+      int e = vcycle32(ctx, ng);
+      if (e) return e;
+    }
+    DSG_CK(ctx, dsg::correct64(ctx->lv[ng][1], f.u, ctx->fine(), 0, st));
+    return defect_launch(ctx);
+  };
+  // Run a phase as a replayed CUDA graph (captured once per sweep-count key),
+  // or by direct launches when graphs are off or the stream cannot be captured.
+  auto run = [&](GraphRec &g, auto &body) -> int {
+    if (ctx->cfg.use_graphs) {
+      if (!graph_matches(g, key)) {
+        int q = graph_capture(ctx, g, key, body);
+        if (q < 0) return q;
+        if (q == 1) {
+          ctx->cfg.use_graphs = 0;  // stream not capturable: launch directly from now on
+          goto direct;
+        }
+      }
+      return graph_run(ctx, g);
+    }
+  direct:
+    int q = body();
+    if (q) return q;
+    DSG_CK(ctx, cudaStreamSynchronize(st));
+    return DSG_OK;
+  };
+  int rc = run(ctx->g_first, first);
   if (rc) return rc;
   double r;
-  rc = defect_host(ctx, &r);
+  rc = defect_read(ctx, &r);
   if (rc) return rc;
   s->relres_init = r;
   int n = 0;
   while (r >= ctx->cfg.tol && n < ctx->cfg.max_vcycles) {
-    FineSplit f = fine_split(ctx);
-    DSG_CK(ctx, cudaMemsetAsync(f.u[0], 0, fine_split_bytes(ctx), st));
-    rc = vcycle32(ctx, ng);
+    rc = run(ctx->g_iter, iterate);
     if (rc) return rc;
-    DSG_CK(ctx, dsg::correct64(ctx->lv[ng][1], f.u, ctx->fine(), 0, st));
-    s->fine_sweeps += ctx->s.npre + ctx->s.npost;
-    n++;
-    rc = defect_host(ctx, &r);
+    s->fine_sweeps += inner * (ctx->s.npre + ctx->s.npost);
+    n += inner;
+    rc = defect_read(ctx, &r);
     if (rc) return rc;
   }
   DSG_CK(ctx, dsg::bc_scalar(ctx->lv[ng][1], ctx->fine(), st));
@@ -546,6 +703,9 @@ void dsg_destroy(dsg_ctx *ctx) {
   if (!ctx) return;
   if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
   for (cudaEvent_t e : ctx->prof_ev) cudaEventDestroy(e);
+  for (cudaEvent_t e : ctx->phase_ev) cudaEventDestroy(e);
+  graph_release(ctx->g_first);
+  graph_release(ctx->g_iter);
   if (ctx->arena) cudaFree(ctx->arena);
   if (ctx->red_host) cudaFreeHost(ctx->red_host);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
@@ -708,6 +868,7 @@ int dsg_solvelpres(dsg_ctx *ctx, int t, dsg_mg_stats *stats) {
   double r2 = 2.0 * tauh2 * mu2;
   const double stdgrav = s.g * (s.tau * s.tau) / s.h;
   const double horgrav = s.g1 * (s.tau * s.tau) / s.h;
+  DSG_CK(ctx, phase_mark(ctx, 3));
   DSG_CK(ctx, dsg::stress(S.p, u, v, w, cc, d, r1, r2, r10, r20, st));
   DSG_CK(ctx, dsg::bc_tensor(S.p, d, st));
   r2 = s.rho2;
@@ -721,9 +882,11 @@ int dsg_solvelpres(dsg_ctx *ctx, int t, dsg_mg_stats *stats) {
   DSG_CK(ctx, dsg::divergence(w3, u, v, w, d, hi2, st));
   dsg_mg_stats ms;
   memset(&ms, 0, sizeof ms);
+  DSG_CK(ctx, phase_mark(ctx, 4));
   int rc = mglin(ctx, &ms);
   if (rc && rc != DSG_E_NOT_CONVERGED) return rc;
   const int mg_rc = rc;
+  DSG_CK(ctx, phase_mark(ctx, 5));
   DSG_CK(ctx, cudaMemcpyAsync(ctx->f[DSG_F_PPREV], w1, d.count() * sizeof(double), cudaMemcpyDeviceToDevice, st));
   DSG_CK(ctx, dsg::project(u, v, w, w1, a, b, c, d, st));
   DSG_CK(ctx, dsg::bc_v(u, v, w, ctx->red_partials, d, s.xvel2, st));
@@ -755,13 +918,18 @@ int dsg_solvelpres(dsg_ctx *ctx, int t, dsg_mg_stats *stats) {
 
 int dsg_step(dsg_ctx *ctx, int t, dsg_mg_stats *stats) {
   if (!ctx) return DSG_E_ARG;
+  DSG_CK(ctx, phase_mark(ctx, 0));
   int rc = dsg_vofmethod(ctx);
   if (rc) return rc;
+  DSG_CK(ctx, phase_mark(ctx, 1));
   rc = dsg_checktime(ctx);
   if (rc) return rc;
+  DSG_CK(ctx, phase_mark(ctx, 2));
   rc = dsg_csf(ctx);
   if (rc) return rc;
-  return dsg_solvelpres(ctx, t, stats);
+  rc = dsg_solvelpres(ctx, t, stats);
+  DSG_CK(ctx, phase_mark(ctx, -1));
+  return rc;
 }
 
 int dsg_liquid_volume(dsg_ctx *ctx, double *out) {
@@ -797,6 +965,8 @@ int dsg_profile_enable(dsg_ctx *ctx, int on) {
   ctx->prof_used = 0;
   ctx->prof_relax_calls = 0;
   ctx->prof_relax_bytes = 0.0;
+  ctx->phase_used = 0;
+  ctx->prof_graph_relax_ms = 0.0;
   ctx->prof_launch0 = dsg::g_launches.load();
   return DSG_OK;
 }
@@ -812,9 +982,17 @@ int dsg_profile_read(dsg_ctx *ctx, dsg_profile *out) {
   }
   out->launches = dsg::g_launches.load() - ctx->prof_launch0;
   out->relax_calls = ctx->prof_relax_calls;
-  out->relax_ms = ms;
+  out->relax_ms = ms + ctx->prof_graph_relax_ms;
   out->relax_bytes = ctx->prof_relax_bytes;
   out->relax_bits = ctx->prof_relax_bits;
+  for (int p = 0; p < 6; p++) out->phase_ms[p] = 0.0;
+  for (size_t q = 0; q + 1 < ctx->phase_used; q++) {
+    const int id = ctx->phase_id[q];
+    if (id < 0 || id > 5) continue;
+    float x = 0.f;
+    DSG_CK(ctx, cudaEventElapsedTime(&x, ctx->phase_ev[q], ctx->phase_ev[q + 1]));
+    out->phase_ms[id] += x;
+  }
   return DSG_OK;
 }
 

@@ -137,6 +137,16 @@ cudaError_t init_drop(double *cc, double *u, double *v, double *w, Dims d, doubl
 }  // namespace dsg
 
 // ---- context ---------------------------------------------------------------
+// A captured CUDA graph of the mixed-mode pressure solve and the finest-level
+// relax event pairs recorded inside it (read back after each replay).
+struct GraphRec {
+  cudaGraphExec_t exec = nullptr;
+  int key[6] = {-1, -1, -1, -1, -1, -1};  // npre, npost, ntop, cycles, inner, profiling
+  std::vector<cudaEvent_t> ev;             // start/end event pairs of finest-level relax calls
+  std::vector<int> ev_n;                   // relax calls timed by each pair
+  long long kernels = 0;                   // kernel nodes in the graph (counted per replay)
+};
+
 struct dsg_ctx {
   dsg_config cfg;
   dsg_scalars s;
@@ -164,6 +174,12 @@ struct dsg_ctx {
   long long prof_relax_calls = 0;
   double prof_relax_bytes = 0.0;
   int prof_relax_bits = 64;
+  double prof_graph_relax_ms = 0.0;   // relax time read back from graph replays
+  GraphRec g_first, g_iter;           // FP32 FMG start + first defect; one outer iteration
+  GraphRec *cap = nullptr;            // graph under capture
+  std::vector<cudaEvent_t> phase_ev;  // phase markers of dsg_step (event pool)
+  std::vector<int> phase_id;          // phase that starts at each marker, -1 = end
+  size_t phase_used = 0;
   dsg::Dims fine() const { return dsg::Dims{nx, ny, nz}; }
   dsg::Dims level(int l) const { return dsg::Dims{lnx[l], lny[l], lnz[l]}; }
 };

@@ -40,6 +40,8 @@ def parse():
     ap.add_argument("--n", type=int, default=256, help="interior cells per side")
     ap.add_argument("--mode", default="best", help="best|tol_fp64|tol_mixed|learned|ref_exact")
     ap.add_argument("--tol", type=float, default=1e-8)
+    ap.add_argument("--inner", type=int, default=2, help="FP32 V-cycles per FP64 defect (mixed modes)")
+    ap.add_argument("--no-graphs", action="store_true", help="launch the mixed solve without CUDA graphs")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -54,10 +56,10 @@ def dist_env():
     return ws, rank, local
 
 
-def workload(dsg, n, mode, tol):
+def workload(dsg, n, mode, tol, inner=2, graphs=True):
     cfg = dsg.config
     return cfg.droplet(n, steps=1000, impact_speed=3.0, noise_si=1e-4, mode=mode, tol=tol,
-                       npre=4, npost=4, ntop=4)
+                       npre=4, npost=4, ntop=4).replace(inner_vcycles=inner, use_graphs=1 if graphs else 0)
 
 
 def measured_peaks():
@@ -186,6 +188,8 @@ def run_gb300(args):
     import torch
     ws, rank, local = dist_env()
     torch.cuda.set_device(local)
+    # one dedicated stream for the library and the timing events
+    torch.cuda.set_stream(torch.cuda.Stream())
     dist = None
     if ws > 1:
         import torch.distributed as dist
@@ -193,7 +197,7 @@ def run_gb300(args):
     dsg = importlib.import_module(PKG)
     dsg.load()
     mode = mode_of(dsg, args.mode)
-    inp = workload(dsg, args.n, mode, args.tol)
+    inp = workload(dsg, args.n, mode, args.tol, args.inner, not args.no_graphs)
     solver = dsg.Solver(inp)
     solver.set_stream(torch.cuda.current_stream().cuda_stream)
     for t in range(1, args.warmup + 1):
@@ -267,11 +271,12 @@ def run_gb300(args):
             per_call_ms = prof["relax_ms"] / prof["relax_calls"]
             per_call_bytes = prof["relax_bytes"] / prof["relax_calls"]
             achieved = per_call_bytes / (per_call_ms / 1e3) / 1e9
-        fused = prof.get("relax_bits") == 32
-        kname = "k_relax32_fine" if fused else "k_relax_colour"
+        split = prof.get("relax_bits") == 32
+        kname = "k_relax32_split" if split else "k_relax_colour"
         traffic = committed_traffic(kname, args.n)
         roof = {"bound": "hbm",
-                "kernel": ("finest-level relax, fused red-black FP32 sweep (u r+w, cc, rhs: 16 B/cell)" if fused
+                "kernel": ("finest-level relax, colour-split FP32 red-black sweep, 2 launches per relax "
+                           "(other colour, own colour r+w, own rhs, cc: 24 B/cell)" if split
                            else "finest-level relax, 2 red-black FP64 colour passes (6 words/cell)"),
                 "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": (achieved / peak) if achieved else None, "traffic": traffic,
@@ -292,6 +297,7 @@ def run_gb300(args):
                                  % (solver_bytes_estimate(inp) / 1e9),
                            "parallelism": "replicas" if ws > 1 else "single"},
                 "vcycles_per_step": vcycles, "gpu_launches": prof["launches"], "roofline": roof,
+                "phase_ms_per_step": {k: v / args.steps for k, v in prof["phase_ms"].items()},
                 "cpu_baseline": cb, "e2e": e2e, "clocks": clk}
         if plain:
             line["plain_fp64"] = plain

@@ -75,6 +75,8 @@ typedef struct dsg_config {
   int max_vcycles;     /* V-cycle / defect-correction cap of the tol modes */
   double noise_si;     /* half-width of the seeded uniform velocity noise [m/s] */
   uint64_t noise_seed; /* seed of the counter-based noise */
+  int inner_vcycles;   /* FP32 V-cycles per FP64 defect evaluation in the mixed modes (<= 0: 1) */
+  int use_graphs;      /* capture the mixed-mode iterations in CUDA graphs (1) or launch directly (0) */
 } dsg_config;
 
 /* Non-dimensional scalars and adaptive counters (COMMON /PHYSICS/, /DIFF/,
@@ -154,6 +156,10 @@ typedef struct dsg_profile {
   double relax_ms;     /* summed event time of those calls */
   double relax_bytes;  /* their algorithmic bytes: 6 words (u r+w, a, b, c, rhs) per cell */
   int relax_bits;      /* word size of the timed relax: 64 (FP64 modes) or 32 (mixed modes) */
+  /* CUDA-event time of the phases of dsg_step: 0 VOF advection, 1 CFL check,
+   * 2 CSF force, 3 momentum up to the divergence, 4 pressure solve,
+   * 5 projection and adaptivity */
+  double phase_ms[6];
 } dsg_profile;
 /* Start (on=1, counters reset) or stop live profiling of the context. */
 int dsg_profile_enable(dsg_ctx *ctx, int on);

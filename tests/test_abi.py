@@ -49,7 +49,7 @@ def test_struct_layouts_match_header():
             if not decl:
                 continue
             parts = decl.split(None, 1)
-            fields += [f.strip() for f in parts[1].split(",")]
+            fields += [f.strip().split("[")[0] for f in parts[1].split(",")]
         assert fields == [n for n, _ in pyst._fields_], cname
 
 
