@@ -79,7 +79,8 @@ class DsgMgStats(C.Structure):
     """struct dsg_mg_stats."""
     _fields_ = [("mode", C.c_int), ("vcycles", C.c_int), ("fine_sweeps", C.c_int),
                 ("relres_init", C.c_double), ("relres", C.c_double), ("converged", C.c_int),
-                ("fallback", C.c_int), ("epsdiv", C.c_double)]
+                ("fallback", C.c_int), ("epsdiv", C.c_double), ("relres_prev", C.c_double),
+                ("relres_net", C.c_double)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -128,6 +129,16 @@ SIGNATURES = [
     ("dsg_bc_out", _i, [_dp, _i, _i, _i, _vp]),
     ("dsg_filterc27", _i, [_dp, _dp, _i, _i, _i, _vp]),
     ("dsg_mglin_noalloc", _i, [_dp] * 6 + [_i] * 7 + [_d] * 3 + [_vp]),
+    ("dsg_net_param_count", C.c_int64, []),
+    ("dsg_net_create", _i, [_i, _i, _i, C.c_uint64, _PP]),
+    ("dsg_net_destroy", None, [_vp]),
+    ("dsg_net_device_bytes", C.c_int64, [_vp]),
+    ("dsg_net_get_params", _i, [_vp, _vp, C.c_int64]),
+    ("dsg_net_set_params", _i, [_vp, _vp, C.c_int64]),
+    ("dsg_net_forward_host", _i, [_vp, _vp, _vp]),
+    ("dsg_net_grad_host", _i, [_vp, _vp, _vp, C.POINTER(C.c_float), _vp]),
+    ("dsg_net_train_step", _i, [_vp, C.c_float, C.POINTER(C.c_float)]),
+    ("dsg_attach_net", _i, [_vp, _vp, _i]),
 ]
 
 _LIB = None

@@ -445,6 +445,18 @@ int fmg32(dsg_ctx *ctx) {
   return DSG_OK;
 }
 
+// After a solve: store (input features, solved correction) as the attached
+// network's training pair when recording is on.
+int record_pair(dsg_ctx *ctx) {
+  if (!ctx->net || !ctx->net_record) return DSG_OK;
+  double **F = ctx->lv[ctx->ng];
+  int rc = dsg::nn::net_features(ctx->net, F[0], F[3], ctx->f[DSG_F_PPREV], F[1], F[4], F[5], F[6], ctx->fine(),
+                                 ctx->s.lengthsize, ctx->stream);
+  if (rc) return rc;
+  dsg::nn::net_set_target(ctx->net, true, ctx->stream);
+  return DSG_OK;
+}
+
 int mixed_solve(dsg_ctx *ctx, dsg_mg_stats *s) {
   const int ng = ctx->ng;
   cudaStream_t st = ctx->stream;
@@ -493,11 +505,49 @@ int mixed_solve(dsg_ctx *ctx, dsg_mg_stats *s) {
     DSG_CK(ctx, cudaStreamSynchronize(st));
     return DSG_OK;
   };
-  int rc = run(ctx->g_first, first);
-  if (rc) return rc;
+  int rc;
   double r;
-  rc = defect_read(ctx, &r);
-  if (rc) return rc;
+  if (ctx->cfg.mode == DSG_MODE_LEARNED) {
+    // Guarded learned start: the previous-step pressure and the network's
+    // correction of it are both judged by their FP64 defect; the network's
+    // guess is kept only if it has the smaller relative residual.
+    if (!ctx->net) return dsg::set_error(ctx, DSG_E_STATE, "learned mode without an attached network");
+    double **F = ctx->lv[ng];
+    double *p = F[1], *pprev = ctx->f[DSG_F_PPREV];
+    const size_t bytes = ctx->fine().count() * sizeof(double);
+    rc = coef_hierarchy32(ctx);
+    if (rc) return rc;
+    DSG_CK(ctx, cudaMemcpyAsync(p, pprev, bytes, cudaMemcpyDeviceToDevice, st));
+    double r_prev, r_net;
+    rc = defect_host(ctx, &r_prev);
+    if (rc) return rc;
+    rc = dsg::nn::net_features(ctx->net, F[0], F[3], pprev, nullptr, F[4], F[5], F[6], ctx->fine(),
+                               ctx->s.lengthsize, st);
+    if (rc) return rc;
+    rc = dsg::nn::net_guess(ctx->net, p, pprev, ctx->fine(), ctx->s.lengthsize, st);
+    if (rc) return rc;
+    DSG_CK(ctx, dsg::bc_scalar(p, ctx->fine(), st));
+    rc = defect_host(ctx, &r_net);
+    if (rc) return rc;
+    if (r_net < r_prev) {
+      r = r_net;
+      s->fallback = 0;
+    } else {
+      DSG_CK(ctx, cudaMemcpyAsync(p, pprev, bytes, cudaMemcpyDeviceToDevice, st));
+      rc = defect_host(ctx, &r);
+      if (rc) return rc;
+      s->fallback = 1;
+    }
+    ctx->last_relres_prev = r_prev;
+    ctx->last_relres_net = r_net;
+    s->relres_prev = r_prev;
+    s->relres_net = r_net;
+  } else {
+    rc = run(ctx->g_first, first);
+    if (rc) return rc;
+    rc = defect_read(ctx, &r);
+    if (rc) return rc;
+  }
   s->relres_init = r;
   int n = 0;
   while (r >= ctx->cfg.tol && n < ctx->cfg.max_vcycles) {
@@ -520,7 +570,7 @@ int mglin(dsg_ctx *ctx, dsg_mg_stats *stats) {
   const double om = ctx->cfg.omega;
   cudaStream_t st = ctx->stream;
   int fine_sweeps = 0;
-  if (ctx->cfg.mode == DSG_MODE_TOL_MIXED) {
+  if (ctx->cfg.mode == DSG_MODE_TOL_MIXED || ctx->cfg.mode == DSG_MODE_LEARNED) {
     dsg_mg_stats s;
     memset(&s, 0, sizeof s);
     s.mode = ctx->cfg.mode;
@@ -528,6 +578,8 @@ int mglin(dsg_ctx *ctx, dsg_mg_stats *stats) {
     s.relres_init = -1.0;
     s.epsdiv = -1.0;
     int rc = mixed_solve(ctx, &s);
+    if (rc) return rc;
+    rc = record_pair(ctx);
     if (rc) return rc;
     ctx->s.last_vcycles = s.vcycles;
     ctx->s.last_relres = s.relres;
@@ -586,7 +638,9 @@ int mglin(dsg_ctx *ctx, dsg_mg_stats *stats) {
     ctx->s.last_vcycles = n;
     ctx->s.last_relres = r;
     ctx->s.last_relres_fmg = s.relres_init;
-  } else if (ctx->cfg.mode != DSG_MODE_REF_EXACT && ctx->cfg.mode != DSG_MODE_TOL_MIXED) {
+    int rr = record_pair(ctx);
+    if (rr) return rr;
+  } else if (ctx->cfg.mode != DSG_MODE_REF_EXACT) {
     return dsg::set_error(ctx, DSG_E_ARG, "pressure mode %d is not available in this build", ctx->cfg.mode);
   }
   s.fine_sweeps = fine_sweeps;
@@ -997,5 +1051,12 @@ int dsg_profile_read(dsg_ctx *ctx, dsg_profile *out) {
 }
 
 int64_t dsg_launch_count(void) { return dsg::g_launches.load(); }
+
+int dsg_attach_net(dsg_ctx *ctx, dsg_net *net, int record) {
+  if (!ctx) return dsg::set_error(nullptr, DSG_E_ARG, "null context");
+  ctx->net = net;
+  ctx->net_record = net ? record : 0;
+  return DSG_OK;
+}
 
 }  // extern "C"

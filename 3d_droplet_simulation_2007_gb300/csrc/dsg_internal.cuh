@@ -136,6 +136,18 @@ cudaError_t init_drop(double *cc, double *u, double *v, double *w, Dims d, doubl
 
 }  // namespace dsg
 
+struct dsg_net;
+namespace dsg {
+namespace nn {
+// nn.cu: features of the current pressure system into the network input (and
+// the training target when p is given); p = p_prev + network correction.
+int net_features(dsg_net *n, const double *cc, const double *rhs, const double *pprev, const double *p,
+                 const double *a, const double *b, const double *c, Dims d, double lengthsize, cudaStream_t st);
+int net_guess(dsg_net *n, double *p, const double *pprev, Dims d, double lengthsize, cudaStream_t st);
+void net_set_target(dsg_net *n, bool v, cudaStream_t st);
+}  // namespace nn
+}  // namespace dsg
+
 // ---- context ---------------------------------------------------------------
 // A captured CUDA graph of the mixed-mode pressure solve and the finest-level
 // relax event pairs recorded inside it (read back after each replay).
@@ -177,6 +189,10 @@ struct dsg_ctx {
   double prof_graph_relax_ms = 0.0;   // relax time read back from graph replays
   GraphRec g_first, g_iter;           // FP32 FMG start + first defect; one outer iteration
   GraphRec *cap = nullptr;            // graph under capture
+  dsg_net *net = nullptr;             // learned initial guess (DSG_MODE_LEARNED)
+  int net_record = 0;                 // store a training pair after every solve
+  double last_relres_prev = -1.0;     // learned mode: relres of the previous pressure
+  double last_relres_net = -1.0;      // learned mode: relres of the network's guess
   std::vector<cudaEvent_t> phase_ev;  // phase markers of dsg_step (event pool)
   std::vector<int> phase_id;          // phase that starts at each marker, -1 = end
   size_t phase_used = 0;

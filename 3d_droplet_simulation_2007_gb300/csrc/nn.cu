@@ -1,0 +1,983 @@
+// nn.cu -- the learned multigrid initial guess: a small 3D convolutional
+// U-Net (no reference counterpart) with hand-written BF16 tensor-core kernels.
+//
+// Network (~251k parameters), channels-last activations over the interior
+// cells (D x H x W, each a multiple of 8):
+//   E1 conv 3->16 + ReLU   (full resolution; input padded to 16 channels)
+//   E2 conv 16->32 + ReLU  (1/2, after 2x2x2 average pooling)
+//   E3 conv 32->64 + ReLU  (1/4)
+//   E4 conv 64->64 + ReLU  (1/8)
+//   D3 conv 64->32 + ReLU  on up(E4) + E3
+//   D2 conv 32->16 + ReLU  on up(D3) + E2
+//   D1 conv 16->1          on up(D2) + E1  (linear output, channel padded to 8)
+// All convolutions are 3x3x3, zero padded.  They run as implicit GEMMs on the
+// tensor cores with mma.sync m16n8k16 (BF16 inputs, FP32 accumulation):
+// M = voxels (16 per warp), N = output channels, K = 27 taps x input channels.
+// The backward pass uses the same kernel for the data gradient (flipped,
+// transposed weights) and a second implicit GEMM for the weight gradient
+// (M = input channels, N = output channels, K = voxels).
+#include <cuda_bf16.h>
+
+#include <math.h>
+#include <string.h>
+
+#include <vector>
+
+#include "dsg_internal.cuh"
+
+namespace dsg {
+namespace nn {
+
+typedef __nv_bfloat16 bf16;
+
+// ---- layer table -------------------------------------------------------------
+struct LayerDef {
+  int cin, cout;   // logical channels
+  int cinp, coutp; // padded channels (multiples of 16 / 8)
+  int level;       // resolution level (0 = full)
+  bool relu;
+};
+constexpr int kLayers = 7;
+constexpr LayerDef kDefs[kLayers] = {
+    {3, 16, 16, 16, 0, true},   // E1
+    {16, 32, 16, 32, 1, true},  // E2
+    {32, 64, 32, 64, 2, true},  // E3
+    {64, 64, 64, 64, 3, true},  // E4
+    {64, 32, 64, 32, 2, true},  // D3
+    {32, 16, 32, 16, 1, true},  // D2
+    {16, 1, 16, 8, 0, false},   // D1
+};
+
+// channels of a layer's output gradient (the output layer is padded to 16 so
+// its gradient feeds the 16-wide data/weight gradient GEMMs)
+inline int grad_ch(int l) { return kDefs[l].coutp < 16 ? 16 : kDefs[l].coutp; }
+
+inline long long layer_params(int l) { return 27LL * kDefs[l].cin * kDefs[l].cout + kDefs[l].cout; }
+constexpr long long kParams = 27LL * (3 * 16 + 16 * 32 + 32 * 64 + 64 * 64 + 64 * 32 + 32 * 16 + 16 * 1) +
+                              (16 + 32 + 64 + 64 + 32 + 16 + 1);
+#define DSG_NET_PARAMS ((size_t)dsg::nn::kParams)
+
+// ---- helpers -------------------------------------------------------------------
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void ldmatrix_x4(unsigned &r0, unsigned &r1, unsigned &r2, unsigned &r3, unsigned addr) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+               : "r"(addr));
+}
+
+__device__ __forceinline__ void ldmatrix_x4_trans(unsigned &r0, unsigned &r1, unsigned &r2, unsigned &r3,
+                                                  unsigned addr) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+               : "r"(addr));
+}
+
+__device__ __forceinline__ void ldmatrix_x2_trans(unsigned &r0, unsigned &r1, unsigned addr) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x2.trans.shared.b16 {%0,%1}, [%2];" : "=r"(r0), "=r"(r1) : "r"(addr));
+}
+
+__device__ __forceinline__ void mma_bf16(float (&c)[4], unsigned a0, unsigned a1, unsigned a2, unsigned a3,
+                                         unsigned b0, unsigned b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+// ---- convolution forward / data gradient (implicit GEMM) -----------------------
+// X: [D][H][W][CIN] bf16, Wp: packed B fragments [27][CIN/16][COUT/8][32 lanes] x uint2,
+// Y: [D][H][W][COUT] (bf16, or float when OUTF).  CTA = 8 warps, tile 16 (x) x 8 (y)
+// x 1 (z) voxels; warp w computes the 16 voxels of row y0+w for all COUT.
+// Tap t = (dz+1)*9 + (dy+1)*3 + (dx+1) reads X at (x+dx, y+dy, z+dz).
+constexpr int CTX = 16, CTY = 8;
+
+template <int CIN, int COUT, bool RELU, bool OUTF>
+__global__ void __launch_bounds__(256) k_conv3(const bf16 *__restrict__ X, const uint2 *__restrict__ Wp,
+                                               const float *__restrict__ bias, void *__restrict__ Yv, int W, int H,
+                                               int D) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  bf16 *tile = reinterpret_cast<bf16 *>(smem);  // [3][CTY+2][CTX+2][CIN]
+  constexpr int HX = CTX + 2, HY = CTY + 2;
+  const int x0 = blockIdx.x * CTX, y0 = blockIdx.y * CTY, z = blockIdx.z;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  // cooperative halo load, 16-byte vectors of 8 channels
+  constexpr int VPV = CIN / 8;  // vectors per voxel
+  const int nvec = 3 * HY * HX * VPV;
+  for (int e = tid; e < nvec; e += 256) {
+    const int c8 = e % VPV;
+    const int v = e / VPV;
+    const int hx = v % HX, hy = (v / HX) % HY, hz = v / (HX * HY);
+    const int gx = x0 + hx - 1, gy = y0 + hy - 1, gz = z + hz - 1;
+    uint4 val = make_uint4(0u, 0u, 0u, 0u);
+    if (gx >= 0 && gx < W && gy >= 0 && gy < H && gz >= 0 && gz < D)
+      val = reinterpret_cast<const uint4 *>(X + (((size_t)gz * H + gy) * W + gx) * CIN)[c8];
+    reinterpret_cast<uint4 *>(tile + (size_t)v * CIN)[c8] = val;
+  }
+  __syncthreads();
+  float acc[COUT / 8][4];
+#pragma unroll
+  for (int n = 0; n < COUT / 8; n++) acc[n][0] = acc[n][1] = acc[n][2] = acc[n][3] = 0.f;
+  // ldmatrix row owned by this lane: matrix mi = lane/8 -> A rows (mi&1)*8 + lane%8,
+  // channel offset (mi>>1)*8
+  const int arow = ((lane >> 3) & 1) * 8 + (lane & 7);
+  const int acol = (lane >> 4) * 8;
+  for (int tap = 0; tap < 27; tap++) {
+    const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;  // halo offsets 0..2
+    const int hv = (dz * HY + (warp + dy)) * HX + (arow + dx);
+    const unsigned abase = smem_u32(tile + (size_t)hv * CIN + acol);
+#pragma unroll
+    for (int kk = 0; kk < CIN / 16; kk++) {
+      unsigned a0, a1, a2, a3;
+      ldmatrix_x4(a0, a1, a2, a3, abase + kk * 32);
+      const uint2 *wp = Wp + ((size_t)(tap * (CIN / 16) + kk) * (COUT / 8)) * 32 + lane;
+#pragma unroll
+      for (int n = 0; n < COUT / 8; n++) {
+        const uint2 b = __ldg(wp + n * 32);
+        mma_bf16(acc[n], a0, a1, a2, a3, b.x, b.y);
+      }
+    }
+  }
+  // epilogue: rows g, g+8 of the warp's 16 voxels, columns n*8 + 2t, 2t+1
+  const int g = lane >> 2, t4 = lane & 3;
+  const int y = y0 + warp;
+  if (y >= H) return;
+#pragma unroll
+  for (int half = 0; half < 2; half++) {
+    const int x = x0 + g + half * 8;
+    if (x >= W) continue;
+    const size_t vox = ((size_t)z * H + y) * W + x;
+#pragma unroll
+    for (int n = 0; n < COUT / 8; n++) {
+      const int co = n * 8 + 2 * t4;
+      float v0 = acc[n][half * 2 + 0], v1 = acc[n][half * 2 + 1];
+      if (bias) {
+        v0 += bias[co];
+        v1 += bias[co + 1];
+      }
+      if (RELU) {
+        v0 = fmaxf(v0, 0.f);
+        v1 = fmaxf(v1, 0.f);
+      }
+      if (OUTF) {
+        float *Y = reinterpret_cast<float *>(Yv);
+        Y[vox * COUT + co] = v0;
+        Y[vox * COUT + co + 1] = v1;
+      } else {
+        bf16 *Y = reinterpret_cast<bf16 *>(Yv);
+        *reinterpret_cast<__nv_bfloat162 *>(Y + vox * COUT + co) = __floats2bfloat162_rn(v0, v1);
+      }
+    }
+  }
+}
+
+// ---- weight gradient (implicit GEMM over voxels) ----------------------------------
+// dW[tap][ci][co] += sum_v X[v + off(tap)][ci] * G[v][co].  A CTA takes a brick of
+// CTX x CTY x BZ voxels; warp w owns (tap, ci block) pairs w, w+8, ...; for each
+// pair it accumulates a 16 (ci) x COUT tile over the brick with A = X^T and
+// B = G loaded by ldmatrix.trans, then adds it to dW with atomics.
+constexpr int BZ = 4;
+
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(256) k_conv3_wgrad(const bf16 *__restrict__ X, const bf16 *__restrict__ G,
+                                                     float *__restrict__ dW, int W, int H, int D) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int HX = CTX + 2, HY = CTY + 2, HZ = BZ + 2;
+  bf16 *xt = reinterpret_cast<bf16 *>(smem);               // [HZ][HY][HX][CIN]
+  bf16 *gt = xt + (size_t)HZ * HY * HX * CIN;               // [BZ][CTY][CTX][COUT]
+  const int x0 = blockIdx.x * CTX, y0 = blockIdx.y * CTY, z0 = blockIdx.z * BZ;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  {
+    constexpr int VPV = CIN / 8;
+    const int nvec = HZ * HY * HX * VPV;
+    for (int e = tid; e < nvec; e += 256) {
+      const int c8 = e % VPV, v = e / VPV;
+      const int hx = v % HX, hy = (v / HX) % HY, hz = v / (HX * HY);
+      const int gx = x0 + hx - 1, gy = y0 + hy - 1, gz = z0 + hz - 1;
+      uint4 val = make_uint4(0u, 0u, 0u, 0u);
+      if (gx >= 0 && gx < W && gy >= 0 && gy < H && gz >= 0 && gz < D)
+        val = reinterpret_cast<const uint4 *>(X + (((size_t)gz * H + gy) * W + gx) * CIN)[c8];
+      reinterpret_cast<uint4 *>(xt + (size_t)v * CIN)[c8] = val;
+    }
+    constexpr int GPV = COUT / 8;
+    const int ngv = BZ * CTY * CTX * GPV;
+    for (int e = tid; e < ngv; e += 256) {
+      const int c8 = e % GPV, v = e / GPV;
+      const int bx = v % CTX, by = (v / CTX) % CTY, bz = v / (CTX * CTY);
+      const int gx = x0 + bx, gy = y0 + by, gz = z0 + bz;
+      uint4 val = make_uint4(0u, 0u, 0u, 0u);
+      if (gx < W && gy < H && gz < D) val = reinterpret_cast<const uint4 *>(G + (((size_t)gz * H + gy) * W + gx) * COUT)[c8];
+      reinterpret_cast<uint4 *>(gt + (size_t)v * COUT)[c8] = val;
+    }
+  }
+  __syncthreads();
+  constexpr int KB = CIN / 16;
+  const int npairs = 27 * KB;
+  // A = X^T (16 ci x 16 voxels): stored rows are voxels with ci contiguous, so
+  // ldmatrix.trans of the 4 8x8 blocks gives the row-major A fragment:
+  //   m0: ci 0-7,  v 0-7 ; m1: ci 8-15, v 0-7 ; m2: ci 0-7, v 8-15 ; m3: ci 8-15, v 8-15
+  // B = G (16 voxels x 8 co): stored rows are voxels with co contiguous; the
+  // col-major B fragment is ldmatrix.trans of blocks (v 0-7) and (v 8-15).
+  const int lrow = lane & 7, lmat = lane >> 3;
+  for (int pr = warp; pr < npairs; pr += 8) {
+    const int tap = pr / KB, kb = pr % KB;
+    const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
+    float acc[COUT / 8][4];
+#pragma unroll
+    for (int n = 0; n < COUT / 8; n++) acc[n][0] = acc[n][1] = acc[n][2] = acc[n][3] = 0.f;
+    for (int bz = 0; bz < BZ; bz++)
+      for (int by = 0; by < CTY; by++) {
+        // the 16 voxels of this k-step: x = 0..15 of row (by, bz)
+        const int av = lrow + ((lmat >> 1) << 3);        // voxel index for this lane's A row address
+        const int ach = kb * 16 + ((lmat & 1) << 3);     // ci offset
+        const int hv = ((bz + dz) * HY + (by + dy)) * HX + (av + dx);
+        unsigned a0, a1, a2, a3;
+        ldmatrix_x4_trans(a0, a1, a2, a3, smem_u32(xt + (size_t)hv * CIN + ach));
+        const int gvrow = (bz * CTY + by) * CTX;
+#pragma unroll
+        for (int n = 0; n < COUT / 8; n++) {
+          const int bvox = (lane & 15);
+          unsigned b0, b1;
+          ldmatrix_x2_trans(b0, b1, smem_u32(gt + (size_t)(gvrow + bvox) * COUT + n * 8));
+          mma_bf16(acc[n], a0, a1, a2, a3, b0, b1);
+        }
+      }
+    const int g = lane >> 2, t4 = lane & 3;
+#pragma unroll
+    for (int n = 0; n < COUT / 8; n++)
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const int ci = kb * 16 + g + (q >> 1) * 8;
+        const int co = n * 8 + 2 * t4 + (q & 1);
+        atomicAdd(dW + ((size_t)tap * CIN + ci) * COUT + co, acc[n][q]);
+      }
+  }
+}
+
+// ---- elementwise kernels ------------------------------------------------------
+// 2x2x2 average pooling, channels-last bf16.
+__global__ void k_pool(const bf16 *__restrict__ X, bf16 *__restrict__ Y, int W, int H, int D, int C) {
+  const int Wc = W / 2, Hc = H / 2, Dc = D / 2;
+  const size_t n = (size_t)Wc * Hc * Dc * C;
+  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+    const int c = (int)(q % C);
+    size_t v = q / C;
+    const int x = (int)(v % Wc), y = (int)((v / Wc) % Hc), z = (int)(v / ((size_t)Wc * Hc));
+    float s = 0.f;
+    for (int k = 0; k < 8; k++) {
+      const int xx = 2 * x + (k & 1), yy = 2 * y + ((k >> 1) & 1), zz = 2 * z + (k >> 2);
+      s += __bfloat162float(X[(((size_t)zz * H + yy) * W + xx) * C + c]);
+    }
+    Y[q] = __float2bfloat16(0.125f * s);
+  }
+}
+
+// Y = up(A) + B: A at half resolution, Y/B at full, channels-last bf16.
+__global__ void k_upadd(const bf16 *__restrict__ A, const bf16 *__restrict__ B, bf16 *__restrict__ Y, int W, int H,
+                        int D, int C) {
+  const size_t n = (size_t)W * H * D * C;
+  const int Wc = W / 2, Hc = H / 2;
+  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+    const int c = (int)(q % C);
+    size_t v = q / C;
+    const int x = (int)(v % W), y = (int)((v / W) % H), z = (int)(v / ((size_t)W * H));
+    const float a = __bfloat162float(A[(((size_t)(z >> 1) * Hc + (y >> 1)) * Wc + (x >> 1)) * C + c]);
+    Y[q] = __float2bfloat16(a + __bfloat162float(B[q]));
+  }
+}
+
+// Backward of Y = up(A) + B: dB = dY, dA = sum over the 8 children (FP32).
+__global__ void k_upadd_back(const bf16 *__restrict__ dY, float *__restrict__ dA, int W, int H, int D, int C) {
+  const int Wc = W / 2, Hc = H / 2, Dc = D / 2;
+  const size_t n = (size_t)Wc * Hc * Dc * C;
+  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+    const int c = (int)(q % C);
+    size_t v = q / C;
+    const int x = (int)(v % Wc), y = (int)((v / Wc) % Hc), z = (int)(v / ((size_t)Wc * Hc));
+    float s = 0.f;
+    for (int k = 0; k < 8; k++) {
+      const int xx = 2 * x + (k & 1), yy = 2 * y + ((k >> 1) & 1), zz = 2 * z + (k >> 2);
+      s += __bfloat162float(dY[(((size_t)zz * H + yy) * W + xx) * C + c]);
+    }
+    dA[q] = s;
+  }
+}
+
+// Backward of pooling: dX(child) += dY(parent)/8 (accumulates into an FP32 buffer).
+__global__ void k_pool_back_acc(const bf16 *__restrict__ dY, float *__restrict__ dX, int W, int H, int D, int C) {
+  const size_t n = (size_t)W * H * D * C;
+  const int Wc = W / 2, Hc = H / 2;
+  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+    const int c = (int)(q % C);
+    size_t v = q / C;
+    const int x = (int)(v % W), y = (int)((v / W) % H), z = (int)(v / ((size_t)W * H));
+    dX[q] += 0.125f * __bfloat162float(dY[(((size_t)(z >> 1) * Hc + (y >> 1)) * Wc + (x >> 1)) * C + c]);
+  }
+}
+
+// G = bf16(dAcc * (act > 0)) (ReLU derivative), also the bias gradient.
+__global__ void k_relu_back(const float *__restrict__ dacc, const bf16 *__restrict__ act, bf16 *__restrict__ G,
+                            float *__restrict__ dbias, size_t nvox, int C, int relu) {
+  __shared__ float sb[64];
+  if (threadIdx.x < 64) sb[threadIdx.x] = 0.f;
+  __syncthreads();
+  const size_t n = nvox * C;
+  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+    float g = dacc[q];
+    if (relu && !(__bfloat162float(act[q]) > 0.f)) g = 0.f;
+    G[q] = __float2bfloat16(g);
+    atomicAdd(&sb[q % C], g);
+  }
+  __syncthreads();
+  if (threadIdx.x < C) atomicAdd(&dbias[threadIdx.x], sb[threadIdx.x]);
+}
+
+// bf16 -> float accumulate: dst += src.
+__global__ void k_acc_bf16(float *__restrict__ dst, const bf16 *__restrict__ src, size_t n) {
+  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+    dst[q] += __bfloat162float(src[q]);
+}
+
+// Output layer loss: y (float, 8 padded channels, channel 0 used), target t.
+// loss = mean (y - t)^2 ; dY (16 channels) channel 0 = 2 (y - t) / N, others 0.
+__global__ void k_mse(const float *__restrict__ y, const float *__restrict__ t, float *__restrict__ dy,
+                      double *__restrict__ loss, size_t nvox) {
+  __shared__ double sh[256];
+  double s = 0.0;
+  for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < nvox; v += (size_t)gridDim.x * blockDim.x) {
+    const float d = y[v * 8] - t[v];
+    s += (double)d * d;
+#pragma unroll
+    for (int c = 0; c < 16; c++) dy[v * 16 + c] = c == 0 ? 2.f * d / (float)nvox : 0.f;
+  }
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int k = 128; k > 0; k >>= 1) {
+    if (threadIdx.x < k) sh[threadIdx.x] += sh[threadIdx.x + k];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) atomicAdd(loss, sh[0] / (double)nvox);
+}
+
+// Pack FP32 weights W[tap][ci][co] (logical sizes) into B fragments of the
+// forward conv (transpose=0) or of the data-gradient conv (transpose=1: uses
+// W[26-tap][co][ci], i.e. spatially flipped with in/out swapped).
+__global__ void k_pack(const float *__restrict__ Wt, uint2 *__restrict__ Wp, int cin, int cout, int kin, int kout,
+                       int transpose) {
+  // kin/kout: padded channel counts of the GEMM (K side / N side)
+  const int nfrag = 27 * (kin / 16) * (kout / 8) * 32;
+  for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nfrag; f += gridDim.x * blockDim.x) {
+    const int lane = f & 31;
+    int r = f >> 5;
+    const int n = r % (kout / 8);
+    r /= kout / 8;
+    const int kk = r % (kin / 16);
+    const int tap = r / (kin / 16);
+    const int g = lane >> 2, t4 = lane & 3;
+    float v[4];
+    for (int q = 0; q < 4; q++) {
+      const int k = kk * 16 + 2 * t4 + (q & 1) + (q >> 1) * 8;  // b0,b1: k=2t,2t+1 ; b2,b3: +8
+      const int nn = n * 8 + g;
+      float w = 0.f;
+      if (!transpose) {
+        if (k < cin && nn < cout) w = Wt[((size_t)tap * cin + k) * cout + nn];
+      } else {
+        // data gradient: K runs over the forward output channels, N over the inputs
+        if (k < cout && nn < cin) w = Wt[((size_t)(26 - tap) * cin + nn) * cout + k];
+      }
+      v[q] = w;
+    }
+    __nv_bfloat162 lo = __floats2bfloat162_rn(v[0], v[1]), hi = __floats2bfloat162_rn(v[2], v[3]);
+    Wp[f] = make_uint2(*reinterpret_cast<unsigned *>(&lo), *reinterpret_cast<unsigned *>(&hi));
+  }
+}
+
+// Adam step on FP32 master parameters.
+__global__ void k_adam(float *__restrict__ p, const float *__restrict__ g, float *__restrict__ m,
+                       float *__restrict__ v, size_t n, float lr, float b1, float b2, float eps, float c1, float c2,
+                       float clip) {
+  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+    float gq = g[q];
+    if (!isfinite(gq)) gq = 0.f;
+    gq = fmaxf(-clip, fminf(clip, gq));
+    const float mq = b1 * m[q] + (1.f - b1) * gq;
+    const float vq = b2 * v[q] + (1.f - b2) * gq * gq;
+    m[q] = mq;
+    v[q] = vq;
+    p[q] -= lr * (mq / c1) / (sqrtf(vq / c2) + eps);
+  }
+}
+
+// Network input from the solver fields (interior cells, channels-last, 16 padded
+// channels): c0 = volume fraction, c1 = rhs / s, c2 = (rhs - L p_prev) / s, where
+// s = RMS(rhs) is read from device memory.  Also writes the FP32 target
+// (p - p_prev) / (s h^2) when p is given (training snapshots).
+__global__ void k_features(bf16 *__restrict__ Xin, float *__restrict__ target, const double *__restrict__ cc,
+                           const double *__restrict__ rhs, const double *__restrict__ pprev,
+                           const double *__restrict__ p, const double *__restrict__ a, const double *__restrict__ b,
+                           const double *__restrict__ c, const double *__restrict__ sums, Dims d, double h2i,
+                           double h2) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  const int W = d.nx - 2, H = d.ny - 2;
+  if (x >= W || y >= H) return;
+  const int i = x + 2, j = y + 2, k = z + 2;
+  const size_t q = d.ix(i, j, k);
+  const size_t sy = d.sy(), sz = d.sz();
+  const double n_int = (double)W * H * (d.nz - 2);
+  const double s = sqrt(sums[0] / n_int) + 1e-300;
+  const double uc = pprev[q];
+  const double xp = (i + 1 == d.nx) ? 0.0 : pprev[q + 1];
+  const double xm = (i - 1 == 1) ? uc : pprev[q - 1];
+  const double yp = (j + 1 == d.ny) ? uc : pprev[q + sy];
+  const double ym = (j - 1 == 1) ? uc : pprev[q - sy];
+  const double zp = (k + 1 == d.nz) ? uc : pprev[q + sz];
+  const double zm = (k - 1 == 1) ? uc : pprev[q - sz];
+  const double r = -h2i * (a[q] * (xp - uc) + a[q - 1] * (xm - uc) + b[q] * (yp - uc) + b[q - sy] * (ym - uc) +
+                           c[q] * (zp - uc) + c[q - sz] * (zm - uc)) +
+                   rhs[q];
+  const size_t v = ((size_t)z * H + y) * W + x;
+  bf16 *o = Xin + v * 16;
+  o[0] = __float2bfloat16((float)cc[q]);
+  o[1] = __float2bfloat16((float)(rhs[q] / s));
+  o[2] = __float2bfloat16((float)(r / s));
+#pragma unroll
+  for (int ch = 3; ch < 16; ch++) o[ch] = __float2bfloat16(0.f);
+  if (target) target[v] = (float)((p[q] - uc) / (s * h2));
+}
+
+// p = p_prev + s h^2 q over the interior (q = network output, channel 0 of 8).
+__global__ void k_apply_guess(double *__restrict__ p, const double *__restrict__ pprev, const float *__restrict__ qout,
+                              const double *__restrict__ sums, Dims d, double h2) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  const int W = d.nx - 2, H = d.ny - 2;
+  if (x >= W || y >= H) return;
+  const double s = sqrt(sums[0] / ((double)W * H * (d.nz - 2))) + 1e-300;
+  const size_t q = d.ix(x + 2, y + 2, z + 2);
+  const size_t v = ((size_t)z * H + y) * W + x;
+  p[q] = pprev[q] + s * h2 * (double)qout[v * 8];
+}
+
+// sums[0] = sum of rhs^2 over the interior (single block per launch row, atomics).
+__global__ void k_sumsq(const double *__restrict__ f, double *__restrict__ sums, Dims d) {
+  __shared__ double sh[256];
+  const size_t n = (size_t)(d.nx - 2) * (d.ny - 2) * (d.nz - 2);
+  double s = 0.0;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t % (d.nx - 2)) + 2;
+    const size_t r = t / (d.nx - 2);
+    const int j = (int)(r % (d.ny - 2)) + 2, k = (int)(r / (d.ny - 2)) + 2;
+    const double v = f[d.ix(i, j, k)];
+    s += v * v;
+  }
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int k = 128; k > 0; k >>= 1) {
+    if (threadIdx.x < k) sh[threadIdx.x] += sh[threadIdx.x + k];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) atomicAdd(sums, sh[0]);
+}
+
+inline int eblocks(size_t n) { return (int)((n + 255) / 256 < 8192 ? (n + 255) / 256 : 8192); }
+
+}  // namespace nn
+}  // namespace dsg
+
+// ============================================================================
+// network object
+// ============================================================================
+using namespace dsg::nn;
+
+struct dsg_net {
+  int W[4], H[4], D[4];             // interior sizes per level
+  float *params = nullptr;          // FP32 master: per layer W[27][cin][cout] then bias[cout]
+  float *grad = nullptr, *adam_m = nullptr, *adam_v = nullptr;
+  uint2 *packf[kLayers], *packb[kLayers];  // packed forward / data-gradient B fragments
+  long long poff[kLayers];          // offset of each layer's weights in params
+  // activations (bf16 channels-last)
+  bf16 *x0;                          // input 16 ch, level 0
+  bf16 *e1, *p1, *e2, *p2, *e3, *p3, *e4;  // encoder
+  bf16 *u3, *d3, *u2, *d2, *u1;            // decoder inputs/outputs
+  float *yout;                      // output 8 ch (channel 0 used), level 0
+  float *target;                    // training target, level 0
+  // backward buffers
+  float *dy_out;                    // dL/dy (8 ch)
+  bf16 *gbuf, *gbuf2;               // bf16 gradients
+  float *acc_e1, *acc_e2, *acc_e3;  // FP32 gradients of the encoder activations
+  float *tmp;                       // FP32 gradient of a decoder output
+  float *wscratch;                  // bias (64) + padded weight gradient of one layer
+  float *xin_f32, *yhost_f32;       // staging of the host-array entry points
+  double *loss_dev, *sums_dev;      // loss; sum of rhs^2 of the current system
+  double *loss_host;
+  long long step = 0;               // Adam steps taken
+  bool have_target = false;         // a training pair is recorded
+  cudaStream_t stream = 0;          // stream of the attached context (training)
+  void *arena = nullptr;
+  size_t arena_bytes = 0;
+  std::string err;
+};
+
+namespace {
+
+template <int CIN, int COUT, bool RELU, bool OUTF>
+cudaError_t conv_launch(const bf16 *X, const uint2 *Wp, const float *bias, void *Y, int W, int H, int D,
+                        cudaStream_t st) {
+  const size_t smem = 3 * (CTY + 2) * (CTX + 2) * CIN * sizeof(bf16);
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_conv3<CIN, COUT, RELU, OUTF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  const dim3 grid((unsigned)((W + CTX - 1) / CTX), (unsigned)((H + CTY - 1) / CTY), (unsigned)D);
+  DSG_COUNT k_conv3<CIN, COUT, RELU, OUTF><<<grid, 256, smem, st>>>(X, Wp, bias, Y, W, H, D);
+  return cudaGetLastError();
+}
+
+template <int CIN, int COUT>
+cudaError_t wgrad_launch(const bf16 *X, const bf16 *G, float *dW, int W, int H, int D, cudaStream_t st) {
+  const size_t smem = ((size_t)(BZ + 2) * (CTY + 2) * (CTX + 2) * CIN + (size_t)BZ * CTY * CTX * COUT) * sizeof(bf16);
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e =
+        cudaFuncSetAttribute(k_conv3_wgrad<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  const dim3 grid((unsigned)((W + CTX - 1) / CTX), (unsigned)((H + CTY - 1) / CTY), (unsigned)((D + BZ - 1) / BZ));
+  DSG_COUNT k_conv3_wgrad<CIN, COUT><<<grid, 256, smem, st>>>(X, G, dW, W, H, D);
+  return cudaGetLastError();
+}
+
+// forward conv of layer l; data-gradient conv uses the same kernels with the
+// channel roles swapped (packb).
+cudaError_t conv_fwd(dsg_net *n, int l, const bf16 *X, void *Y, cudaStream_t st) {
+  const int lv = kDefs[l].level;
+  const int W = n->W[lv], H = n->H[lv], D = n->D[lv];
+  const float *bias = n->params + n->poff[l] + 27LL * kDefs[l].cin * kDefs[l].cout;
+  switch (l) {
+    case 0: return conv_launch<16, 16, true, false>(X, n->packf[0], bias, Y, W, H, D, st);
+    case 1: return conv_launch<16, 32, true, false>(X, n->packf[1], bias, Y, W, H, D, st);
+    case 2: return conv_launch<32, 64, true, false>(X, n->packf[2], bias, Y, W, H, D, st);
+    case 3: return conv_launch<64, 64, true, false>(X, n->packf[3], bias, Y, W, H, D, st);
+    case 4: return conv_launch<64, 32, true, false>(X, n->packf[4], bias, Y, W, H, D, st);
+    case 5: return conv_launch<32, 16, true, false>(X, n->packf[5], bias, Y, W, H, D, st);
+    default: return conv_launch<16, 8, false, true>(X, n->packf[6], bias, Y, W, H, D, st);
+  }
+}
+
+// data gradient of layer l: dX (bf16, cinp channels) from G (bf16, coutp channels)
+cudaError_t conv_dgrad(dsg_net *n, int l, const bf16 *G, bf16 *dX, cudaStream_t st) {
+  const int lv = kDefs[l].level;
+  const int W = n->W[lv], H = n->H[lv], D = n->D[lv];
+  switch (l) {
+    case 1: return conv_launch<32, 16, false, false>(G, n->packb[1], nullptr, dX, W, H, D, st);
+    case 2: return conv_launch<64, 32, false, false>(G, n->packb[2], nullptr, dX, W, H, D, st);
+    case 3: return conv_launch<64, 64, false, false>(G, n->packb[3], nullptr, dX, W, H, D, st);
+    case 4: return conv_launch<32, 64, false, false>(G, n->packb[4], nullptr, dX, W, H, D, st);
+    case 5: return conv_launch<16, 32, false, false>(G, n->packb[5], nullptr, dX, W, H, D, st);
+    case 6: return conv_launch<16, 16, false, false>(G, n->packb[6], nullptr, dX, W, H, D, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// weight gradient of layer l into n->grad (FP32 [27][cinp][coutp] scratch then folded)
+cudaError_t conv_wgrad(dsg_net *n, int l, const bf16 *X, const bf16 *G, float *dWpad, cudaStream_t st) {
+  const int lv = kDefs[l].level;
+  const int W = n->W[lv], H = n->H[lv], D = n->D[lv];
+  switch (l) {
+    case 0: return wgrad_launch<16, 16>(X, G, dWpad, W, H, D, st);
+    case 1: return wgrad_launch<16, 32>(X, G, dWpad, W, H, D, st);
+    case 2: return wgrad_launch<32, 64>(X, G, dWpad, W, H, D, st);
+    case 3: return wgrad_launch<64, 64>(X, G, dWpad, W, H, D, st);
+    case 4: return wgrad_launch<64, 32>(X, G, dWpad, W, H, D, st);
+    case 5: return wgrad_launch<32, 16>(X, G, dWpad, W, H, D, st);
+    default: return wgrad_launch<16, 16>(X, G, dWpad, W, H, D, st);
+  }
+}
+
+// fold a padded [27][kin][kout] gradient into the logical [27][cin][cout] one
+__global__ void k_fold_wgrad(float *__restrict__ dst, const float *__restrict__ src, int cin, int cout, int kin,
+                             int kout) {
+  const int n = 27 * cin * cout;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    const int co = q % cout, ci = (q / cout) % cin, tap = q / (cout * cin);
+    dst[q] = src[((size_t)tap * kin + ci) * kout + co];
+  }
+}
+
+int net_fail(dsg_net *n, cudaError_t e, const char *where) {
+  char buf[256];
+  snprintf(buf, sizeof buf, "CUDA error %d (%s) at %s", (int)e, cudaGetErrorString(e), where);
+  if (n) n->err = buf;
+  return dsg::set_error(nullptr, e == cudaErrorMemoryAllocation ? DSG_E_NOMEM : DSG_E_CUDA, "%s", buf);
+}
+
+#define NCK(n, expr)                                       \
+  do {                                                     \
+    cudaError_t _e = (expr);                               \
+    if (_e != cudaSuccess) return net_fail((n), _e, #expr); \
+  } while (0)
+
+size_t vox(const dsg_net *n, int lv) { return (size_t)n->W[lv] * n->H[lv] * n->D[lv]; }
+
+int repack(dsg_net *n, cudaStream_t st) {
+  for (int l = 0; l < kLayers; l++) {
+    const LayerDef &L = kDefs[l];
+    const float *Wt = n->params + n->poff[l];
+    int nf = 27 * (L.cinp / 16) * (L.coutp / 8) * 32;
+    DSG_COUNT k_pack<<<eblocks(nf), 256, 0, st>>>(Wt, n->packf[l], L.cin, L.cout, L.cinp, L.coutp, 0);
+    if (l > 0) {
+      // data gradient: K = forward outputs (padded to 16), N = forward inputs (padded to 8/16)
+      const int kin = L.coutp < 16 ? 16 : L.coutp, kout = L.cinp;
+      nf = 27 * (kin / 16) * (kout / 8) * 32;
+      DSG_COUNT k_pack<<<eblocks(nf), 256, 0, st>>>(Wt, n->packb[l], L.cin, L.cout, kin, kout, 1);
+    }
+  }
+  NCK(n, cudaGetLastError());
+  return DSG_OK;
+}
+
+int forward(dsg_net *n, cudaStream_t st) {
+  NCK(n, conv_fwd(n, 0, n->x0, n->e1, st));
+  DSG_COUNT k_pool<<<eblocks(vox(n, 1) * 16), 256, 0, st>>>(n->e1, n->p1, n->W[0], n->H[0], n->D[0], 16);
+  NCK(n, conv_fwd(n, 1, n->p1, n->e2, st));
+  DSG_COUNT k_pool<<<eblocks(vox(n, 2) * 32), 256, 0, st>>>(n->e2, n->p2, n->W[1], n->H[1], n->D[1], 32);
+  NCK(n, conv_fwd(n, 2, n->p2, n->e3, st));
+  DSG_COUNT k_pool<<<eblocks(vox(n, 3) * 64), 256, 0, st>>>(n->e3, n->p3, n->W[2], n->H[2], n->D[2], 64);
+  NCK(n, conv_fwd(n, 3, n->p3, n->e4, st));
+  DSG_COUNT k_upadd<<<eblocks(vox(n, 2) * 64), 256, 0, st>>>(n->e4, n->e3, n->u3, n->W[2], n->H[2], n->D[2], 64);
+  NCK(n, conv_fwd(n, 4, n->u3, n->d3, st));
+  DSG_COUNT k_upadd<<<eblocks(vox(n, 1) * 32), 256, 0, st>>>(n->d3, n->e2, n->u2, n->W[1], n->H[1], n->D[1], 32);
+  NCK(n, conv_fwd(n, 5, n->u2, n->d2, st));
+  DSG_COUNT k_upadd<<<eblocks(vox(n, 0) * 16), 256, 0, st>>>(n->d2, n->e1, n->u1, n->W[0], n->H[0], n->D[0], 16);
+  NCK(n, conv_fwd(n, 6, n->u1, n->yout, st));
+  NCK(n, cudaGetLastError());
+  return DSG_OK;
+}
+
+// One layer's backward: dacc (FP32 dL/d(output after activation), coutp channels)
+// -> G = bf16(dacc * relu'), bias grad, weight grad (into grad), and the data
+// gradient dX (bf16, cinp channels) if want_dx.
+int layer_back(dsg_net *n, int l, const float *dacc, const bf16 *act_out, const bf16 *X, bf16 *dX, float *wscratch,
+               cudaStream_t st) {
+  const LayerDef &L = kDefs[l];
+  const int lv = L.level;
+  const size_t nv = vox(n, lv);
+  float *dbias = n->grad + n->poff[l] + 27LL * L.cin * L.cout;
+  // G into gbuf (coutp channels); the bias gradient of padded channels is dropped
+  NCK(n, cudaMemsetAsync(wscratch, 0, (size_t)64 * sizeof(float), st));
+  const int gc = grad_ch(l);
+  DSG_COUNT k_relu_back<<<eblocks(nv * gc), 256, 0, st>>>(dacc, act_out, n->gbuf, wscratch, nv, gc, L.relu ? 1 : 0);
+  NCK(n, cudaMemcpyAsync(dbias, wscratch, L.cout * sizeof(float), cudaMemcpyDeviceToDevice, st));
+  float *wpad = wscratch + 64;
+  const size_t wn = (size_t)27 * L.cinp * gc;
+  NCK(n, cudaMemsetAsync(wpad, 0, wn * sizeof(float), st));
+  NCK(n, conv_wgrad(n, l, X, n->gbuf, wpad, st));
+  DSG_COUNT k_fold_wgrad<<<eblocks(27 * L.cin * L.cout), 256, 0, st>>>(n->grad + n->poff[l], wpad, L.cin, L.cout,
+                                                                       L.cinp, gc);
+  if (dX) NCK(n, conv_dgrad(n, l, n->gbuf, dX, st));
+  NCK(n, cudaGetLastError());
+  return DSG_OK;
+}
+
+// Backward pass of the U-Net for the loss of the current output/target;
+// parameter gradients into n->grad.
+int backward(dsg_net *n, cudaStream_t st) {
+  const size_t v0 = vox(n, 0), v1 = vox(n, 1), v2 = vox(n, 2), v3 = vox(n, 3);
+  float *ws = n->wscratch;
+  int rc;
+  NCK(n, cudaMemsetAsync(n->grad, 0, DSG_NET_PARAMS * sizeof(float), st));
+  NCK(n, cudaMemsetAsync(n->acc_e1, 0, v0 * 16 * sizeof(float), st));
+  NCK(n, cudaMemsetAsync(n->acc_e2, 0, v1 * 32 * sizeof(float), st));
+  NCK(n, cudaMemsetAsync(n->acc_e3, 0, v2 * 64 * sizeof(float), st));
+  // D1: y = conv6(u1), u1 = up(d2) + e1
+  if ((rc = layer_back(n, 6, n->dy_out, nullptr, n->u1, n->gbuf2, ws, st))) return rc;
+  DSG_COUNT k_acc_bf16<<<eblocks(v0 * 16), 256, 0, st>>>(n->acc_e1, n->gbuf2, v0 * 16);
+  DSG_COUNT k_upadd_back<<<eblocks(v1 * 16), 256, 0, st>>>(n->gbuf2, n->tmp, n->W[0], n->H[0], n->D[0], 16);
+  // D2: d2 = relu(conv5(u2)), u2 = up(d3) + e2
+  if ((rc = layer_back(n, 5, n->tmp, n->d2, n->u2, n->gbuf2, ws, st))) return rc;
+  DSG_COUNT k_acc_bf16<<<eblocks(v1 * 32), 256, 0, st>>>(n->acc_e2, n->gbuf2, v1 * 32);
+  DSG_COUNT k_upadd_back<<<eblocks(v2 * 32), 256, 0, st>>>(n->gbuf2, n->tmp, n->W[1], n->H[1], n->D[1], 32);
+  // D3: d3 = relu(conv4(u3)), u3 = up(e4) + e3
+  if ((rc = layer_back(n, 4, n->tmp, n->d3, n->u3, n->gbuf2, ws, st))) return rc;
+  DSG_COUNT k_acc_bf16<<<eblocks(v2 * 64), 256, 0, st>>>(n->acc_e3, n->gbuf2, v2 * 64);
+  DSG_COUNT k_upadd_back<<<eblocks(v3 * 64), 256, 0, st>>>(n->gbuf2, n->tmp, n->W[2], n->H[2], n->D[2], 64);
+  // E4: e4 = relu(conv3(p3)), p3 = pool(e3)
+  if ((rc = layer_back(n, 3, n->tmp, n->e4, n->p3, n->gbuf2, ws, st))) return rc;
+  DSG_COUNT k_pool_back_acc<<<eblocks(v2 * 64), 256, 0, st>>>(n->gbuf2, n->acc_e3, n->W[2], n->H[2], n->D[2], 64);
+  // E3: e3 = relu(conv2(p2)), p2 = pool(e2)
+  if ((rc = layer_back(n, 2, n->acc_e3, n->e3, n->p2, n->gbuf2, ws, st))) return rc;
+  DSG_COUNT k_pool_back_acc<<<eblocks(v1 * 32), 256, 0, st>>>(n->gbuf2, n->acc_e2, n->W[1], n->H[1], n->D[1], 32);
+  // E2: e2 = relu(conv1(p1)), p1 = pool(e1)
+  if ((rc = layer_back(n, 1, n->acc_e2, n->e2, n->p1, n->gbuf2, ws, st))) return rc;
+  DSG_COUNT k_pool_back_acc<<<eblocks(v0 * 16), 256, 0, st>>>(n->gbuf2, n->acc_e1, n->W[0], n->H[0], n->D[0], 16);
+  // E1: e1 = relu(conv0(x0)); no input gradient
+  if ((rc = layer_back(n, 0, n->acc_e1, n->e1, n->x0, nullptr, ws, st))) return rc;
+  NCK(n, cudaGetLastError());
+  return DSG_OK;
+}
+
+int loss_grad(dsg_net *n, cudaStream_t st) {
+  NCK(n, cudaMemsetAsync(n->loss_dev, 0, sizeof(double), st));
+  DSG_COUNT k_mse<<<eblocks(vox(n, 0)), 256, 0, st>>>(n->yout, n->target, n->dy_out, n->loss_dev, vox(n, 0));
+  NCK(n, cudaGetLastError());
+  return DSG_OK;
+}
+
+// x (FP32 host, 3 channels per voxel) -> n->x0 (bf16, 16 channels)
+__global__ void k_input_from_f32(bf16 *__restrict__ x0, const float *__restrict__ x, size_t nvox) {
+  for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < nvox; v += (size_t)gridDim.x * blockDim.x)
+#pragma unroll
+    for (int c = 0; c < 16; c++) x0[v * 16 + c] = __float2bfloat16(c < 3 ? x[v * 3 + c] : 0.f);
+}
+
+__global__ void k_output_ch0(float *__restrict__ y, const float *__restrict__ yout, size_t nvox) {
+  for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < nvox; v += (size_t)gridDim.x * blockDim.x)
+    y[v] = yout[v * 8];
+}
+
+// splitmix64-based normal deviates for He initialisation (host)
+double host_normal(uint64_t &state) {
+  auto next = [&]() {
+    uint64_t z = (state += 0x9E3779B97F4A7C15ULL);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    z ^= z >> 31;
+    return ((double)(z >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+  };
+  const double u1 = next(), u2 = next();
+  return sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
+}
+
+}  // namespace
+
+namespace dsg {
+namespace nn {
+
+// Solver hooks (used by dsg.cu): features of the current pressure system into
+// the network input; optional training target from the solved pressure.
+int net_features(dsg_net *n, const double *cc, const double *rhs, const double *pprev, const double *p,
+                 const double *a, const double *b, const double *c, Dims d, double lengthsize, cudaStream_t st) {
+  if (n->W[0] != d.nx - 2 || n->H[0] != d.ny - 2 || n->D[0] != d.nz - 2)
+    return dsg::set_error(nullptr, DSG_E_ARG, "network sized %dx%dx%d, grid interior %dx%dx%d", n->W[0], n->H[0],
+                          n->D[0], d.nx - 2, d.ny - 2, d.nz - 2);
+  const double h1 = lengthsize / (d.nx - 2);
+  NCK(n, cudaMemsetAsync(n->sums_dev, 0, sizeof(double), st));
+  DSG_COUNT k_sumsq<<<1216, 256, 0, st>>>(rhs, n->sums_dev, d);
+  const dim3 blk(32, 8), grid((unsigned)((d.nx - 2 + 31) / 32), (unsigned)((d.ny - 2 + 7) / 8), (unsigned)(d.nz - 2));
+  DSG_COUNT k_features<<<grid, blk, 0, st>>>(n->x0, p ? n->target : nullptr, cc, rhs, pprev, p, a, b, c, n->sums_dev, d,
+                                             1.0 / (h1 * h1), h1 * h1);
+  NCK(n, cudaGetLastError());
+  return DSG_OK;
+}
+
+// p = p_prev + s h^2 net(x) on the interior (features must be current).
+int net_guess(dsg_net *n, double *p, const double *pprev, Dims d, double lengthsize, cudaStream_t st) {
+  int rc = forward(n, st);
+  if (rc) return rc;
+  const double h1 = lengthsize / (d.nx - 2);
+  const dim3 blk(32, 8), grid((unsigned)((d.nx - 2 + 31) / 32), (unsigned)((d.ny - 2 + 7) / 8), (unsigned)(d.nz - 2));
+  DSG_COUNT k_apply_guess<<<grid, blk, 0, st>>>(p, pprev, n->yout, n->sums_dev, d, h1 * h1);
+  NCK(n, cudaGetLastError());
+  return DSG_OK;
+}
+
+void net_set_target(dsg_net *n, bool v, cudaStream_t st) {
+  n->have_target = v;
+  n->stream = st;
+}
+
+}  // namespace nn
+}  // namespace dsg
+
+// ============================================================================
+// C ABI
+// ============================================================================
+extern "C" {
+
+int64_t dsg_net_param_count(void) { return DSG_NET_PARAMS; }
+
+int dsg_net_create(int W, int H, int D, uint64_t seed, dsg_net **out) {
+  if (!out) return dsg::set_error(nullptr, DSG_E_ARG, "null output");
+  *out = nullptr;
+  if (W < 8 || H < 8 || D < 8 || (W % 8) || (H % 8) || (D % 8))
+    return dsg::set_error(nullptr, DSG_E_ARG, "network grid %dx%dx%d: sides must be multiples of 8", W, H, D);
+  dsg_net *n = new dsg_net();
+  for (int l = 0; l < 4; l++) {
+    n->W[l] = W >> l;
+    n->H[l] = H >> l;
+    n->D[l] = D >> l;
+  }
+  long long off = 0;
+  for (int l = 0; l < kLayers; l++) {
+    n->poff[l] = off;
+    off += layer_params(l);
+  }
+  const size_t v0 = vox(n, 0), v1 = vox(n, 1), v2 = vox(n, 2), v3 = vox(n, 3);
+  auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  std::vector<std::pair<void **, size_t>> plan;
+  plan.push_back({(void **)&n->params, up(DSG_NET_PARAMS * 4)});
+  plan.push_back({(void **)&n->grad, up(DSG_NET_PARAMS * 4)});
+  plan.push_back({(void **)&n->adam_m, up(DSG_NET_PARAMS * 4)});
+  plan.push_back({(void **)&n->adam_v, up(DSG_NET_PARAMS * 4)});
+  for (int l = 0; l < kLayers; l++) {
+    const LayerDef &L = kDefs[l];
+    plan.push_back({(void **)&n->packf[l], up((size_t)27 * (L.cinp / 16) * (L.coutp / 8) * 32 * sizeof(uint2))});
+    const int kin = L.coutp < 16 ? 16 : L.coutp;
+    plan.push_back({(void **)&n->packb[l], up((size_t)27 * (kin / 16) * (L.cinp / 8) * 32 * sizeof(uint2))});
+  }
+  plan.push_back({(void **)&n->x0, up(v0 * 16 * 2)});
+  plan.push_back({(void **)&n->e1, up(v0 * 16 * 2)});
+  plan.push_back({(void **)&n->p1, up(v1 * 16 * 2)});
+  plan.push_back({(void **)&n->e2, up(v1 * 32 * 2)});
+  plan.push_back({(void **)&n->p2, up(v2 * 32 * 2)});
+  plan.push_back({(void **)&n->e3, up(v2 * 64 * 2)});
+  plan.push_back({(void **)&n->p3, up(v3 * 64 * 2)});
+  plan.push_back({(void **)&n->e4, up(v3 * 64 * 2)});
+  plan.push_back({(void **)&n->u3, up(v2 * 64 * 2)});
+  plan.push_back({(void **)&n->d3, up(v2 * 32 * 2)});
+  plan.push_back({(void **)&n->u2, up(v1 * 32 * 2)});
+  plan.push_back({(void **)&n->d2, up(v1 * 16 * 2)});
+  plan.push_back({(void **)&n->u1, up(v0 * 16 * 2)});
+  plan.push_back({(void **)&n->yout, up(v0 * 8 * 4)});
+  plan.push_back({(void **)&n->target, up(v0 * 4)});
+  plan.push_back({(void **)&n->dy_out, up(v0 * 16 * 4)});
+  plan.push_back({(void **)&n->acc_e1, up(v0 * 16 * 4)});
+  plan.push_back({(void **)&n->acc_e2, up(v1 * 32 * 4)});
+  plan.push_back({(void **)&n->acc_e3, up(v2 * 64 * 4)});
+  plan.push_back({(void **)&n->tmp, up(v1 * 16 * 4 > v2 * 32 * 4 ? v1 * 16 * 4 : v2 * 32 * 4)});
+  plan.push_back({(void **)&n->gbuf, up(v0 * 16 * 2)});
+  plan.push_back({(void **)&n->gbuf2, up(v0 * 16 * 2)});
+  plan.push_back({(void **)&n->wscratch, up((64 + 27 * 64 * 64) * 4)});
+  plan.push_back({(void **)&n->xin_f32, up(v0 * 3 * 4)});
+  plan.push_back({(void **)&n->yhost_f32, up(v0 * 4)});
+  plan.push_back({(void **)&n->loss_dev, 256});
+  plan.push_back({(void **)&n->sums_dev, 256});
+  size_t total = 0;
+  for (auto &e : plan) total += e.second;
+  cudaError_t e = cudaMalloc(&n->arena, total);
+  if (e == cudaSuccess) e = cudaMemset(n->arena, 0, total);
+  if (e == cudaSuccess) e = cudaMallocHost(&n->loss_host, sizeof(double));
+  if (e != cudaSuccess) {
+    int rc = net_fail(n, e, "dsg_net_create");
+    dsg_net_destroy(n);
+    return rc;
+  }
+  n->arena_bytes = total;
+  char *p = (char *)n->arena;
+  for (auto &ent : plan) {
+    *ent.first = p;
+    p += ent.second;
+  }
+  // He initialisation of the weights, zero biases
+  std::vector<float> h(DSG_NET_PARAMS, 0.f);
+  uint64_t state = seed * 0x2545F4914F6CDD1DULL + 1;
+  for (int l = 0; l < kLayers; l++) {
+    const double sd = sqrt(2.0 / (27.0 * kDefs[l].cin)) * (l == kLayers - 1 ? 0.1 : 1.0);
+    for (long long q = 0; q < 27LL * kDefs[l].cin * kDefs[l].cout; q++)
+      h[n->poff[l] + q] = (float)(sd * host_normal(state));
+  }
+  e = cudaMemcpy(n->params, h.data(), DSG_NET_PARAMS * sizeof(float), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    int rc = net_fail(n, e, "upload params");
+    dsg_net_destroy(n);
+    return rc;
+  }
+  int rc = repack(n, 0);
+  if (rc == DSG_OK) {
+    e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) rc = net_fail(n, e, "repack");
+  }
+  if (rc) {
+    dsg_net_destroy(n);
+    return rc;
+  }
+  *out = n;
+  return DSG_OK;
+}
+
+void dsg_net_destroy(dsg_net *n) {
+  if (!n) return;
+  if (n->arena) cudaFree(n->arena);
+  if (n->loss_host) cudaFreeHost(n->loss_host);
+  delete n;
+}
+
+int dsg_net_get_params(dsg_net *n, float *host, int64_t count) {
+  if (!n || !host || count != DSG_NET_PARAMS) return dsg::set_error(nullptr, DSG_E_ARG, "bad parameter buffer");
+  NCK(n, cudaMemcpy(host, n->params, DSG_NET_PARAMS * sizeof(float), cudaMemcpyDeviceToHost));
+  return DSG_OK;
+}
+
+int dsg_net_set_params(dsg_net *n, const float *host, int64_t count) {
+  if (!n || !host || count != DSG_NET_PARAMS) return dsg::set_error(nullptr, DSG_E_ARG, "bad parameter buffer");
+  NCK(n, cudaMemcpy(n->params, host, DSG_NET_PARAMS * sizeof(float), cudaMemcpyHostToDevice));
+  int rc = repack(n, 0);
+  if (rc) return rc;
+  NCK(n, cudaDeviceSynchronize());
+  return DSG_OK;
+}
+
+int dsg_net_forward_host(dsg_net *n, const float *x, float *y) {
+  if (!n || !x || !y) return dsg::set_error(nullptr, DSG_E_ARG, "null argument");
+  const size_t v0 = vox(n, 0);
+  NCK(n, cudaMemcpy(n->xin_f32, x, v0 * 3 * sizeof(float), cudaMemcpyHostToDevice));
+  DSG_COUNT k_input_from_f32<<<eblocks(v0), 256>>>(n->x0, n->xin_f32, v0);
+  int rc = forward(n, 0);
+  if (rc) return rc;
+  DSG_COUNT k_output_ch0<<<eblocks(v0), 256>>>(n->yhost_f32, n->yout, v0);
+  NCK(n, cudaMemcpy(y, n->yhost_f32, v0 * sizeof(float), cudaMemcpyDeviceToHost));
+  return DSG_OK;
+}
+
+int dsg_net_grad_host(dsg_net *n, const float *x, const float *t, float *loss, float *grad) {
+  if (!n || !x || !t || !loss || !grad) return dsg::set_error(nullptr, DSG_E_ARG, "null argument");
+  const size_t v0 = vox(n, 0);
+  NCK(n, cudaMemcpy(n->xin_f32, x, v0 * 3 * sizeof(float), cudaMemcpyHostToDevice));
+  DSG_COUNT k_input_from_f32<<<eblocks(v0), 256>>>(n->x0, n->xin_f32, v0);
+  NCK(n, cudaMemcpy(n->target, t, v0 * sizeof(float), cudaMemcpyHostToDevice));
+  int rc = forward(n, 0);
+  if (!rc) rc = loss_grad(n, 0);
+  if (!rc) rc = backward(n, 0);
+  if (rc) return rc;
+  double l = 0.0;
+  NCK(n, cudaMemcpy(&l, n->loss_dev, sizeof(double), cudaMemcpyDeviceToHost));
+  *loss = (float)l;
+  NCK(n, cudaMemcpy(grad, n->grad, DSG_NET_PARAMS * sizeof(float), cudaMemcpyDeviceToHost));
+  return DSG_OK;
+}
+
+int dsg_net_train_step(dsg_net *n, float lr, float *loss) {
+  if (!n) return dsg::set_error(nullptr, DSG_E_ARG, "null network");
+  if (!n->have_target) return dsg::set_error(nullptr, DSG_E_STATE, "no recorded training pair");
+  cudaStream_t st = n->stream;
+  int rc = forward(n, st);
+  if (!rc) rc = loss_grad(n, st);
+  if (!rc) rc = backward(n, st);
+  if (rc) return rc;
+  n->step++;
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float c1 = 1.f - powf(b1, (float)n->step), c2 = 1.f - powf(b2, (float)n->step);
+  DSG_COUNT k_adam<<<eblocks(DSG_NET_PARAMS), 256, 0, st>>>(n->params, n->grad, n->adam_m, n->adam_v, DSG_NET_PARAMS,
+                                                           lr, b1, b2, 1e-8f, c1, c2, 1.0f);
+  rc = repack(n, st);
+  if (rc) return rc;
+  NCK(n, cudaMemcpyAsync(n->loss_host, n->loss_dev, sizeof(double), cudaMemcpyDeviceToHost, st));
+  NCK(n, cudaStreamSynchronize(st));
+  if (loss) *loss = (float)*n->loss_host;
+  n->have_target = false;
+  return DSG_OK;
+}
+
+int64_t dsg_net_device_bytes(const dsg_net *n) { return n ? (int64_t)n->arena_bytes : 0; }
+
+}  // extern "C"

@@ -1,0 +1,192 @@
+"""The learned multigrid initial guess: host wrapper and training driver.
+
+A ``Net`` is the 3D convolutional U-Net of ``csrc/nn.cu`` (BF16 tensor-core
+kernels, FP32 accumulation) sized for one interior grid.  ``train`` runs the
+solver itself at 128^3 on droplets of random diameter (1-3 mm) and impact
+speed (0.5-4 m/s), records after every pressure solve the pair (features of
+the system, solved correction of the previous pressure) and takes one Adam
+step on it: the network learns from the solver's own snapshots, on the fly.
+In ``MODE_LEARNED`` the solver asks the attached network for a correction of
+the previous-step pressure and keeps it only if its FP64 residual is below
+that of the previous-step pressure itself.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _lib
+from .config import InputData, MODE_LEARNED, MODE_TOL_MIXED, droplet
+
+WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "warmstart_weights.npy")
+
+
+class Net:
+    """One network instance on the current CUDA device."""
+
+    def __init__(self, W, H=None, D=None, seed=0):
+        self.lib = _lib.load()
+        H = W if H is None else H
+        D = W if D is None else D
+        h = C.c_void_p()
+        _lib.check(self.lib.dsg_net_create(W, H, D, seed, C.byref(h)))
+        self.h = h
+        self.shape = (D, H, W)
+        self.nparams = int(self.lib.dsg_net_param_count())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.dsg_net_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def params(self):
+        out = np.empty(self.nparams, dtype=np.float32)
+        _lib.check(self.lib.dsg_net_get_params(self.h, out.ctypes.data, self.nparams))
+        return out
+
+    @params.setter
+    def params(self, value):
+        v = np.ascontiguousarray(value, dtype=np.float32)
+        if v.size != self.nparams:
+            raise ValueError("expected %d parameters" % self.nparams)
+        _lib.check(self.lib.dsg_net_set_params(self.h, v.ctypes.data, self.nparams))
+
+    def forward(self, x):
+        """x: (D, H, W, 3) -> (D, H, W)."""
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        assert x.shape == self.shape + (3,)
+        y = np.empty(self.shape, dtype=np.float32)
+        _lib.check(self.lib.dsg_net_forward_host(self.h, x.ctypes.data, y.ctypes.data))
+        return y
+
+    def loss_grad(self, x, t):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        g = np.empty(self.nparams, dtype=np.float32)
+        loss = C.c_float()
+        _lib.check(self.lib.dsg_net_grad_host(self.h, x.ctypes.data, t.ctypes.data, C.byref(loss), g.ctypes.data))
+        return float(loss.value), g
+
+    def train_step(self, lr):
+        loss = C.c_float()
+        _lib.check(self.lib.dsg_net_train_step(self.h, lr, C.byref(loss)))
+        return float(loss.value)
+
+    def attach(self, solver, record=False):
+        _lib.check(self.lib.dsg_attach_net(solver.ctx, self.h, 1 if record else 0), solver.ctx)
+        solver.net = self
+
+    def save(self, path=WEIGHTS):
+        np.save(path, self.params)
+
+    def load(self, path=WEIGHTS):
+        self.params = np.load(path)
+        return self
+
+
+def detach(solver):
+    _lib.check(_lib.load().dsg_attach_net(solver.ctx, None, 0), solver.ctx)
+    solver.net = None
+
+
+def training_instances(count, seed=0):
+    """Droplet diameters U[1,3] mm and impact speeds U[0.5,4] m/s (seeded)."""
+    rng = np.random.default_rng(seed)
+    return [(float(rng.uniform(1e-3, 3e-3)), float(rng.uniform(0.5, 4.0))) for _ in range(count)]
+
+
+def train(n=128, instances=20, steps=1000, lr=1e-3, seed=0, log=None, tol=1e-8):
+    """Train a network on the solver's own snapshots at n^3 (one Adam step per
+    solved time step).  Returns (net, history of losses)."""
+    from .solver import Solver
+    net = Net(n, seed=seed)
+    losses = []
+    for k, (diam, speed) in enumerate(training_instances(instances, seed)):
+        inp = droplet(n, steps=steps, impact_speed=speed, diameter=diam, noise_si=1e-4, mode=MODE_TOL_MIXED,
+                      tol=tol, npre=4, npost=4, ntop=4, seed=seed * 1000 + k)
+        with Solver(inp) as s:
+            net.attach(s, record=True)
+            for t in range(1, steps + 1):
+                s.step(t)
+                if t > 1:  # the first step has no previous pressure
+                    losses.append(net.train_step(lr))
+            detach(s)
+        if log:
+            log("instance %d (D=%.2f mm, v=%.2f m/s): mean loss of its last 50 steps %.4g"
+                % (k, diam * 1e3, speed, float(np.mean(losses[-50:])) if losses else float("nan")))
+    return net, losses
+
+
+def learned_config(inp):
+    """The same run with the learned initial guess."""
+    d = inp.as_dict() if isinstance(inp, InputData) else dict(inp)
+    d["mode"] = MODE_LEARNED
+    return InputData(**d)
+
+
+def evaluate(inp, net=None, steps=8, warmup=2, stream=None):
+    """Run `steps` time steps (after `warmup`) and report V-cycles, initial
+    residuals, guard fallbacks and ms per step."""
+    import time
+    from .solver import Solver
+    out = {"vcycles": [], "relres_init": [], "fallback": [], "relres_net": [], "relres_prev": []}
+    with Solver(inp) as s:
+        if net is not None:
+            net.attach(s)
+        for t in range(1, warmup + 1):
+            s.step(t)
+        s.synchronize()
+        t0 = time.perf_counter()
+        for t in range(warmup + 1, warmup + steps + 1):
+            st = s.step(t)
+            for k in out:
+                out[k].append(st[k] if k in st else None)
+        s.synchronize()
+        out["ms_per_step"] = 1e3 * (time.perf_counter() - t0) / steps
+        if net is not None:
+            detach(s)
+    return out
+
+
+def main(argv=None):
+    import argparse
+    import json
+    import time
+    ap = argparse.ArgumentParser(description="train the learned initial guess on solver snapshots")
+    ap.add_argument("--n", type=int, default=128)
+    ap.add_argument("--instances", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--out", default=WEIGHTS)
+    ap.add_argument("--eval-n", type=int, default=256)
+    ap.add_argument("--eval-steps", type=int, default=8)
+    a = ap.parse_args(argv)
+    t0 = time.perf_counter()
+    net, losses = train(a.n, a.instances, a.steps, a.lr, a.seed, log=print)
+    t_train = time.perf_counter() - t0
+    net.save(a.out)
+    print(json.dumps({"snapshots": len(losses), "train_s": t_train, "loss_first": float(np.mean(losses[:50])),
+                      "loss_last": float(np.mean(losses[-200:]))}))
+    if a.eval_steps:
+        n = a.eval_n
+        base = droplet(n, steps=1000, impact_speed=3.0, noise_si=1e-4, mode=MODE_TOL_MIXED, tol=1e-8, npre=4, npost=4,
+                       ntop=4)
+        ev = Net(n).load(a.out)
+        zero = Net(n)
+        zero.params = np.zeros(zero.nparams, dtype=np.float32)
+        r_mixed = evaluate(base, steps=a.eval_steps)
+        r_prev = evaluate(learned_config(base), zero, steps=a.eval_steps)
+        r_learn = evaluate(learned_config(base), ev, steps=a.eval_steps)
+        print(json.dumps({"n": n, "fmg_start": r_mixed, "previous_pressure_start": r_prev, "learned_start": r_learn}))
+
+
+if __name__ == "__main__":
+    main()

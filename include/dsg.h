@@ -101,6 +101,8 @@ typedef struct dsg_mg_stats {
   int converged;      /* 1 if relres < tol (tol modes) */
   int fallback;       /* 1 if the learned guess was rejected for the previous-step pressure */
   double epsdiv;      /* h*max|div| of the adaptivity check, -1 if not run this step */
+  double relres_prev; /* learned mode: relres of the previous-step pressure as a guess */
+  double relres_net;  /* learned mode: relres of the network's guess */
 } dsg_mg_stats;
 
 typedef struct dsg_ctx dsg_ctx;
@@ -167,6 +169,34 @@ int dsg_profile_enable(dsg_ctx *ctx, int on);
 int dsg_profile_read(dsg_ctx *ctx, dsg_profile *out);
 /* Total kernel launches made by the library in this process. */
 int64_t dsg_launch_count(void);
+
+/* ---- learned initial guess (no reference counterpart) ----------------------
+ * A 3D convolutional U-Net (4 levels, 16/32/64/64 channels, 3x3x3 kernels,
+ * 250785 parameters, BF16 weights/activations, FP32 accumulation, tensor-core
+ * implicit-GEMM kernels) predicting the pressure correction from the volume
+ * fraction (density), the divergence right-hand side and the previous
+ * pressure (through its defect under the current operator).  A network is
+ * sized for one interior grid W x H x D (each a multiple of 8). */
+typedef struct dsg_net dsg_net;
+int64_t dsg_net_param_count(void);
+int dsg_net_create(int W, int H, int D, uint64_t seed, dsg_net **out); /* He-initialised */
+void dsg_net_destroy(dsg_net *net);
+int64_t dsg_net_device_bytes(const dsg_net *net);
+/* FP32 parameters, layer by layer: weights [27][cin][cout] then bias[cout] */
+int dsg_net_get_params(dsg_net *net, float *host, int64_t count);
+int dsg_net_set_params(dsg_net *net, const float *host, int64_t count);
+/* forward on host arrays: x = W*H*D voxels x 3 channels (x fastest, channels
+ * innermost), y = W*H*D outputs */
+int dsg_net_forward_host(dsg_net *net, const float *x, float *y);
+/* loss = mean (y - t)^2 and its gradient with respect to every parameter */
+int dsg_net_grad_host(dsg_net *net, const float *x, const float *t, float *loss, float *grad);
+/* one Adam step on the training pair recorded by the attached context */
+int dsg_net_train_step(dsg_net *net, float lr, float *loss);
+/* Attach a network to a context (NULL detaches).  record=1: after every
+ * pressure solve the context stores (input, solved correction) as the net's
+ * training pair.  DSG_MODE_LEARNED uses the attached network for its initial
+ * guess. */
+int dsg_attach_net(dsg_ctx *ctx, dsg_net *net, int record);
 
 /* ---- array-level kernels (device pointers, reference argument lists) ----
  * `stream` is a cudaStream_t (NULL = legacy default stream). */

@@ -1,0 +1,131 @@
+"""The learned initial guess: tensor-core network kernels against the numpy
+oracle, training, and the guarded learned solve.
+
+The oracle (oracle/nn_oracle.py) rounds to bfloat16 where the GPU stores
+bfloat16; what remains is FP32 accumulation order, which can flip the bf16
+rounding of single stored values (2^-8 relative), so forward outputs are
+compared at 2e-2 of their max-norm and gradients per layer at 3e-2 of their
+norm with a cosine above 0.999.
+"""
+import numpy as np
+import pytest
+
+import oracle.nn_oracle as NO
+from conftest import relerr
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [(16, 16, 16), (8, 16, 24)]  # (D, H, W)
+
+
+def _net(dsg, shape, seed=3):
+    from importlib import import_module
+    learned = import_module(dsg.__name__ + ".learned")
+    D, H, W = shape
+    return learned.Net(W, H, D, seed=seed), learned
+
+
+def _inputs(shape, seed):
+    r = np.random.default_rng(seed)
+    x = r.standard_normal(shape + (3,)).astype(np.float32)
+    x[..., 0] = r.uniform(0.0, 1.0, size=shape)
+    t = r.standard_normal(shape).astype(np.float32) * 0.1
+    return x, t
+
+
+def test_param_count(gpu_lib):
+    assert gpu_lib.load().dsg_net_param_count() == NO.param_count() == 250785
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_forward_matches_oracle(gpu_lib, shape):
+    net, _ = _net(gpu_lib, shape)
+    # larger biases and a non-trivial output layer so every path is exercised
+    p = net.params.copy()
+    r = np.random.default_rng(5)
+    p += (r.standard_normal(p.size) * 0.02).astype(np.float32)
+    net.params = p
+    x, _ = _inputs(shape, 1)
+    y = net.forward(x)
+    y_ref, _ = NO.forward(p.astype(np.float64), x.astype(np.float64), bf16=True)
+    assert np.all(np.isfinite(y))
+    assert relerr(y, y_ref) < 2e-2, relerr(y, y_ref)
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_gradients_match_oracle(gpu_lib, shape):
+    net, _ = _net(gpu_lib, shape, seed=7)
+    p = net.params.copy()
+    p += (np.random.default_rng(6).standard_normal(p.size) * 0.02).astype(np.float32)
+    net.params = p
+    x, t = _inputs(shape, 2)
+    loss, g = net.loss_grad(x, t)
+    loss_ref, g_ref, _ = NO.loss_and_grad(p.astype(np.float64), x.astype(np.float64), t.astype(np.float64))
+    assert abs(loss - loss_ref) <= 1e-2 * loss_ref
+    off = 0
+    for l, (ci, co, _) in enumerate(NO.LAYERS):
+        n = 27 * ci * co + co
+        a, b = g[off:off + n].astype(np.float64), g_ref[off:off + n]
+        off += n
+        err = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+        cos = float(a @ b / max(np.linalg.norm(a) * np.linalg.norm(b), 1e-30))
+        assert err < 3e-2 and cos > 0.999, (l, err, cos)
+
+
+def test_gradients_close_to_fp64(gpu_lib):
+    """Against the oracle without bf16 rounding: the gradient direction holds."""
+    shape = (16, 16, 16)
+    net, _ = _net(gpu_lib, shape, seed=8)
+    p = net.params
+    x, t = _inputs(shape, 4)
+    _, g = net.loss_grad(x, t)
+    _, g64, _ = NO.loss_and_grad(p.astype(np.float64), x.astype(np.float64), t.astype(np.float64), bf16=False)
+    cos = float(g @ g64 / (np.linalg.norm(g) * np.linalg.norm(g64)))
+    assert cos > 0.99, cos
+
+
+def test_training_on_solver_snapshots_reduces_loss(gpu_lib):
+    dsg = gpu_lib
+    net, learned = _net(dsg, (32, 32, 32), seed=1)
+    inp = dsg.config.droplet(32, mode=dsg.config.MODE_TOL_MIXED, tol=1e-9, impact_speed=2.0)
+    losses = []
+    with dsg.Solver(inp) as s:
+        net.attach(s, record=True)
+        for t in range(1, 61):
+            s.step(t)
+            if t > 1:
+                losses.append(net.train_step(2e-3))
+        learned.detach(s)
+    assert all(np.isfinite(losses))
+    assert np.mean(losses[-10:]) < 0.5 * np.mean(losses[:5]), (losses[:5], losses[-10:])
+
+
+def test_learned_mode_converges_and_guards(gpu_lib):
+    """Learned mode reaches the tolerance from either guess and picks the one
+    with the smaller residual; fields match the FP64 oracle from the same state."""
+    dsg = gpu_lib
+    from oracle import Oracle
+    from test_mixed_gpu import _sync_state
+    tol = 1e-10
+    net, _ = _net(dsg, (32, 32, 32), seed=2)
+    ora = Oracle(dsg.config.droplet(32, mode=dsg.config.MODE_TOL_FP64, tol=tol).as_dict())
+    gpu = dsg.Solver(dsg.config.droplet(32, mode=dsg.config.MODE_LEARNED, tol=tol), init=False)
+    net.attach(gpu)
+    for t in range(1, 6):
+        _sync_state(gpu, ora)
+        gpu.set_field("pprev", ora.field("p") if t > 1 else np.zeros(ora.shape))
+        ora.step(t)
+        st = gpu.step(t)
+        assert st["converged"] == 1 and st["relres"] < tol, st
+        assert st["fallback"] == (0 if st["relres_net"] < st["relres_prev"] else 1)
+        assert st["relres_init"] == min(st["relres_net"], st["relres_prev"])
+        for name in ("p", "u", "v", "w", "cc"):
+            assert relerr(gpu.field(name), ora.field(name)) < 1e-7, (t, name)
+
+
+def test_learned_mode_needs_network(gpu_lib):
+    dsg = gpu_lib
+    with dsg.Solver(dsg.config.droplet(16, mode=dsg.config.MODE_LEARNED, tol=1e-8)) as s:
+        with pytest.raises(dsg.DsgError) as e:
+            s.step(1)
+        assert e.value.code == -6
