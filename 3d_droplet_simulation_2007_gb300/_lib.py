@@ -16,12 +16,13 @@ DSG_E_NOMEM = -3
 DSG_E_NOT_CONVERGED = -4
 DSG_E_NONFINITE = -5
 DSG_E_STATE = -6
+NET_INPUTS = 5  # DSG_NET_INPUTS
 
 ERROR_NAMES = {0: "DSG_OK", -1: "DSG_E_ARG", -2: "DSG_E_CUDA", -3: "DSG_E_NOMEM",
                -4: "DSG_E_NOT_CONVERGED", -5: "DSG_E_NONFINITE", -6: "DSG_E_STATE"}
 
 FIELDS = ["cc", "p", "res", "rhs", "a", "b", "c", "ei", "u", "v", "w",
-          "s11", "s22", "s33", "s12", "s13", "s23", "rhon", "mun", "pprev"]
+          "s11", "s22", "s33", "s12", "s13", "s23", "rhon", "mun", "pprev", "pprev2"]
 FIELD_ID = {n: i for i, n in enumerate(FIELDS)}
 
 
@@ -43,7 +44,8 @@ class DsgConfig(C.Structure):
         ("tsave", C.c_int), ("surfacet", C.c_int),
         ("mode", C.c_int), ("tol", C.c_double), ("max_vcycles", C.c_int),
         ("noise_si", C.c_double), ("noise_seed", C.c_uint64),
-        ("inner_vcycles", C.c_int), ("use_graphs", C.c_int),
+        ("inner_vcycles", C.c_int), ("use_graphs", C.c_int), ("tail_nodes", C.c_int),
+        ("warm_start", C.c_int),
     ]
 
 

@@ -83,6 +83,8 @@ class InputData:
     noise_seed: int = 0
     inner_vcycles: int = 2
     use_graphs: int = 1
+    tail_nodes: int = 0
+    warm_start: int = 0
 
     def as_dict(self):
         return asdict(self)
@@ -116,15 +118,18 @@ def format_inputdata(inp):
 
 def droplet(n, steps=200, impact_speed=1.0, noise_si=1e-4, mode=MODE_REF_EXACT, tol=1e-10,
             npre=5, npost=5, ntop=4, cycles=2, diameter=2e-3, seed=0):
-    """Droplet impacting a flat wall on an n^3-cell grid (n = 2^k).
+    """Droplet impacting a flat wall on an n^3-cell grid.
+
+    n = 2^k gives the reference's multigrid hierarchy; other even sides
+    (48, 96, 160, ...) coarsen while the interior stays even.
 
     Cubic domain of 4 droplet diameters, drop centre 0.1 D above the wall
     (y0 = R + 0.1 D), liquid/gas density 1000/1.2, viscosity 1e-3/1.8e-5,
     sigma 0.072, gravity -9.81 along y, CSF surface tension, central
     convection, laminar, maxcfl 0.1, omega 1.5.
     """
-    if n < 4 or (n & (n - 1)) != 0:
-        raise ValueError("n must be a power of two >= 4 (reference MG needs 2^k+2 nodes)")
+    if n < 4:
+        raise ValueError("n must be at least 4")
     r = 0.5 * diameter
     return InputData(
         nx=n + 2, ny=n + 2, nz=n + 2, tmax=steps, cycles=cycles, npre=npre, ntop=ntop,

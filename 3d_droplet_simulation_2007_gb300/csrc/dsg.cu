@@ -274,26 +274,48 @@ cudaError_t relax32_level(dsg_ctx *ctx, int n, int l) {
   return e;
 }
 
+// Arguments of the coarse-tail kernel for FP32 levels 1..top of ctx.
+void tail_args(dsg_ctx *ctx, int top, dsg::TailArgs *A) {
+  memset(A, 0, sizeof *A);
+  for (int l = 1; l <= top; l++) {
+    float **L = ctx->lv32[l];
+    A->lv[l] = dsg::TailLevel{L[U32], L[RHS32], L[A32], L[B32], L[C32], L[EI32], ctx->level(l), level_h2(ctx, l)};
+  }
+  A->top = top;
+  A->npre = ctx->s.npre;
+  A->npost = ctx->s.npost;
+  A->ntop = ctx->s.ntop;
+  A->omega = (float)ctx->cfg.omega;
+}
+
 int vcycle32(dsg_ctx *ctx, int j) {
   cudaStream_t st = ctx->stream;
   const int ng = ctx->ng;
   float r1, r2;
   phase_coefs(ctx, &r1, &r2);
-  for (int jj = j; jj >= 2; jj--) {
+  // levels 1..jt in one single-block launch (0: every level pass by pass)
+  const int jt = ctx->tail_top < j ? ctx->tail_top : j;
+  for (int jj = j; jj >= 2 && jj > jt; jj--) {
     float **L = ctx->lv32[jj];
+    float **Lc = ctx->lv32[jj - 1];
     DSG_CK(ctx, relax32_level(ctx, ctx->s.npre, jj));
     if (jj == ng) {
       FineSplit f = fine_split(ctx);
-      DSG_CK(ctx, dsg::resid_restrict32_split(ctx->lv32[jj - 1][RHS32], f.u, f.r, L[A32], ctx->level(jj),
+      DSG_CK(ctx, dsg::resid_restrict32_split(Lc[RHS32], Lc[U32], f.u, f.r, L[A32], ctx->level(jj),
                                               1.0f / level_h2(ctx, jj), r1, r2, st));
     } else {
-      DSG_CK(ctx, dsg::resid_restrict32(ctx->lv32[jj - 1][RHS32], L[U32], L[RHS32], L[A32], L[B32], L[C32],
+      DSG_CK(ctx, dsg::resid_restrict32(Lc[RHS32], Lc[U32], L[U32], L[RHS32], L[A32], L[B32], L[C32],
                                         ctx->level(jj), 1.0f / level_h2(ctx, jj), st));
     }
-    DSG_CK(ctx, cudaMemsetAsync(ctx->lv32[jj - 1][U32], 0, ctx->level(jj - 1).count() * sizeof(float), st));
   }
-  DSG_CK(ctx, relax32_level(ctx, ctx->s.ntop, 1));
-  for (int jj = 2; jj <= j; jj++) {
+  if (jt >= 1) {
+    dsg::TailArgs A;
+    tail_args(ctx, jt, &A);
+    DSG_CK(ctx, dsg::vtail32(A, st));
+  } else {
+    DSG_CK(ctx, relax32_level(ctx, ctx->s.ntop, 1));
+  }
+  for (int jj = jt >= 1 ? jt + 1 : 2; jj <= j; jj++) {
     if (jj == ng) {
       FineSplit f = fine_split(ctx);
       DSG_CK(ctx, dsg::prolong32_split(f.u, ctx->lv32[jj - 1][U32], ctx->level(jj), 1, st));
@@ -450,7 +472,8 @@ int fmg32(dsg_ctx *ctx) {
 int record_pair(dsg_ctx *ctx) {
   if (!ctx->net || !ctx->net_record) return DSG_OK;
   double **F = ctx->lv[ctx->ng];
-  int rc = dsg::nn::net_features(ctx->net, F[0], F[3], ctx->f[DSG_F_PPREV], F[1], F[4], F[5], F[6], ctx->fine(),
+  int rc = dsg::nn::net_features(ctx->net, F[0], F[3], ctx->f[DSG_F_PPREV], ctx->f[DSG_F_PPREV2], F[1], F[4],
+                                 F[5], F[6], ctx->fine(),
                                  ctx->s.lengthsize, ctx->stream);
   if (rc) return rc;
   dsg::nn::net_set_target(ctx->net, true, ctx->stream);
@@ -509,11 +532,11 @@ int mixed_solve(dsg_ctx *ctx, dsg_mg_stats *s) {
   double r;
   if (ctx->cfg.mode == DSG_MODE_LEARNED) {
     // Guarded learned start: the previous-step pressure and the network's
-    // correction of it are both judged by their FP64 defect; the network's
-    // guess is kept only if it has the smaller relative residual.
+    // guess are both judged by their FP64 defect; the network's guess is kept
+    // only if it has the smaller relative residual.
     if (!ctx->net) return dsg::set_error(ctx, DSG_E_STATE, "learned mode without an attached network");
     double **F = ctx->lv[ng];
-    double *p = F[1], *pprev = ctx->f[DSG_F_PPREV];
+    double *p = F[1], *pprev = ctx->f[DSG_F_PPREV], *pprev2 = ctx->f[DSG_F_PPREV2];
     const size_t bytes = ctx->fine().count() * sizeof(double);
     rc = coef_hierarchy32(ctx);
     if (rc) return rc;
@@ -521,10 +544,10 @@ int mixed_solve(dsg_ctx *ctx, dsg_mg_stats *s) {
     double r_prev, r_net;
     rc = defect_host(ctx, &r_prev);
     if (rc) return rc;
-    rc = dsg::nn::net_features(ctx->net, F[0], F[3], pprev, nullptr, F[4], F[5], F[6], ctx->fine(),
+    rc = dsg::nn::net_features(ctx->net, F[0], F[3], pprev, pprev2, nullptr, F[4], F[5], F[6], ctx->fine(),
                                ctx->s.lengthsize, st);
     if (rc) return rc;
-    rc = dsg::nn::net_guess(ctx->net, p, pprev, ctx->fine(), ctx->s.lengthsize, st);
+    rc = dsg::nn::net_guess(ctx->net, p, pprev2, ctx->fine(), st);
     if (rc) return rc;
     DSG_CK(ctx, dsg::bc_scalar(p, ctx->fine(), st));
     rc = defect_host(ctx, &r_net);
@@ -542,6 +565,14 @@ int mixed_solve(dsg_ctx *ctx, dsg_mg_stats *s) {
     ctx->last_relres_net = r_net;
     s->relres_prev = r_prev;
     s->relres_net = r_net;
+  } else if (ctx->cfg.warm_start == 1) {
+    // previous-step pressure as the initial guess
+    rc = coef_hierarchy32(ctx);
+    if (rc) return rc;
+    DSG_CK(ctx, cudaMemcpyAsync(ctx->lv[ng][1], ctx->f[DSG_F_PPREV], ctx->fine().count() * sizeof(double),
+                                cudaMemcpyDeviceToDevice, st));
+    rc = defect_host(ctx, &r);
+    if (rc) return rc;
   } else {
     rc = run(ctx->g_first, first);
     if (rc) return rc;
@@ -667,16 +698,9 @@ int dsg_create(const dsg_config *cfg, dsg_ctx **out) {
     return dsg::set_error(nullptr, DSG_E_ARG, "grid %dx%dx%d too small", cfg->nx, cfg->ny, cfg->nz);
   if (cfg->mode < 0 || cfg->mode > DSG_MODE_LEARNED)
     return dsg::set_error(nullptr, DSG_E_ARG, "unknown mode %d", cfg->mode);
-  // memoryaloc, main.f:284-298
-  int nn = cfg->nx < cfg->ny ? cfg->nx : cfg->ny;
-  nn = nn < cfg->nz ? nn : cfg->nz;
-  int j = nn - 2, ng = 1;
-  while (j > 2) {
-    j /= 2;
-    ng++;
-  }
-  if ((1 << ng) + 2 != nn || ng > 30)
-    return dsg::set_error(nullptr, DSG_E_ARG, "STOP: nn .ne. 2**ng + 2 (%d vs %d)", nn, (1 << ng) + 2);
+  // memoryaloc, main.f:284-298 (generalised to sides that are not 2^k+2)
+  const int ng = dsg::level_count(cfg->nx, cfg->ny, cfg->nz);
+  if (ng < 1) return dsg::set_error(nullptr, DSG_E_ARG, "grid %dx%dx%d too small", cfg->nx, cfg->ny, cfg->nz);
   dsg_ctx *ctx = new dsg_ctx();
   ctx->cfg = *cfg;
   ctx->nx = cfg->nx;
@@ -748,6 +772,12 @@ int dsg_create(const dsg_config *cfg, dsg_ctx **out) {
   ctx->s.cycles = cfg->cycles;
   ctx->s.ng = ng;
   ctx->s.last_epsdiv = -1.0;
+  {
+    const long long cap = cfg->tail_nodes == 0 ? 18LL * 18 * 18 : cfg->tail_nodes;
+    ctx->tail_top = 0;
+    for (int l = 1; l < ng && l <= dsg::kTailMaxLevels; l++)
+      if ((long long)ctx->lnx[l] * ctx->lny[l] * ctx->lnz[l] <= cap) ctx->tail_top = l;
+  }
   nondim(ctx);
   *out = ctx;
   return DSG_OK;
@@ -941,6 +971,9 @@ int dsg_solvelpres(dsg_ctx *ctx, int t, dsg_mg_stats *stats) {
   if (rc && rc != DSG_E_NOT_CONVERGED) return rc;
   const int mg_rc = rc;
   DSG_CK(ctx, phase_mark(ctx, 5));
+  if (ctx->net)
+    DSG_CK(ctx, cudaMemcpyAsync(ctx->f[DSG_F_PPREV2], ctx->f[DSG_F_PPREV], d.count() * sizeof(double),
+                                cudaMemcpyDeviceToDevice, st));
   DSG_CK(ctx, cudaMemcpyAsync(ctx->f[DSG_F_PPREV], w1, d.count() * sizeof(double), cudaMemcpyDeviceToDevice, st));
   DSG_CK(ctx, dsg::project(u, v, w, w1, a, b, c, d, st));
   DSG_CK(ctx, dsg::bc_v(u, v, w, ctx->red_partials, d, s.xvel2, st));

@@ -40,6 +40,27 @@ inline dim3 interior_grid(const Dims &d, dim3 blk) {
               (unsigned)(d.nz - 2));
 }
 
+// Number of multigrid levels.  For min(nx,ny,nz) = 2^k+2 it is memoryaloc's
+// count (main.f:284-298), halving until the smallest interior extent is 2.
+// Other sides, which the reference refuses (main.f:296-297), coarsen while every
+// interior extent is even and the smallest is at least 4 (48, 96 and 160 cells
+// per side end at 3, 3 and 5 coarsest cells).  0 below 2 interior cells.
+inline int level_count(int nx, int ny, int nz) {
+  int mx = nx - 2, my = ny - 2, mz = nz - 2;
+  if (mx < 2 || my < 2 || mz < 2) return 0;
+  int ng = 1;
+  for (;;) {
+    int m = mx < my ? mx : my;
+    m = mz < m ? mz : m;
+    if (m < 4 || (mx & 1) || (my & 1) || (mz & 1) || ng >= 31) break;
+    mx /= 2;
+    my /= 2;
+    mz /= 2;
+    ng++;
+  }
+  return ng;
+}
+
 // Number of blocks of the deterministic reductions (fixed so that results do
 // not depend on the device).
 constexpr int kRedBlocks = 1216;  // 8 x 152 SMs
@@ -107,8 +128,8 @@ cudaError_t project(double *u, double *v, double *w, const double *p, const doub
 // mg32.cu (mixed precision)
 cudaError_t relax32_n(int n, float *u, float h2, const float *rhs, const float *a, const float *b, const float *c,
                       const float *ei, Dims d, float omega, cudaStream_t st);
-cudaError_t resid_restrict32(float *rhs_c, const float *u, const float *rhs, const float *a, const float *b,
-                             const float *c, Dims df, float h2i, cudaStream_t st);
+cudaError_t resid_restrict32(float *rhs_c, float *u_c, const float *u, const float *rhs, const float *a,
+                             const float *b, const float *c, Dims df, float h2i, cudaStream_t st);
 cudaError_t addint32(float *uf, const float *uc, Dims df, cudaStream_t st);
 cudaError_t interp32(float *uf, const float *uc, Dims df, cudaStream_t st);
 cudaError_t restrict32(float *uc, const float *uf, Dims dc, cudaStream_t st);
@@ -116,11 +137,27 @@ cudaError_t acfromac32(float *a, float *b, float *c, float *ei, const float *a2,
                        Dims dc, cudaStream_t st);
 cudaError_t acfromac64to32(float *a, float *b, float *c, float *ei, const double *a2, const double *b2,
                            const double *c2, Dims dc, cudaStream_t st);
+// coarse tail: levels top..1 of one V-cycle in one thread block (per instance)
+constexpr int kTailThreads = 1024;
+constexpr int kTailMaxLevels = 12;
+struct TailLevel {
+  float *u, *rhs;
+  const float *a, *b, *c, *ei;
+  Dims d;
+  float h2;
+};
+struct TailArgs {
+  TailLevel lv[kTailMaxLevels + 1];  // 1..top
+  int top, npre, npost, ntop;
+  float omega;
+};
+cudaError_t vtail32(const TailArgs &args, cudaStream_t st);
+cudaError_t vtail32_batch(const TailArgs *args_dev, int n, cudaStream_t st);
 // finest level in colour-split storage ({even, odd} arrays of (nx-2)/2 x (ny-2) x (nz-2))
 cudaError_t relax32_split_n(int n, float *const u[2], float *const rhs[2], const float *cc, Dims d, float h2,
                             float omega, float r1, float r2, cudaStream_t st);
-cudaError_t resid_restrict32_split(float *rhs_c, float *const u[2], float *const rhs[2], const float *cc, Dims df,
-                                   float h2i, float r1, float r2, cudaStream_t st);
+cudaError_t resid_restrict32_split(float *rhs_c, float *u_c, float *const u[2], float *const rhs[2], const float *cc,
+                                   Dims df, float h2i, float r1, float r2, cudaStream_t st);
 cudaError_t prolong32_split(float *const u[2], const float *uc, Dims df, int add, cudaStream_t st);
 cudaError_t restrict32_split(float *uc, float *const rhs[2], Dims dc, cudaStream_t st);
 cudaError_t split_from64(float *const dst[2], const double *src, Dims d, cudaStream_t st);
@@ -141,9 +178,10 @@ namespace dsg {
 namespace nn {
 // nn.cu: features of the current pressure system into the network input (and
 // the training target when p is given); p = p_prev + network correction.
-int net_features(dsg_net *n, const double *cc, const double *rhs, const double *pprev, const double *p,
-                 const double *a, const double *b, const double *c, Dims d, double lengthsize, cudaStream_t st);
-int net_guess(dsg_net *n, double *p, const double *pprev, Dims d, double lengthsize, cudaStream_t st);
+int net_features(dsg_net *n, const double *cc, const double *rhs, const double *p1, const double *p2,
+                 const double *p, const double *a, const double *b, const double *c, Dims d, double lengthsize,
+                 cudaStream_t st);
+int net_guess(dsg_net *n, double *p, const double *p2, Dims d, cudaStream_t st);
 void net_set_target(dsg_net *n, bool v, cudaStream_t st);
 }  // namespace nn
 }  // namespace dsg
@@ -163,6 +201,7 @@ struct dsg_ctx {
   dsg_config cfg;
   dsg_scalars s;
   int nx, ny, nz, ng;
+  int tail_top = 0;           // FP32 levels 1..tail_top run in the single-block tail kernel (0: none)
   int lnx[32], lny[32], lnz[32];
   double *lv[32][8];          // [level][CC,P,RES,RHS,A,B,C,EI], level 1..ng
   float *lv32[32][6];         // FP32 hierarchy [level][U,RHS,A,B,C,EI] of the mixed mode;

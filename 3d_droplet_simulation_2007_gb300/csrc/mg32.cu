@@ -112,7 +112,7 @@ __global__ void k_relax32_split(float *__restrict__ self, const float *__restric
 
 // Finest-level residual (cc-derived operator, virtual ghosts) restricted to the
 // coarse rhs: mean of the 8 fine residuals of each coarse cell.
-__global__ void k_resid_restrict32_split(float *__restrict__ rhs_c, const float *__restrict__ ue,
+__global__ void k_resid_restrict32_split(float *__restrict__ rhs_c, float *__restrict__ u_c, const float *__restrict__ ue,
                                          const float *__restrict__ uo, const float *__restrict__ re,
                                          const float *__restrict__ ro, const float *__restrict__ cc, Dims df,
                                          Split sp, Dims dc, float h2i, float r1, float r2) {
@@ -147,7 +147,9 @@ __global__ void k_resid_restrict32_split(float *__restrict__ rhs_c, const float 
                           cb * (zm - uc);
         acc += split_get(re, ro, sp, i, j, k) - h2i * lap;
       }
-  rhs_c[dc.ix(ic, jc, kc)] = 0.125f * acc;
+  const size_t qc = dc.ix(ic, jc, kc);
+  rhs_c[qc] = 0.125f * acc;
+  u_c[qc] = 0.f;
 }
 
 // Fine (split) u = or += injection of the coarse correction.
@@ -192,14 +194,15 @@ __global__ void k_split_from64(float *__restrict__ ev, float *__restrict__ od, c
   dst[sp.at((i - 2) >> 1, j, k)] = (float)src[d.ix(i, j, k)];
 }
 
-__global__ void k_relax32(float *__restrict__ u, const float *__restrict__ rhs, const float *__restrict__ a,
-                          const float *__restrict__ b, const float *__restrict__ c, const float *__restrict__ ei,
-                          Dims d, float h2, float omega, int colour) {
-  const int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
-  const int k = blockIdx.z + 2;
-  if (j > d.ny - 1) return;
-  const int i = 2 + ((j + k + colour) & 1) + 2 * (int)(blockIdx.x * blockDim.x + threadIdx.x);
-  if (i > d.nx - 1) return;
+// ---- coarse levels: natural layout ------------------------------------------
+//
+// The per-cell operations are shared by the one-launch-per-pass kernels and by
+// the single-block tail kernel below, so both give the same bits.
+
+// One red-black update of cell (i,j,k) (relax, main.f:3956-3997).
+__device__ __forceinline__ void relax32_cell(float *u, const float *rhs, const float *a, const float *b,
+                                             const float *c, const float *ei, Dims d, int i, int j, int k,
+                                             float h2, float omega) {
   const size_t q = d.ix(i, j, k);
   const size_t sy = d.sy(), sz = d.sz();
   const float uc = u[q];
@@ -209,15 +212,11 @@ __global__ void k_relax32(float *__restrict__ u, const float *__restrict__ rhs, 
   u[q] = omega * (s * ei[q]) + (1.f - omega) * uc;
 }
 
-// Coarse rhs = mean of the 8 fine residuals (resid + rstrct, main.f:3718-3725).
-__global__ void k_resid_restrict32(float *__restrict__ rhs_c, const float *__restrict__ u,
-                                   const float *__restrict__ rhs, const float *__restrict__ a,
-                                   const float *__restrict__ b, const float *__restrict__ c, Dims df, Dims dc,
-                                   float h2i) {
-  const int ic = blockIdx.x * blockDim.x + threadIdx.x + 2;
-  const int jc = blockIdx.y * blockDim.y + threadIdx.y + 2;
-  const int kc = blockIdx.z + 2;
-  if (ic > dc.nx - 1 || jc > dc.ny - 1) return;
+// Coarse rhs of coarse cell (ic,jc,kc) = mean of its 8 fine residuals (resid +
+// rstrct, main.f:3718-3725); the coarse correction starts at zero (main.f:3726).
+__device__ __forceinline__ void resid_restrict32_cell(float *rhs_c, float *u_c, const float *u, const float *rhs,
+                                                      const float *a, const float *b, const float *c, Dims df,
+                                                      Dims dc, float h2i, int ic, int jc, int kc) {
   const size_t sy = df.sy(), sz = df.sz();
   float acc = 0.f;
 #pragma unroll
@@ -234,7 +233,33 @@ __global__ void k_resid_restrict32(float *__restrict__ rhs_c, const float *__res
                           b[q - sy] * (n.ym - uc) + c[q] * (n.zp - uc) + c[q - sz] * (n.zm - uc);
         acc += rhs[q] - h2i * lap;
       }
-  rhs_c[dc.ix(ic, jc, kc)] = 0.125f * acc;
+  const size_t qc = dc.ix(ic, jc, kc);
+  rhs_c[qc] = 0.125f * acc;
+  u_c[qc] = 0.f;
+}
+
+__global__ void k_relax32(float *__restrict__ u, const float *__restrict__ rhs, const float *__restrict__ a,
+                          const float *__restrict__ b, const float *__restrict__ c, const float *__restrict__ ei,
+                          Dims d, float h2, float omega, int colour) {
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
+  const int k = blockIdx.z + 2;
+  if (j > d.ny - 1) return;
+  const int i = 2 + ((j + k + colour) & 1) + 2 * (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (i > d.nx - 1) return;
+  relax32_cell(u, rhs, a, b, c, ei, d, i, j, k, h2, omega);
+}
+
+// Coarse rhs = mean of the 8 fine residuals; coarse correction = 0 (interior;
+// the FP32 kernels never read ghost values).
+__global__ void k_resid_restrict32(float *__restrict__ rhs_c, float *__restrict__ u_c, const float *__restrict__ u,
+                                   const float *__restrict__ rhs, const float *__restrict__ a,
+                                   const float *__restrict__ b, const float *__restrict__ c, Dims df, Dims dc,
+                                   float h2i) {
+  const int ic = blockIdx.x * blockDim.x + threadIdx.x + 2;
+  const int jc = blockIdx.y * blockDim.y + threadIdx.y + 2;
+  const int kc = blockIdx.z + 2;
+  if (ic > dc.nx - 1 || jc > dc.ny - 1) return;
+  resid_restrict32_cell(rhs_c, u_c, u, rhs, a, b, c, df, dc, h2i, ic, jc, kc);
 }
 
 // u += injection of the coarse correction (addint, main.f:3934-3954), interior.
@@ -244,6 +269,64 @@ __global__ void k_addint32(float *__restrict__ uf, const float *__restrict__ uc,
   const int k = blockIdx.z + 2;
   if (i > df.nx - 1 || j > df.ny - 1) return;
   uf[df.ix(i, j, k)] += uc[dc.ix((i >> 1) + 1, (j >> 1) + 1, (k >> 1) + 1)];
+}
+
+// ---- coarse tail: every level at or below `top` in one thread block ---------
+//
+// On levels of a few thousand cells a launch costs more than its work.  The
+// tail kernel runs the rest of a V-cycle from level `top` down to the coarsest
+// grid and back (pre-sweeps, residual restriction, NTOP coarsest sweeps,
+// prolongation, post-sweeps: mglin's recursion, main.f:3703-3759) inside one
+// block, with a block barrier between passes in place of a launch boundary.
+// The level arrays stay in L1/L2.  One block per instance: the ensemble
+// launches one block per member.
+__device__ void tail_relax(const TailLevel &L, int n, float omega) {
+  const Dims d = L.d;
+  const int hx = (d.nx - 1) / 2;  // cells of one colour per row, rounded up
+  const int ny2 = d.ny - 2;
+  const int total = hx * ny2 * (d.nz - 2);
+  for (int s = 0; s < n; s++)
+    for (int colour = 0; colour < 2; colour++) {
+      for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        const int m = t % hx, r = t / hx;
+        const int j = 2 + r % ny2, k = 2 + r / ny2;
+        const int i = 2 + ((j + k + colour) & 1) + 2 * m;
+        if (i <= d.nx - 1) relax32_cell(L.u, L.rhs, L.a, L.b, L.c, L.ei, d, i, j, k, L.h2, omega);
+      }
+      __syncthreads();
+    }
+}
+
+__device__ void tail_body(const TailArgs &A) {
+  for (int l = A.top; l >= 2; l--) {
+    const TailLevel &F = A.lv[l], &C = A.lv[l - 1];
+    tail_relax(F, A.npre, A.omega);
+    const int cx = C.d.nx - 2, cy = C.d.ny - 2, total = cx * cy * (C.d.nz - 2);
+    const float h2i = 1.0f / F.h2;
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+      const int ic = 2 + t % cx, r = t / cx;
+      resid_restrict32_cell(C.rhs, C.u, F.u, F.rhs, F.a, F.b, F.c, F.d, C.d, h2i, ic, 2 + r % cy, 2 + r / cy);
+    }
+    __syncthreads();
+  }
+  tail_relax(A.lv[1], A.ntop, A.omega);
+  for (int l = 2; l <= A.top; l++) {
+    const TailLevel &F = A.lv[l], &C = A.lv[l - 1];
+    const int fx = F.d.nx - 2, fy = F.d.ny - 2, total = fx * fy * (F.d.nz - 2);
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+      const int i = 2 + t % fx, r = t / fx;
+      const int j = 2 + r % fy, k = 2 + r / fy;
+      F.u[F.d.ix(i, j, k)] += C.u[C.d.ix((i >> 1) + 1, (j >> 1) + 1, (k >> 1) + 1)];
+    }
+    __syncthreads();
+    tail_relax(F, A.npost, A.omega);
+  }
+}
+
+__global__ void __launch_bounds__(kTailThreads, 1) k_vtail32(TailArgs A) { tail_body(A); }
+
+__global__ void __launch_bounds__(kTailThreads, 1) k_vtail32_batch(const TailArgs *__restrict__ all, int n) {
+  if ((int)blockIdx.x < n) tail_body(all[blockIdx.x]);
 }
 
 // Interior injection (interp, main.f:3866-3900) for the FMG start.
@@ -444,12 +527,12 @@ cudaError_t relax32_split_n(int n, float *const u[2], float *const rhs[2], const
   return cudaGetLastError();
 }
 
-cudaError_t resid_restrict32_split(float *rhs_c, float *const u[2], float *const rhs[2], const float *cc, Dims df,
-                                   float h2i, float r1, float r2, cudaStream_t st) {
+cudaError_t resid_restrict32_split(float *rhs_c, float *u_c, float *const u[2], float *const rhs[2], const float *cc,
+                                   Dims df, float h2i, float r1, float r2, cudaStream_t st) {
   const Dims dc{df.nx / 2 + 1, df.ny / 2 + 1, df.nz / 2 + 1};
   const Split sp{(df.nx - 2) >> 1, df.ny - 2, df.nz - 2};
-  DSG_COUNT k_resid_restrict32_split<<<interior_grid(dc, kBlk), kBlk, 0, st>>>(rhs_c, u[0], u[1], rhs[0], rhs[1], cc,
-                                                                            df, sp, dc, h2i, r1, r2);
+  DSG_COUNT k_resid_restrict32_split<<<interior_grid(dc, kBlk), kBlk, 0, st>>>(rhs_c, u_c, u[0], u[1], rhs[0], rhs[1],
+                                                                            cc, df, sp, dc, h2i, r1, r2);
   return cudaGetLastError();
 }
 
@@ -473,10 +556,21 @@ cudaError_t split_from64(float *const dst[2], const double *src, Dims d, cudaStr
   return cudaGetLastError();
 }
 
-cudaError_t resid_restrict32(float *rhs_c, const float *u, const float *rhs, const float *a, const float *b,
-                             const float *c, Dims df, float h2i, cudaStream_t st) {
+cudaError_t resid_restrict32(float *rhs_c, float *u_c, const float *u, const float *rhs, const float *a,
+                             const float *b, const float *c, Dims df, float h2i, cudaStream_t st) {
   const Dims dc{df.nx / 2 + 1, df.ny / 2 + 1, df.nz / 2 + 1};
-  DSG_COUNT k_resid_restrict32<<<interior_grid(dc, kBlk), kBlk, 0, st>>>(rhs_c, u, rhs, a, b, c, df, dc, h2i);
+  DSG_COUNT k_resid_restrict32<<<interior_grid(dc, kBlk), kBlk, 0, st>>>(rhs_c, u_c, u, rhs, a, b, c, df, dc, h2i);
+  return cudaGetLastError();
+}
+
+cudaError_t vtail32(const TailArgs &args, cudaStream_t st) {
+  DSG_COUNT k_vtail32<<<1, kTailThreads, 0, st>>>(args);
+  return cudaGetLastError();
+}
+
+cudaError_t vtail32_batch(const TailArgs *args_dev, int n, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  DSG_COUNT k_vtail32_batch<<<n, kTailThreads, 0, st>>>(args_dev, n);
   return cudaGetLastError();
 }
 

@@ -38,8 +38,9 @@ struct LayerDef {
   bool relu;
 };
 constexpr int kLayers = 7;
+constexpr int kIn = DSG_NET_INPUTS;  // logical input channels (padded to 16)
 constexpr LayerDef kDefs[kLayers] = {
-    {3, 16, 16, 16, 0, true},   // E1
+    {kIn, 16, 16, 16, 0, true}, // E1
     {16, 32, 16, 32, 1, true},  // E2
     {32, 64, 32, 64, 2, true},  // E3
     {64, 64, 64, 64, 3, true},  // E4
@@ -53,7 +54,7 @@ constexpr LayerDef kDefs[kLayers] = {
 inline int grad_ch(int l) { return kDefs[l].coutp < 16 ? 16 : kDefs[l].coutp; }
 
 inline long long layer_params(int l) { return 27LL * kDefs[l].cin * kDefs[l].cout + kDefs[l].cout; }
-constexpr long long kParams = 27LL * (3 * 16 + 16 * 32 + 32 * 64 + 64 * 64 + 64 * 32 + 32 * 16 + 16 * 1) +
+constexpr long long kParams = 27LL * (kIn * 16 + 16 * 32 + 32 * 64 + 64 * 64 + 64 * 32 + 32 * 16 + 16 * 1) +
                               (16 + 32 + 64 + 64 + 32 + 16 + 1);
 #define DSG_NET_PARAMS ((size_t)dsg::nn::kParams)
 
@@ -412,14 +413,17 @@ __global__ void k_adam(float *__restrict__ p, const float *__restrict__ g, float
 }
 
 // Network input from the solver fields (interior cells, channels-last, 16 padded
-// channels): c0 = volume fraction, c1 = rhs / s, c2 = (rhs - L p_prev) / s, where
-// s = RMS(rhs) is read from device memory.  Also writes the FP32 target
-// (p - p_prev) / (s h^2) when p is given (training snapshots).
+// channels): c0 = volume fraction, c1 = rhs / s_r, c2 = (rhs - L p1) / s_r,
+// c3 = p1 / s_p, c4 = p2 / s_p, where p1, p2 are the pressures of the last two
+// steps, s_r = RMS(rhs) and s_p = RMS(p1) (sums[0], sums[1] in device memory).
+// With p given (training snapshots) also writes the FP32 target (p - p2) / s_p.
+// The pressure alternates in sign from step to step (the off-diagonal stresses
+// carry over with a sign flip, main.f:3291-3300), so p2 is the closer base.
 __global__ void k_features(bf16 *__restrict__ Xin, float *__restrict__ target, const double *__restrict__ cc,
-                           const double *__restrict__ rhs, const double *__restrict__ pprev,
-                           const double *__restrict__ p, const double *__restrict__ a, const double *__restrict__ b,
-                           const double *__restrict__ c, const double *__restrict__ sums, Dims d, double h2i,
-                           double h2) {
+                           const double *__restrict__ rhs, const double *__restrict__ p1,
+                           const double *__restrict__ p2, const double *__restrict__ p,
+                           const double *__restrict__ a, const double *__restrict__ b,
+                           const double *__restrict__ c, const double *__restrict__ sums, Dims d, double h2i) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
@@ -429,42 +433,45 @@ __global__ void k_features(bf16 *__restrict__ Xin, float *__restrict__ target, c
   const size_t q = d.ix(i, j, k);
   const size_t sy = d.sy(), sz = d.sz();
   const double n_int = (double)W * H * (d.nz - 2);
-  const double s = sqrt(sums[0] / n_int) + 1e-300;
-  const double uc = pprev[q];
-  const double xp = (i + 1 == d.nx) ? 0.0 : pprev[q + 1];
-  const double xm = (i - 1 == 1) ? uc : pprev[q - 1];
-  const double yp = (j + 1 == d.ny) ? uc : pprev[q + sy];
-  const double ym = (j - 1 == 1) ? uc : pprev[q - sy];
-  const double zp = (k + 1 == d.nz) ? uc : pprev[q + sz];
-  const double zm = (k - 1 == 1) ? uc : pprev[q - sz];
+  const double sr = sqrt(sums[0] / n_int) + 1e-300;
+  const double sp = sqrt(sums[1] / n_int) + 1e-300;
+  const double uc = p1[q];
+  const double xp = (i + 1 == d.nx) ? 0.0 : p1[q + 1];
+  const double xm = (i - 1 == 1) ? uc : p1[q - 1];
+  const double yp = (j + 1 == d.ny) ? uc : p1[q + sy];
+  const double ym = (j - 1 == 1) ? uc : p1[q - sy];
+  const double zp = (k + 1 == d.nz) ? uc : p1[q + sz];
+  const double zm = (k - 1 == 1) ? uc : p1[q - sz];
   const double r = -h2i * (a[q] * (xp - uc) + a[q - 1] * (xm - uc) + b[q] * (yp - uc) + b[q - sy] * (ym - uc) +
                            c[q] * (zp - uc) + c[q - sz] * (zm - uc)) +
                    rhs[q];
   const size_t v = ((size_t)z * H + y) * W + x;
   bf16 *o = Xin + v * 16;
   o[0] = __float2bfloat16((float)cc[q]);
-  o[1] = __float2bfloat16((float)(rhs[q] / s));
-  o[2] = __float2bfloat16((float)(r / s));
+  o[1] = __float2bfloat16((float)(rhs[q] / sr));
+  o[2] = __float2bfloat16((float)(r / sr));
+  o[3] = __float2bfloat16((float)(uc / sp));
+  o[4] = __float2bfloat16((float)(p2[q] / sp));
 #pragma unroll
-  for (int ch = 3; ch < 16; ch++) o[ch] = __float2bfloat16(0.f);
-  if (target) target[v] = (float)((p[q] - uc) / (s * h2));
+  for (int ch = 5; ch < 16; ch++) o[ch] = __float2bfloat16(0.f);
+  if (target) target[v] = (float)((p[q] - p2[q]) / sp);
 }
 
-// p = p_prev + s h^2 q over the interior (q = network output, channel 0 of 8).
-__global__ void k_apply_guess(double *__restrict__ p, const double *__restrict__ pprev, const float *__restrict__ qout,
-                              const double *__restrict__ sums, Dims d, double h2) {
+// p = p2 + s_p q over the interior (q = network output, channel 0 of 8).
+__global__ void k_apply_guess(double *__restrict__ p, const double *__restrict__ p2, const float *__restrict__ qout,
+                              const double *__restrict__ sums, Dims d) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
   const int W = d.nx - 2, H = d.ny - 2;
   if (x >= W || y >= H) return;
-  const double s = sqrt(sums[0] / ((double)W * H * (d.nz - 2))) + 1e-300;
+  const double sp = sqrt(sums[1] / ((double)W * H * (d.nz - 2))) + 1e-300;
   const size_t q = d.ix(x + 2, y + 2, z + 2);
   const size_t v = ((size_t)z * H + y) * W + x;
-  p[q] = pprev[q] + s * h2 * (double)qout[v * 8];
+  p[q] = p2[q] + sp * (double)qout[v * 8];
 }
 
-// sums[0] = sum of rhs^2 over the interior (single block per launch row, atomics).
+// *sums += sum of f^2 over the interior (block partials, one atomic per block).
 __global__ void k_sumsq(const double *__restrict__ f, double *__restrict__ sums, Dims d) {
   __shared__ double sh[256];
   const size_t n = (size_t)(d.nx - 2) * (d.ny - 2) * (d.nz - 2);
@@ -514,7 +521,7 @@ struct dsg_net {
   float *tmp;                       // FP32 gradient of a decoder output
   float *wscratch;                  // bias (64) + padded weight gradient of one layer
   float *xin_f32, *yhost_f32;       // staging of the host-array entry points
-  double *loss_dev, *sums_dev;      // loss; sum of rhs^2 of the current system
+  double *loss_dev, *sums_dev;      // loss; sums of rhs^2 and p1^2 of the current system
   double *loss_host;
   long long step = 0;               // Adam steps taken
   bool have_target = false;         // a training pair is recorded
@@ -737,7 +744,7 @@ int loss_grad(dsg_net *n, cudaStream_t st) {
 __global__ void k_input_from_f32(bf16 *__restrict__ x0, const float *__restrict__ x, size_t nvox) {
   for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < nvox; v += (size_t)gridDim.x * blockDim.x)
 #pragma unroll
-    for (int c = 0; c < 16; c++) x0[v * 16 + c] = __float2bfloat16(c < 3 ? x[v * 3 + c] : 0.f);
+    for (int c = 0; c < 16; c++) x0[v * 16 + c] = __float2bfloat16(c < kIn ? x[v * kIn + c] : 0.f);
 }
 
 __global__ void k_output_ch0(float *__restrict__ y, const float *__restrict__ yout, size_t nvox) {
@@ -765,28 +772,29 @@ namespace nn {
 
 // Solver hooks (used by dsg.cu): features of the current pressure system into
 // the network input; optional training target from the solved pressure.
-int net_features(dsg_net *n, const double *cc, const double *rhs, const double *pprev, const double *p,
-                 const double *a, const double *b, const double *c, Dims d, double lengthsize, cudaStream_t st) {
+int net_features(dsg_net *n, const double *cc, const double *rhs, const double *p1, const double *p2,
+                 const double *p, const double *a, const double *b, const double *c, Dims d, double lengthsize,
+                 cudaStream_t st) {
   if (n->W[0] != d.nx - 2 || n->H[0] != d.ny - 2 || n->D[0] != d.nz - 2)
     return dsg::set_error(nullptr, DSG_E_ARG, "network sized %dx%dx%d, grid interior %dx%dx%d", n->W[0], n->H[0],
                           n->D[0], d.nx - 2, d.ny - 2, d.nz - 2);
   const double h1 = lengthsize / (d.nx - 2);
-  NCK(n, cudaMemsetAsync(n->sums_dev, 0, sizeof(double), st));
+  NCK(n, cudaMemsetAsync(n->sums_dev, 0, 2 * sizeof(double), st));
   DSG_COUNT k_sumsq<<<1216, 256, 0, st>>>(rhs, n->sums_dev, d);
+  DSG_COUNT k_sumsq<<<1216, 256, 0, st>>>(p1, n->sums_dev + 1, d);
   const dim3 blk(32, 8), grid((unsigned)((d.nx - 2 + 31) / 32), (unsigned)((d.ny - 2 + 7) / 8), (unsigned)(d.nz - 2));
-  DSG_COUNT k_features<<<grid, blk, 0, st>>>(n->x0, p ? n->target : nullptr, cc, rhs, pprev, p, a, b, c, n->sums_dev, d,
-                                             1.0 / (h1 * h1), h1 * h1);
+  DSG_COUNT k_features<<<grid, blk, 0, st>>>(n->x0, p ? n->target : nullptr, cc, rhs, p1, p2, p, a, b, c,
+                                             n->sums_dev, d, 1.0 / (h1 * h1));
   NCK(n, cudaGetLastError());
   return DSG_OK;
 }
 
-// p = p_prev + s h^2 net(x) on the interior (features must be current).
-int net_guess(dsg_net *n, double *p, const double *pprev, Dims d, double lengthsize, cudaStream_t st) {
+// p = p2 + s_p net(x) on the interior (features must be current).
+int net_guess(dsg_net *n, double *p, const double *p2, Dims d, cudaStream_t st) {
   int rc = forward(n, st);
   if (rc) return rc;
-  const double h1 = lengthsize / (d.nx - 2);
   const dim3 blk(32, 8), grid((unsigned)((d.nx - 2 + 31) / 32), (unsigned)((d.ny - 2 + 7) / 8), (unsigned)(d.nz - 2));
-  DSG_COUNT k_apply_guess<<<grid, blk, 0, st>>>(p, pprev, n->yout, n->sums_dev, d, h1 * h1);
+  DSG_COUNT k_apply_guess<<<grid, blk, 0, st>>>(p, p2, n->yout, n->sums_dev, d);
   NCK(n, cudaGetLastError());
   return DSG_OK;
 }
@@ -858,7 +866,7 @@ int dsg_net_create(int W, int H, int D, uint64_t seed, dsg_net **out) {
   plan.push_back({(void **)&n->gbuf, up(v0 * 16 * 2)});
   plan.push_back({(void **)&n->gbuf2, up(v0 * 16 * 2)});
   plan.push_back({(void **)&n->wscratch, up((64 + 27 * 64 * 64) * 4)});
-  plan.push_back({(void **)&n->xin_f32, up(v0 * 3 * 4)});
+  plan.push_back({(void **)&n->xin_f32, up(v0 * kIn * 4)});
   plan.push_back({(void **)&n->yhost_f32, up(v0 * 4)});
   plan.push_back({(void **)&n->loss_dev, 256});
   plan.push_back({(void **)&n->sums_dev, 256});
@@ -930,7 +938,7 @@ int dsg_net_set_params(dsg_net *n, const float *host, int64_t count) {
 int dsg_net_forward_host(dsg_net *n, const float *x, float *y) {
   if (!n || !x || !y) return dsg::set_error(nullptr, DSG_E_ARG, "null argument");
   const size_t v0 = vox(n, 0);
-  NCK(n, cudaMemcpy(n->xin_f32, x, v0 * 3 * sizeof(float), cudaMemcpyHostToDevice));
+  NCK(n, cudaMemcpy(n->xin_f32, x, v0 * kIn * sizeof(float), cudaMemcpyHostToDevice));
   DSG_COUNT k_input_from_f32<<<eblocks(v0), 256>>>(n->x0, n->xin_f32, v0);
   int rc = forward(n, 0);
   if (rc) return rc;
@@ -942,7 +950,7 @@ int dsg_net_forward_host(dsg_net *n, const float *x, float *y) {
 int dsg_net_grad_host(dsg_net *n, const float *x, const float *t, float *loss, float *grad) {
   if (!n || !x || !t || !loss || !grad) return dsg::set_error(nullptr, DSG_E_ARG, "null argument");
   const size_t v0 = vox(n, 0);
-  NCK(n, cudaMemcpy(n->xin_f32, x, v0 * 3 * sizeof(float), cudaMemcpyHostToDevice));
+  NCK(n, cudaMemcpy(n->xin_f32, x, v0 * kIn * sizeof(float), cudaMemcpyHostToDevice));
   DSG_COUNT k_input_from_f32<<<eblocks(v0), 256>>>(n->x0, n->xin_f32, v0);
   NCK(n, cudaMemcpy(n->target, t, v0 * sizeof(float), cudaMemcpyHostToDevice));
   int rc = forward(n, 0);

@@ -2,13 +2,19 @@
 
 A ``Net`` is the 3D convolutional U-Net of ``csrc/nn.cu`` (BF16 tensor-core
 kernels, FP32 accumulation) sized for one interior grid.  ``train`` runs the
-solver itself at 128^3 on droplets of random diameter (1-3 mm) and impact
-speed (0.5-4 m/s), records after every pressure solve the pair (features of
-the system, solved correction of the previous pressure) and takes one Adam
-step on it: the network learns from the solver's own snapshots, on the fly.
-In ``MODE_LEARNED`` the solver asks the attached network for a correction of
-the previous-step pressure and keeps it only if its FP64 residual is below
-that of the previous-step pressure itself.
+solver itself on droplets of random diameter (1-3 mm) and impact speed
+(0.5-4 m/s), records after every pressure solve the pair (features of the
+system, solved pressure) and takes one Adam step on it: the network learns
+from the solver's own snapshots, on the fly.  Training runs at 128^3 and is
+then continued at the grid the network will serve (the parameters carry over
+between grid sizes: the network is convolutional).
+
+The pressure of this scheme alternates in sign from step to step (the
+off-diagonal stresses carry over between steps with a sign flip,
+main.f:3291-3300), so the network sees the last two pressures p1, p2 and
+predicts the correction of p2.  In ``MODE_LEARNED`` the solver keeps the
+network's guess only if its FP64 residual is below that of the previous-step
+pressure p1, the guess it falls back to.
 """
 import ctypes as C
 import os
@@ -59,9 +65,9 @@ class Net:
         _lib.check(self.lib.dsg_net_set_params(self.h, v.ctypes.data, self.nparams))
 
     def forward(self, x):
-        """x: (D, H, W, 3) -> (D, H, W)."""
+        """x: (D, H, W, NET_INPUTS) -> (D, H, W)."""
         x = np.ascontiguousarray(x, dtype=np.float32)
-        assert x.shape == self.shape + (3,)
+        assert x.shape == self.shape + (_lib.NET_INPUTS,)
         y = np.empty(self.shape, dtype=np.float32)
         _lib.check(self.lib.dsg_net_forward_host(self.h, x.ctypes.data, y.ctypes.data))
         return y
@@ -102,26 +108,44 @@ def training_instances(count, seed=0):
     return [(float(rng.uniform(1e-3, 3e-3)), float(rng.uniform(0.5, 4.0))) for _ in range(count)]
 
 
-def train(n=128, instances=20, steps=1000, lr=1e-3, seed=0, log=None, tol=1e-8):
+def train(n=128, instances=20, steps=1000, lr=1e-3, seed=0, log=None, tol=1e-8, max_seconds=None, net=None):
     """Train a network on the solver's own snapshots at n^3 (one Adam step per
-    solved time step).  Returns (net, history of losses)."""
+    solved time step from the third step on).  Continues ``net`` if given
+    (sized n^3).  Stops early, between instances, once ``max_seconds`` of wall
+    clock have passed.  Returns (net, history of losses)."""
+    import time
     from .solver import Solver
-    net = Net(n, seed=seed)
+    net = Net(n, seed=seed) if net is None else net
     losses = []
+    t0 = time.perf_counter()
     for k, (diam, speed) in enumerate(training_instances(instances, seed)):
+        if max_seconds is not None and k > 0 and time.perf_counter() - t0 > max_seconds:
+            break
         inp = droplet(n, steps=steps, impact_speed=speed, diameter=diam, noise_si=1e-4, mode=MODE_TOL_MIXED,
                       tol=tol, npre=4, npost=4, ntop=4, seed=seed * 1000 + k)
         with Solver(inp) as s:
             net.attach(s, record=True)
             for t in range(1, steps + 1):
-                s.step(t)
-                if t > 1:  # the first step has no previous pressure
+                try:
+                    s.step(t)
+                except _lib.DsgError as e:  # an unconverged or blown-up run ends its instance
+                    if log:
+                        log("instance %d stopped at step %d: %s" % (k, t, e))
+                    break
+                if t > 2:  # the first two steps lack a pressure history
                     losses.append(net.train_step(lr))
             detach(s)
         if log:
-            log("instance %d (D=%.2f mm, v=%.2f m/s): mean loss of its last 50 steps %.4g"
-                % (k, diam * 1e3, speed, float(np.mean(losses[-50:])) if losses else float("nan")))
+            log("n=%d instance %d (D=%.2f mm, v=%.2f m/s): mean loss of its last 50 steps %.4g"
+                % (n, k, diam * 1e3, speed, float(np.mean(losses[-50:])) if losses else float("nan")))
     return net, losses
+
+
+def resized(net, n):
+    """A network for an n^3 grid with the parameters of ``net``."""
+    out = Net(n)
+    out.params = net.params
+    return out
 
 
 def learned_config(inp):
@@ -131,12 +155,13 @@ def learned_config(inp):
     return InputData(**d)
 
 
-def evaluate(inp, net=None, steps=8, warmup=2, stream=None):
+def evaluate(inp, net=None, steps=8, warmup=2):
     """Run `steps` time steps (after `warmup`) and report V-cycles, initial
     residuals, guard fallbacks and ms per step."""
     import time
     from .solver import Solver
-    out = {"vcycles": [], "relres_init": [], "fallback": [], "relres_net": [], "relres_prev": []}
+    keys = ("vcycles", "relres_init", "fallback", "relres_net", "relres_prev")
+    out = {k: [] for k in keys}
     with Solver(inp) as s:
         if net is not None:
             net.attach(s)
@@ -146,13 +171,23 @@ def evaluate(inp, net=None, steps=8, warmup=2, stream=None):
         t0 = time.perf_counter()
         for t in range(warmup + 1, warmup + steps + 1):
             st = s.step(t)
-            for k in out:
-                out[k].append(st[k] if k in st else None)
+            for k in keys:
+                out[k].append(st[k])
         s.synchronize()
         out["ms_per_step"] = 1e3 * (time.perf_counter() - t0) / steps
         if net is not None:
             detach(s)
     return out
+
+
+def compare_starts(n, net, steps=8, warmup=20, speed=3.0, diameter=2e-3, seed=0):
+    """V-cycles and time per step at n^3 from the FP32 full-multigrid start,
+    from the previous-step pressure, and from the guarded learned guess."""
+    base = droplet(n, steps=1000, impact_speed=speed, diameter=diameter, noise_si=1e-4, mode=MODE_TOL_MIXED,
+                   tol=1e-8, npre=4, npost=4, ntop=4, seed=seed)
+    return {"fmg_start": evaluate(base, steps=steps, warmup=warmup),
+            "previous_pressure_start": evaluate(base.replace(warm_start=1), steps=steps, warmup=warmup),
+            "learned_start": evaluate(learned_config(base), net, steps=steps, warmup=warmup)}
 
 
 def main(argv=None):
@@ -165,27 +200,30 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--fine-n", type=int, default=256, help="grid of the second training phase (0: none)")
+    ap.add_argument("--fine-instances", type=int, default=4)
+    ap.add_argument("--fine-steps", type=int, default=400)
     ap.add_argument("--out", default=WEIGHTS)
-    ap.add_argument("--eval-n", type=int, default=256)
     ap.add_argument("--eval-steps", type=int, default=8)
+    ap.add_argument("--eval-warmup", type=int, default=20)
+    ap.add_argument("--max-seconds", type=float, default=None)
     a = ap.parse_args(argv)
     t0 = time.perf_counter()
-    net, losses = train(a.n, a.instances, a.steps, a.lr, a.seed, log=print)
-    t_train = time.perf_counter() - t0
+    net, losses = train(a.n, a.instances, a.steps, a.lr, a.seed, log=print, max_seconds=a.max_seconds)
+    t1 = time.perf_counter()
+    rec = {"snapshots": len(losses), "train_s": t1 - t0, "loss_first": float(np.mean(losses[:50])),
+           "loss_last": float(np.mean(losses[-200:]))}
+    if a.fine_n:
+        net = resized(net, a.fine_n)
+        net, l2 = train(a.fine_n, a.fine_instances, a.fine_steps, 0.5 * a.lr, a.seed + 1, log=print, net=net)
+        rec.update({"fine_n": a.fine_n, "fine_snapshots": len(l2), "fine_train_s": time.perf_counter() - t1,
+                    "fine_loss_first": float(np.mean(l2[:20])), "fine_loss_last": float(np.mean(l2[-100:]))})
     net.save(a.out)
-    print(json.dumps({"snapshots": len(losses), "train_s": t_train, "loss_first": float(np.mean(losses[:50])),
-                      "loss_last": float(np.mean(losses[-200:]))}))
+    print(json.dumps(rec))
     if a.eval_steps:
-        n = a.eval_n
-        base = droplet(n, steps=1000, impact_speed=3.0, noise_si=1e-4, mode=MODE_TOL_MIXED, tol=1e-8, npre=4, npost=4,
-                       ntop=4)
-        ev = Net(n).load(a.out)
-        zero = Net(n)
-        zero.params = np.zeros(zero.nparams, dtype=np.float32)
-        r_mixed = evaluate(base, steps=a.eval_steps)
-        r_prev = evaluate(learned_config(base), zero, steps=a.eval_steps)
-        r_learn = evaluate(learned_config(base), ev, steps=a.eval_steps)
-        print(json.dumps({"n": n, "fmg_start": r_mixed, "previous_pressure_start": r_prev, "learned_start": r_learn}))
+        n = a.fine_n or a.n
+        ev = resized(net, n)
+        print(json.dumps({"n": n, **compare_starts(n, ev, a.eval_steps, a.eval_warmup)}))
 
 
 if __name__ == "__main__":

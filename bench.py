@@ -42,6 +42,8 @@ def parse():
     ap.add_argument("--tol", type=float, default=1e-8)
     ap.add_argument("--inner", type=int, default=2, help="FP32 V-cycles per FP64 defect (mixed modes)")
     ap.add_argument("--no-graphs", action="store_true", help="launch the mixed solve without CUDA graphs")
+    ap.add_argument("--tail-nodes", type=int, default=0,
+                    help="largest FP32 level (nodes) of the single-block coarse tail (0: default, -1: off)")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -56,10 +58,11 @@ def dist_env():
     return ws, rank, local
 
 
-def workload(dsg, n, mode, tol, inner=2, graphs=True):
+def workload(dsg, n, mode, tol, inner=2, graphs=True, tail_nodes=0):
     cfg = dsg.config
     return cfg.droplet(n, steps=1000, impact_speed=3.0, noise_si=1e-4, mode=mode, tol=tol,
-                       npre=4, npost=4, ntop=4).replace(inner_vcycles=inner, use_graphs=1 if graphs else 0)
+                       npre=4, npost=4, ntop=4).replace(inner_vcycles=inner, use_graphs=1 if graphs else 0,
+                                                        tail_nodes=tail_nodes)
 
 
 def measured_peaks():
@@ -197,7 +200,7 @@ def run_gb300(args):
     dsg = importlib.import_module(PKG)
     dsg.load()
     mode = mode_of(dsg, args.mode)
-    inp = workload(dsg, args.n, mode, args.tol, args.inner, not args.no_graphs)
+    inp = workload(dsg, args.n, mode, args.tol, args.inner, not args.no_graphs, args.tail_nodes)
     solver = dsg.Solver(inp)
     solver.set_stream(torch.cuda.current_stream().cuda_stream)
     for t in range(1, args.warmup + 1):

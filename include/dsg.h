@@ -53,7 +53,8 @@ enum {
   DSG_F_S11 = 11, DSG_F_S22 = 12, DSG_F_S33 = 13, DSG_F_S12 = 14, DSG_F_S13 = 15, DSG_F_S23 = 16,
   DSG_F_RHON = 17, DSG_F_MUN = 18,
   DSG_F_PPREV = 19, /* previous-step pressure (build addition: the reference keeps none) */
-  DSG_NFIELDS = 20
+  DSG_F_PPREV2 = 20, /* pressure of two steps back (kept while a network is attached) */
+  DSG_NFIELDS = 21
 };
 
 /* The 38 positional values of inputdata.in (main.f:188-234) in file order,
@@ -77,6 +78,9 @@ typedef struct dsg_config {
   uint64_t noise_seed; /* seed of the counter-based noise */
   int inner_vcycles;   /* FP32 V-cycles per FP64 defect evaluation in the mixed modes (<= 0: 1) */
   int use_graphs;      /* capture the mixed-mode iterations in CUDA graphs (1) or launch directly (0) */
+  int tail_nodes;      /* mixed modes: FP32 levels of at most this many nodes run in one single-block
+                          launch per V-cycle (0: 18^3 = 5832; < 0: one launch per pass on every level) */
+  int warm_start;      /* DSG_MODE_TOL_MIXED: 0 = FP32 full-multigrid start, 1 = previous-step pressure */
 } dsg_config;
 
 /* Non-dimensional scalars and adaptive counters (COMMON /PHYSICS/, /DIFF/,
@@ -172,11 +176,14 @@ int64_t dsg_launch_count(void);
 
 /* ---- learned initial guess (no reference counterpart) ----------------------
  * A 3D convolutional U-Net (4 levels, 16/32/64/64 channels, 3x3x3 kernels,
- * 250785 parameters, BF16 weights/activations, FP32 accumulation, tensor-core
- * implicit-GEMM kernels) predicting the pressure correction from the volume
- * fraction (density), the divergence right-hand side and the previous
- * pressure (through its defect under the current operator).  A network is
- * sized for one interior grid W x H x D (each a multiple of 8). */
+ * 251649 parameters, BF16 weights/activations, FP32 accumulation, tensor-core
+ * implicit-GEMM kernels) predicting the pressure from DSG_NET_INPUTS channels:
+ * the volume fraction (density), the divergence right-hand side, the defect
+ * of the previous pressure p1 under the current operator, p1 and the pressure
+ * of two steps back p2.  Its output is the correction of p2 in units of
+ * RMS(p1).  A network is sized for one interior grid W x H x D (each a
+ * multiple of 8). */
+#define DSG_NET_INPUTS 5
 typedef struct dsg_net dsg_net;
 int64_t dsg_net_param_count(void);
 int dsg_net_create(int W, int H, int D, uint64_t seed, dsg_net **out); /* He-initialised */
@@ -185,8 +192,8 @@ int64_t dsg_net_device_bytes(const dsg_net *net);
 /* FP32 parameters, layer by layer: weights [27][cin][cout] then bias[cout] */
 int dsg_net_get_params(dsg_net *net, float *host, int64_t count);
 int dsg_net_set_params(dsg_net *net, const float *host, int64_t count);
-/* forward on host arrays: x = W*H*D voxels x 3 channels (x fastest, channels
- * innermost), y = W*H*D outputs */
+/* forward on host arrays: x = W*H*D voxels x DSG_NET_INPUTS channels (x
+ * fastest, channels innermost), y = W*H*D outputs */
 int dsg_net_forward_host(dsg_net *net, const float *x, float *y);
 /* loss = mean (y - t)^2 and its gradient with respect to every parameter */
 int dsg_net_grad_host(dsg_net *net, const float *x, const float *t, float *loss, float *grad);

@@ -1166,16 +1166,33 @@ static void smooth2(ora_state *st) {
       }
 }
 
+/* Number of multigrid levels.  For min(nx,ny,nz) = 2^k+2 this is the count of
+ * memoryaloc (main.f:284-298): halve until the smallest interior extent is 2.
+ * Other sides, which the reference stops on (main.f:296-297), coarsen while
+ * every interior extent is even and the smallest is at least 4, so the
+ * coarsest level may have 3 or 5 interior cells (48, 96 and 160 cells per
+ * side end at 3, 3 and 5).  Returns 0 for a grid below 2 interior cells. */
+int ora_level_count(int nx, int ny, int nz) {
+  int mx = nx - 2, my = ny - 2, mz = nz - 2;
+  if (mx < 2 || my < 2 || mz < 2) return 0;
+  int ng = 1;
+  for (;;) {
+    int m = mx < my ? mx : my;
+    if (mz < m) m = mz;
+    if (m < 4 || (mx & 1) || (my & 1) || (mz & 1) || ng >= 31) break;
+    mx /= 2; my /= 2; mz /= 2;
+    ng++;
+  }
+  return ng;
+}
+
 ora_state *ora_create(const ora_input *in) {
   ora_state *st = (ora_state *)calloc(1, sizeof(ora_state));
   st->in = *in;
   st->nx = in->nx; st->ny = in->ny; st->nz = in->nz;
   /* memoryaloc, main.f:274-322 */
-  int nn = in->nx < in->ny ? in->nx : in->ny;
-  if (in->nz < nn) nn = in->nz;
-  int j = nn - 2, ng = 1;
-  while (j > 2) { j = j / 2; ng = ng + 1; }
-  if ((1 << ng) + 2 != nn || ng >= 31) { free(st); return NULL; }
+  const int ng = ora_level_count(in->nx, in->ny, in->nz);
+  if (ng < 1) { free(st); return NULL; }
   st->s.ng = ng;
   int nnx = in->nx, nny = in->ny, nnz = in->nz;
   for (int l = ng; l >= 1; l--) {

@@ -79,6 +79,7 @@ typedef struct ora_scalars {
 typedef struct ora_state ora_state;
 
 /* ---- whole-solver API --------------------------------------------------- */
+int ora_level_count(int nx, int ny, int nz);
 ora_state *ora_create(const ora_input *in);
 void ora_destroy(ora_state *st);
 int ora_nx(const ora_state *st);

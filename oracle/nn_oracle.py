@@ -12,7 +12,8 @@ offsets -1..1) followed by bias[cout].
 """
 import numpy as np
 
-LAYERS = [(3, 16, True), (16, 32, True), (32, 64, True), (64, 64, True), (64, 32, True), (32, 16, True),
+CIN = 5  # input channels: cc, rhs, defect of p1, p1, p2 (scaled)
+LAYERS = [(CIN, 16, True), (16, 32, True), (32, 64, True), (64, 64, True), (64, 32, True), (32, 16, True),
           (16, 1, False)]
 
 
@@ -98,7 +99,7 @@ def up_back(g):
 
 
 def forward(params, x, bf16=True):
-    """x: (D, H, W, 3).  Returns (y (D,H,W), cache)."""
+    """x: (D, H, W, CIN).  Returns (y (D,H,W), cache)."""
     r = to_bf16 if bf16 else (lambda a: np.asarray(a, np.float64))
     P = [(r(w), np.asarray(b, np.float64)) for w, b in split_params(params)]
     c = {"x0": r(x)}

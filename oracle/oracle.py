@@ -68,6 +68,7 @@ def load():
     lib.ora_create.restype = vp
     lib.ora_create.argtypes = [C.POINTER(OracleInput)]
     lib.ora_destroy.argtypes = [vp]
+    lib.ora_level_count.argtypes = [C.c_int, C.c_int, C.c_int]
     lib.ora_field.restype = _DP
     lib.ora_field.argtypes = [vp, C.c_int]
     lib.ora_level_field.restype = _DP
@@ -135,7 +136,7 @@ class Oracle:
         self.inp = make_input(cfg)
         self.h = self.lib.ora_create(C.byref(self.inp))
         if not self.h:
-            raise ValueError("oracle: min(nx,ny,nz) must be 2**ng+2")
+            raise ValueError("oracle: grid needs at least 2 interior cells per side")
         self.shape = (self.lib.ora_nx(self.h), self.lib.ora_ny(self.h), self.lib.ora_nz(self.h))
 
     def close(self):

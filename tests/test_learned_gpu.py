@@ -27,14 +27,15 @@ def _net(dsg, shape, seed=3):
 
 def _inputs(shape, seed):
     r = np.random.default_rng(seed)
-    x = r.standard_normal(shape + (3,)).astype(np.float32)
+    x = r.standard_normal(shape + (NO.CIN,)).astype(np.float32)
     x[..., 0] = r.uniform(0.0, 1.0, size=shape)
     t = r.standard_normal(shape).astype(np.float32) * 0.1
     return x, t
 
 
 def test_param_count(gpu_lib):
-    assert gpu_lib.load().dsg_net_param_count() == NO.param_count() == 250785
+    assert gpu_lib.load().dsg_net_param_count() == NO.param_count() == 251649
+    assert gpu_lib._lib.NET_INPUTS == NO.CIN
 
 
 @pytest.mark.parametrize("shape", SHAPES)
@@ -111,9 +112,11 @@ def test_learned_mode_converges_and_guards(gpu_lib):
     ora = Oracle(dsg.config.droplet(32, mode=dsg.config.MODE_TOL_FP64, tol=tol).as_dict())
     gpu = dsg.Solver(dsg.config.droplet(32, mode=dsg.config.MODE_LEARNED, tol=tol), init=False)
     net.attach(gpu)
+    hist = [np.zeros(ora.shape), np.zeros(ora.shape)]
     for t in range(1, 6):
         _sync_state(gpu, ora)
-        gpu.set_field("pprev", ora.field("p") if t > 1 else np.zeros(ora.shape))
+        gpu.set_field("pprev", hist[-1])
+        gpu.set_field("pprev2", hist[-2])
         ora.step(t)
         st = gpu.step(t)
         assert st["converged"] == 1 and st["relres"] < tol, st
@@ -121,6 +124,7 @@ def test_learned_mode_converges_and_guards(gpu_lib):
         assert st["relres_init"] == min(st["relres_net"], st["relres_prev"])
         for name in ("p", "u", "v", "w", "cc"):
             assert relerr(gpu.field(name), ora.field(name)) < 1e-7, (t, name)
+        hist.append(ora.field("p").copy())
 
 
 def test_learned_mode_needs_network(gpu_lib):
@@ -129,3 +133,31 @@ def test_learned_mode_needs_network(gpu_lib):
         with pytest.raises(dsg.DsgError) as e:
             s.step(1)
         assert e.value.code == -6
+
+
+def test_trained_network_beats_previous_pressure(gpu_lib):
+    """The committed network (trained on the solver's own 128^3 and 256^3
+    snapshots) starts the solve from a far smaller residual than the
+    previous-step pressure it falls back to, on a droplet it was not trained on."""
+    dsg = gpu_lib
+    from importlib import import_module
+    learned = import_module(dsg.__name__ + ".learned")
+    import os
+    if not os.path.exists(learned.WEIGHTS):
+        pytest.skip("no trained weights")
+    net = learned.Net(128).load()
+    inp = learned.learned_config(dsg.config.droplet(128, steps=1000, impact_speed=2.5, diameter=1.8e-3,
+                                                    mode=dsg.config.MODE_TOL_MIXED, tol=1e-8, npre=4, npost=4,
+                                                    ntop=4, seed=77))
+    ratios, falls = [], []
+    with dsg.Solver(inp) as s:
+        net.attach(s)
+        for t in range(1, 25):
+            st = s.step(t)
+            assert st["converged"] == 1
+            if t > 4:
+                ratios.append(st["relres_net"] / st["relres_prev"])
+                falls.append(st["fallback"])
+        learned.detach(s)
+    assert np.median(ratios) < 0.25, ratios
+    assert np.mean(falls) <= 0.2, falls

@@ -55,3 +55,41 @@ def test_mixed_free_run_volume(gpu_lib):
     vo, vg = ora.liquid_volume(), gpu.liquid_volume()
     assert abs(vg - vo) / vo < 1e-9, (vg, vo)
     assert relerr(gpu.field("p"), ora.field("p")) < 1e-5
+
+
+@pytest.mark.parametrize("n,tail", [(32, 0), (48, 0), (64, 0), (64, 10 ** 6)])
+def test_coarse_tail_is_bit_identical(gpu_lib, n, tail):
+    """The single-block coarse tail computes the same bits as one launch per
+    pass, with fewer launches.  tail=10**6 runs every level below the finest
+    in the tail kernel."""
+    dsg = gpu_lib
+    lib = dsg.load()
+    base = dsg.config.droplet(n, mode=dsg.config.MODE_TOL_MIXED, tol=1e-9, impact_speed=2.0)
+    runs = {}
+    for key, tn in (("pass", -1), ("tail", tail)):
+        with dsg.Solver(base.replace(tail_nodes=tn)) as s:
+            l0 = lib.dsg_launch_count()
+            vc = [s.step(t)["vcycles"] for t in range(1, 6)]
+            s.synchronize()
+            runs[key] = (lib.dsg_launch_count() - l0, vc, {f: s.field(f).copy() for f in ("p", "u", "v", "w", "cc")})
+    assert runs["pass"][1] == runs["tail"][1]
+    for f in ("p", "u", "v", "w", "cc"):
+        assert np.array_equal(runs["pass"][2][f], runs["tail"][2][f]), f
+    assert runs["tail"][0] < runs["pass"][0], (runs["tail"][0], runs["pass"][0])
+
+
+def test_mixed_generalised_grid(gpu_lib):
+    """48^3 interior (coarsest level 3^3): mixed solve against the FP64 oracle."""
+    dsg = gpu_lib
+    from oracle import Oracle
+    tol = 1e-10
+    ora = Oracle(dsg.config.droplet(48, mode=dsg.config.MODE_TOL_FP64, tol=tol).as_dict())
+    gpu = dsg.Solver(dsg.config.droplet(48, mode=dsg.config.MODE_TOL_MIXED, tol=tol), init=False)
+    assert gpu.scalars().ng == 5
+    for t in range(1, 4):
+        _sync_state(gpu, ora)
+        ora.step(t)
+        st = gpu.step(t)
+        assert st["converged"] == 1 and st["relres"] < tol, st
+        for name in ("p", "u", "v", "w", "cc"):
+            assert relerr(gpu.field(name), ora.field(name)) < 1e-7, (t, name)

@@ -61,6 +61,22 @@ def test_noncubic_step(gpu_lib):
         assert relerr(gpu.field(name), ora.field(name)) <= FIELD_TOL, name
 
 
+@pytest.mark.parametrize("n,mode", [(48, 0), (48, 1), (40, 1)])
+def test_generalised_grid_step(gpu_lib, n, mode):
+    """Sides that are not 2^k (the reference stops on them): the multigrid
+    coarsens while the interior stays even, down to 3 (48) or 5 (40) cells."""
+    dsg = gpu_lib
+    inp, ora, gpu = _pair(dsg, n, 4, mode=mode, tol=1e-9, steps=4)
+    assert gpu.scalars().ng == ora.scalars().ng
+    for t in range(1, 5):
+        ora.step(t)
+        st = gpu.step(t)
+        for name in ("cc", "u", "v", "w", "p"):
+            assert relerr(gpu.field(name), ora.field(name)) <= FIELD_TOL, (t, name)
+        if mode == 1:
+            assert st["converged"] == 1 and st["vcycles"] == ora.scalars().last_vcycles
+
+
 def test_isolated_interface_cell(gpu_lib):
     """An isolated partial cell has an all-zero Youngs normal (FL3D would
     divide 0/0); GPU and oracle both advect it as a uniformly filled cell."""
