@@ -81,7 +81,7 @@ class InputData:
     max_vcycles: int = 200
     noise_si: float = 0.0
     noise_seed: int = 0
-    inner_vcycles: int = 2
+    inner_vcycles: int = 0
     use_graphs: int = 1
     tail_nodes: int = 0
     warm_start: int = 0

@@ -486,8 +486,11 @@ int mixed_solve(dsg_ctx *ctx, dsg_mg_stats *s) {
   if ((ctx->nx - 2) & 1)
     return dsg::set_error(ctx, DSG_E_ARG, "mixed mode needs an even number of interior cells along x (%d)",
                           ctx->nx - 2);
-  const int inner = ctx->cfg.inner_vcycles > 0 ? ctx->cfg.inner_vcycles : 1;
-  const int key[6] = {ctx->s.npre, ctx->s.npost, ctx->s.ntop, ctx->cfg.cycles, inner, ctx->prof ? 1 : 0};
+  // inner_vcycles > 0: that many FP32 V-cycles per FP64 defect; 0: as many as
+  // the measured reduction per V-cycle predicts are needed to reach tol
+  const int fixed = ctx->cfg.inner_vcycles;
+  int inner = fixed > 0 ? (fixed < dsg_ctx::kMaxInner ? fixed : dsg_ctx::kMaxInner) : 2;
+  int key[6] = {ctx->s.npre, ctx->s.npost, ctx->s.ntop, ctx->cfg.cycles, 0, ctx->prof ? 1 : 0};
   // start: FP32 coefficient hierarchy, FP32 FMG guess, first FP64 defect
   auto first = [&]() -> int {
     int q = coef_hierarchy32(ctx);
@@ -574,6 +577,7 @@ int mixed_solve(dsg_ctx *ctx, dsg_mg_stats *s) {
     rc = defect_host(ctx, &r);
     if (rc) return rc;
   } else {
+    key[4] = 0;  // the start does not depend on the inner count
     rc = run(ctx->g_first, first);
     if (rc) return rc;
     rc = defect_read(ctx, &r);
@@ -582,12 +586,24 @@ int mixed_solve(dsg_ctx *ctx, dsg_mg_stats *s) {
   s->relres_init = r;
   int n = 0;
   while (r >= ctx->cfg.tol && n < ctx->cfg.max_vcycles) {
-    rc = run(ctx->g_iter, iterate);
+    if (fixed <= 0) {
+      const double need = log(ctx->cfg.tol / r) / log(ctx->rho_est);
+      inner = (int)ceil(need + 0.1);
+      inner = inner < 1 ? 1 : (inner > dsg_ctx::kMaxInner ? dsg_ctx::kMaxInner : inner);
+    }
+    if (inner > ctx->cfg.max_vcycles - n) inner = ctx->cfg.max_vcycles - n;
+    key[4] = inner;
+    rc = run(ctx->g_iter[inner], iterate);
     if (rc) return rc;
     s->fine_sweeps += inner * (ctx->s.npre + ctx->s.npost);
     n += inner;
+    const double r_old = r;
     rc = defect_read(ctx, &r);
     if (rc) return rc;
+    if (r < r_old && r > 0.0) {
+      const double obs = pow(r / r_old, 1.0 / inner);
+      ctx->rho_est = obs < 0.05 ? 0.05 : (obs > 0.9 ? 0.9 : obs);
+    }
   }
   DSG_CK(ctx, dsg::bc_scalar(ctx->lv[ng][1], ctx->fine(), st));
   s->vcycles = n;
@@ -789,7 +805,7 @@ void dsg_destroy(dsg_ctx *ctx) {
   for (cudaEvent_t e : ctx->prof_ev) cudaEventDestroy(e);
   for (cudaEvent_t e : ctx->phase_ev) cudaEventDestroy(e);
   graph_release(ctx->g_first);
-  graph_release(ctx->g_iter);
+  for (GraphRec &g : ctx->g_iter) graph_release(g);
   if (ctx->arena) cudaFree(ctx->arena);
   if (ctx->red_host) cudaFreeHost(ctx->red_host);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);

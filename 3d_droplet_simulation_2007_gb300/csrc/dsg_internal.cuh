@@ -226,7 +226,10 @@ struct dsg_ctx {
   double prof_relax_bytes = 0.0;
   int prof_relax_bits = 64;
   double prof_graph_relax_ms = 0.0;   // relax time read back from graph replays
-  GraphRec g_first, g_iter;           // FP32 FMG start + first defect; one outer iteration
+  static constexpr int kMaxInner = 8;  // FP32 V-cycles of one outer iteration, at most
+  GraphRec g_first;                    // FP32 FMG start + first defect
+  GraphRec g_iter[kMaxInner + 1];      // one outer iteration of k V-cycles + defect, per k
+  double rho_est = 0.3;                // measured residual reduction per FP32 V-cycle
   GraphRec *cap = nullptr;            // graph under capture
   dsg_net *net = nullptr;             // learned initial guess (DSG_MODE_LEARNED)
   int net_record = 0;                 // store a training pair after every solve

@@ -40,7 +40,8 @@ def parse():
     ap.add_argument("--n", type=int, default=256, help="interior cells per side")
     ap.add_argument("--mode", default="best", help="best|tol_fp64|tol_mixed|learned|ref_exact")
     ap.add_argument("--tol", type=float, default=1e-8)
-    ap.add_argument("--inner", type=int, default=2, help="FP32 V-cycles per FP64 defect (mixed modes)")
+    ap.add_argument("--inner", type=int, default=0,
+                    help="FP32 V-cycles per FP64 defect (mixed modes; 0: adaptive)")
     ap.add_argument("--no-graphs", action="store_true", help="launch the mixed solve without CUDA graphs")
     ap.add_argument("--tail-nodes", type=int, default=0,
                     help="largest FP32 level (nodes) of the single-block coarse tail (0: default, -1: off)")
@@ -58,7 +59,7 @@ def dist_env():
     return ws, rank, local
 
 
-def workload(dsg, n, mode, tol, inner=2, graphs=True, tail_nodes=0):
+def workload(dsg, n, mode, tol, inner=0, graphs=True, tail_nodes=0):
     cfg = dsg.config
     return cfg.droplet(n, steps=1000, impact_speed=3.0, noise_si=1e-4, mode=mode, tol=tol,
                        npre=4, npost=4, ntop=4).replace(inner_vcycles=inner, use_graphs=1 if graphs else 0,

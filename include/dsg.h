@@ -76,7 +76,8 @@ typedef struct dsg_config {
   int max_vcycles;     /* V-cycle / defect-correction cap of the tol modes */
   double noise_si;     /* half-width of the seeded uniform velocity noise [m/s] */
   uint64_t noise_seed; /* seed of the counter-based noise */
-  int inner_vcycles;   /* FP32 V-cycles per FP64 defect evaluation in the mixed modes (<= 0: 1) */
+  int inner_vcycles;   /* FP32 V-cycles per FP64 defect evaluation in the mixed modes (<= 0: as many
+                          as the measured reduction per V-cycle predicts to reach tol, at most 8) */
   int use_graphs;      /* capture the mixed-mode iterations in CUDA graphs (1) or launch directly (0) */
   int tail_nodes;      /* mixed modes: FP32 levels of at most this many nodes run in one single-block
                           launch per V-cycle (0: 18^3 = 5832; < 0: one launch per pass on every level) */
