@@ -11,4 +11,5 @@ from . import config  # noqa: F401
 from .config import InputData, parse_inputdata, format_inputdata  # noqa: F401
 from ._lib import DsgError, load  # noqa: F401
 from .solver import Solver  # noqa: F401
+from .ensemble import Ensemble, study_configs  # noqa: F401
 from . import kernels  # noqa: F401

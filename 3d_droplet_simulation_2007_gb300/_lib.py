@@ -141,6 +141,18 @@ SIGNATURES = [
     ("dsg_net_grad_host", _i, [_vp, _vp, _vp, C.POINTER(C.c_float), _vp]),
     ("dsg_net_train_step", _i, [_vp, C.c_float, C.POINTER(C.c_float)]),
     ("dsg_attach_net", _i, [_vp, _vp, _i]),
+    ("dsg_ensemble_create", _i, [C.POINTER(DsgConfig), _i, _i, _PP]),
+    ("dsg_ensemble_destroy", None, [_vp]),
+    ("dsg_ensemble_size", _i, [_vp]),
+    ("dsg_ensemble_workers", _i, [_vp]),
+    ("dsg_ensemble_member", _vp, [_vp, _i]),
+    ("dsg_ensemble_last_error", C.c_char_p, [_vp]),
+    ("dsg_ensemble_set_workers", _i, [_vp, _i]),
+    ("dsg_ensemble_step", _i, [_vp, _i, C.POINTER(DsgMgStats)]),
+    ("dsg_ensemble_last_ms", _d, [_vp]),
+    ("dsg_ensemble_member_ms", _i, [_vp, _DPP]),
+    ("dsg_ensemble_autotune", _i, [_vp, _i, _i, _IP, _IP]),
+    ("dsg_ensemble_plan", _i, [_DPP, _i, _i, _IP]),
 ]
 
 _LIB = None

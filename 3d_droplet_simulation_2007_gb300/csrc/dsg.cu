@@ -14,11 +14,14 @@
 
 #include "dsg_internal.cuh"
 
-static std::string g_last_error;
+// Message of the last failure without a context, per host thread (ensemble
+// workers report concurrently).
+static thread_local std::string g_last_error;
 
 namespace dsg {
 
 std::atomic<long long> g_launches{0};
+thread_local long long t_launches = 0;
 
 int set_error(dsg_ctx *ctx, int code, const char *fmt, ...) {
   char buf[512];
@@ -374,11 +377,12 @@ int graph_capture(dsg_ctx *ctx, GraphRec &g, const int key[6], F body) {
     return 1;
   }
   ctx->cap = &g;
-  const long long launches0 = dsg::g_launches.load();
+  const long long launches0 = dsg::t_launches;
   int rc = body();
   // launches made while capturing became graph nodes: count them per replay
-  g.kernels = dsg::g_launches.load() - launches0;
+  g.kernels = dsg::t_launches - launches0;
   dsg::g_launches.fetch_sub(g.kernels);
+  dsg::t_launches -= g.kernels;
   ctx->cap = nullptr;
   cudaGraph_t graph = nullptr;
   cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
@@ -782,6 +786,7 @@ int dsg_create(const dsg_config *cfg, dsg_ctx **out) {
     return rc;
   }
   ctx->stream = ctx->own_stream;
+  cudaGetDevice(&ctx->device);
   ctx->s.npre = cfg->npre;
   ctx->s.npost = cfg->npost;
   ctx->s.ntop = cfg->ntop;

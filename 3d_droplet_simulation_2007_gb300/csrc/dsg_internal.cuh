@@ -15,8 +15,15 @@ namespace dsg {
 
 // Every kernel launch of the library goes through DSG_COUNT so that the
 // number of launches in a timed region can be reported.
+// The per-thread count lets a graph capture count its own kernel nodes while
+// other host threads (ensemble workers) launch concurrently.
 extern std::atomic<long long> g_launches;
-#define DSG_COUNT dsg::g_launches.fetch_add(1, std::memory_order_relaxed),
+extern thread_local long long t_launches;
+inline void count_launch() {
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  t_launches++;
+}
+#define DSG_COUNT dsg::count_launch(),
 
 // Column-major, 1-based (i,j,k) -> linear offset of an (nx,ny,nz) array.
 struct Dims {
@@ -137,7 +144,7 @@ cudaError_t acfromac32(float *a, float *b, float *c, float *ei, const float *a2,
                        Dims dc, cudaStream_t st);
 cudaError_t acfromac64to32(float *a, float *b, float *c, float *ei, const double *a2, const double *b2,
                            const double *c2, Dims dc, cudaStream_t st);
-// coarse tail: levels top..1 of one V-cycle in one thread block (per instance)
+// coarse tail: levels top..1 of one V-cycle in one thread block
 constexpr int kTailThreads = 1024;
 constexpr int kTailMaxLevels = 12;
 struct TailLevel {
@@ -152,7 +159,6 @@ struct TailArgs {
   float omega;
 };
 cudaError_t vtail32(const TailArgs &args, cudaStream_t st);
-cudaError_t vtail32_batch(const TailArgs *args_dev, int n, cudaStream_t st);
 // finest level in colour-split storage ({even, odd} arrays of (nx-2)/2 x (ny-2) x (nz-2))
 cudaError_t relax32_split_n(int n, float *const u[2], float *const rhs[2], const float *cc, Dims d, float h2,
                             float omega, float r1, float r2, cudaStream_t st);
@@ -201,6 +207,7 @@ struct dsg_ctx {
   dsg_config cfg;
   dsg_scalars s;
   int nx, ny, nz, ng;
+  int device = 0;             // CUDA device the context was created on
   int tail_top = 0;           // FP32 levels 1..tail_top run in the single-block tail kernel (0: none)
   int lnx[32], lny[32], lnz[32];
   double *lv[32][8];          // [level][CC,P,RES,RHS,A,B,C,EI], level 1..ng

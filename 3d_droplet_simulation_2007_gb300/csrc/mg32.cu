@@ -278,8 +278,7 @@ __global__ void k_addint32(float *__restrict__ uf, const float *__restrict__ uc,
 // grid and back (pre-sweeps, residual restriction, NTOP coarsest sweeps,
 // prolongation, post-sweeps: mglin's recursion, main.f:3703-3759) inside one
 // block, with a block barrier between passes in place of a launch boundary.
-// The level arrays stay in L1/L2.  One block per instance: the ensemble
-// launches one block per member.
+// The level arrays stay in L1/L2.
 __device__ void tail_relax(const TailLevel &L, int n, float omega) {
   const Dims d = L.d;
   const int hx = (d.nx - 1) / 2;  // cells of one colour per row, rounded up
@@ -324,10 +323,6 @@ __device__ void tail_body(const TailArgs &A) {
 }
 
 __global__ void __launch_bounds__(kTailThreads, 1) k_vtail32(TailArgs A) { tail_body(A); }
-
-__global__ void __launch_bounds__(kTailThreads, 1) k_vtail32_batch(const TailArgs *__restrict__ all, int n) {
-  if ((int)blockIdx.x < n) tail_body(all[blockIdx.x]);
-}
 
 // Interior injection (interp, main.f:3866-3900) for the FMG start.
 __global__ void k_interp32(float *__restrict__ uf, const float *__restrict__ uc, Dims df, Dims dc) {
@@ -568,11 +563,6 @@ cudaError_t vtail32(const TailArgs &args, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-cudaError_t vtail32_batch(const TailArgs *args_dev, int n, cudaStream_t st) {
-  if (n <= 0) return cudaSuccess;
-  DSG_COUNT k_vtail32_batch<<<n, kTailThreads, 0, st>>>(args_dev, n);
-  return cudaGetLastError();
-}
 
 cudaError_t addint32(float *uf, const float *uc, Dims df, cudaStream_t st) {
   const Dims dc{df.nx / 2 + 1, df.ny / 2 + 1, df.nz / 2 + 1};

@@ -1,0 +1,118 @@
+"""Many independent droplet simulations stepped together on one GPU.
+
+:class:`Ensemble` wraps ``dsg_ensemble`` (include/dsg.h): n contexts, each a
+full simulation with its fields resident in HBM, stepped by a pool of host
+threads on their own CUDA streams so that the members' kernels overlap on the
+GPU.  The autotuner measures each member's step time and picks the number of
+worker threads by timing real steps.  The reference runs one case per
+process; this is the batched study of droplet sizes and Weber numbers.
+"""
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _lib
+from .config import InputData, MODE_TOL_MIXED, droplet
+from .solver import Solver, to_config
+
+
+def study_configs(count=64, sides=(48, 64, 96, 128, 160), we_range=(50.0, 800.0), diameter=2e-3, seed=1000,
+                  mode=MODE_TOL_MIXED, tol=1e-8, steps=1000, **kw):
+    """The droplet study: member i has seed ``seed + i``, a grid side drawn
+    from ``sides`` and a Weber number rho1 v^2 D / sigma log-uniform in
+    ``we_range`` (impact speed v = sqrt(We sigma / (rho1 D)))."""
+    out = []
+    for i in range(count):
+        rng = np.random.default_rng(seed + i)
+        n = int(sides[int(rng.integers(len(sides)))])
+        we = math.exp(rng.uniform(math.log(we_range[0]), math.log(we_range[1])))
+        speed = math.sqrt(we * 0.072 / (1000.0 * diameter))
+        out.append(droplet(n, steps=steps, impact_speed=speed, diameter=diameter, noise_si=1e-4, mode=mode,
+                           tol=tol, npre=4, npost=4, ntop=4, seed=seed + i, **kw))
+    return out
+
+
+class Ensemble:
+    """n simulations stepped together; ``member(i)`` is a Solver view."""
+
+    def __init__(self, inputs, workers=0):
+        self.lib = _lib.load()
+        self.inputs = [x if isinstance(x, InputData) else InputData(**x) for x in inputs]
+        n = len(self.inputs)
+        cfgs = (_lib.DsgConfig * n)(*[to_config(x) for x in self.inputs])
+        h = C.c_void_p()
+        _lib.check(self.lib.dsg_ensemble_create(cfgs, n, workers, C.byref(h)))
+        self.h = h
+        self.n = n
+        self.t = 0
+        self._members = [Solver(self.inputs[i], ctx=self.lib.dsg_ensemble_member(h, i)) for i in range(n)]
+
+    def close(self):
+        if getattr(self, "h", None):
+            for m in self._members:
+                m.ctx = None
+            self.lib.dsg_ensemble_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _ck(self, rc):
+        if rc != _lib.DSG_OK:
+            msg = self.lib.dsg_ensemble_last_error(self.h) or self.lib.dsg_last_error(None)
+            raise _lib.DsgError(rc, msg.decode() if msg else "")
+        return rc
+
+    def member(self, i):
+        return self._members[i]
+
+    @property
+    def workers(self):
+        return self.lib.dsg_ensemble_workers(self.h)
+
+    def set_workers(self, w):
+        self._ck(self.lib.dsg_ensemble_set_workers(self.h, w))
+
+    def step(self, t=None):
+        """One time step of every member; returns their solve statistics."""
+        t = self.t + 1 if t is None else t
+        st = (_lib.DsgMgStats * self.n)()
+        self._ck(self.lib.dsg_ensemble_step(self.h, t, st))
+        self.t = t
+        return [s.as_dict() for s in st]
+
+    @property
+    def last_ms(self):
+        return self.lib.dsg_ensemble_last_ms(self.h)
+
+    def member_ms(self):
+        out = np.zeros(self.n)
+        self._ck(self.lib.dsg_ensemble_member_ms(self.h, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
+
+    def autotune(self, steps_per_trial=2):
+        """Run real steps to measure member costs and pick the worker count."""
+        tn, bw = C.c_int(), C.c_int()
+        self._ck(self.lib.dsg_ensemble_autotune(self.h, self.t + 1, steps_per_trial, C.byref(tn), C.byref(bw)))
+        self.t = tn.value - 1
+        return bw.value
+
+
+def plan(costs, workers):
+    """Worker of each member under the longest-processing-time-first plan."""
+    lib = _lib.load()
+    c = np.ascontiguousarray(costs, dtype=np.float64)
+    out = np.zeros(len(c), dtype=np.int32)
+    _lib.check(lib.dsg_ensemble_plan(c.ctypes.data_as(C.POINTER(C.c_double)), len(c), workers,
+                                     out.ctypes.data_as(C.POINTER(C.c_int))))
+    return out

@@ -31,23 +31,28 @@ def to_config(inp):
 class Solver:
     """One droplet simulation resident on the current CUDA device."""
 
-    def __init__(self, inp, init=True):
+    def __init__(self, inp, init=True, ctx=None):
+        """ctx: wrap an existing context (an ensemble member) without owning it."""
         self.lib = _lib.load()
         self.inp = inp if isinstance(inp, InputData) else InputData(**inp)
         self._cfg = to_config(self.inp)
-        h = C.c_void_p()
-        _lib.check(self.lib.dsg_create(C.byref(self._cfg), C.byref(h)))
-        self.ctx = h
+        self._owned = ctx is None
+        if ctx is None:
+            h = C.c_void_p()
+            _lib.check(self.lib.dsg_create(C.byref(self._cfg), C.byref(h)))
+            ctx = h
+        self.ctx = ctx if isinstance(ctx, C.c_void_p) else C.c_void_p(ctx)
         self.shape = (self.inp.nx, self.inp.ny, self.inp.nz)
         self.t = 0
         self.last_stats = None
-        if init:
+        if init and self._owned:
             self.init_drop()
 
     # ---- lifecycle -------------------------------------------------------
     def close(self):
         if getattr(self, "ctx", None):
-            self.lib.dsg_destroy(self.ctx)
+            if self._owned:
+                self.lib.dsg_destroy(self.ctx)
             self.ctx = None
 
     def __del__(self):

@@ -117,7 +117,7 @@ typedef struct dsg_ctx dsg_ctx;
  * arena; requires min(nx,ny,nz) = 2^ng+2 (memoryaloc main.f:295-298). */
 int dsg_create(const dsg_config *cfg, dsg_ctx **out);
 void dsg_destroy(dsg_ctx *ctx);
-const char *dsg_last_error(const dsg_ctx *ctx); /* ctx may be NULL: last global error */
+const char *dsg_last_error(const dsg_ctx *ctx); /* ctx may be NULL: last error of this host thread */
 int dsg_set_stream(dsg_ctx *ctx, void *cuda_stream); /* NULL = the context's own stream */
 int dsg_synchronize(dsg_ctx *ctx);
 /* Device bytes held by the context arena. */
@@ -232,6 +232,39 @@ int dsg_bc_resid(double *s, int nx, int ny, int nz, void *stream);
 int dsg_bc_out(double *s, int nx, int ny, int nz, void *stream);
 /* filterc27 main.f:5473-5511 */
 int dsg_filterc27(const double *cc, double *cf, int nx, int ny, int nz, void *stream);
+
+/* ---- ensemble -------------------------------------------------------------
+ * No counterpart in the reference (main.f runs one case per process).  An
+ * ensemble holds n independent contexts (cfgs[i], each initialised as
+ * dsg_init_drop does) on the current device and steps them together: one
+ * dsg_ensemble_step is one time step t of every member.  A pool of `workers`
+ * host threads (<= 0: one per hardware thread, at most n) steps the members on
+ * their own streams, members assigned to workers by longest-processing-time
+ * first on a cost per member.  stats (n entries, may be NULL) receives each
+ * member's solve statistics; on failure the first failing member's code is
+ * returned and dsg_ensemble_last_error names it.  Members are ordinary
+ * contexts for dsg_download/dsg_upload/dsg_get_scalars between steps; they
+ * must not be stepped or destroyed individually. */
+typedef struct dsg_ensemble dsg_ensemble;
+int dsg_ensemble_create(const dsg_config *cfgs, int n, int workers, dsg_ensemble **out);
+void dsg_ensemble_destroy(dsg_ensemble *e);
+int dsg_ensemble_size(const dsg_ensemble *e);
+int dsg_ensemble_workers(const dsg_ensemble *e);
+dsg_ctx *dsg_ensemble_member(dsg_ensemble *e, int i);
+const char *dsg_ensemble_last_error(const dsg_ensemble *e);
+int dsg_ensemble_set_workers(dsg_ensemble *e, int workers);
+int dsg_ensemble_step(dsg_ensemble *e, int t, dsg_mg_stats *stats);
+/* host wall time of the last ensemble step and of each member's step (ms) */
+double dsg_ensemble_last_ms(const dsg_ensemble *e);
+int dsg_ensemble_member_ms(const dsg_ensemble *e, double *out);
+/* Autotuner: runs real time steps t0, t0+1, ... (the simulation advances):
+ * one warm-up step, one step on a single worker that measures every member's
+ * step time (the costs of the plan from then on), then steps_per_trial steps
+ * per worker count 1, 2, 4, ... up to twice the hardware threads (at most n);
+ * keeps the fastest count.  *t_next = the next step index. */
+int dsg_ensemble_autotune(dsg_ensemble *e, int t0, int steps_per_trial, int *t_next, int *best_workers);
+/* The plan alone: assign[i] = worker of member i for the given costs. */
+int dsg_ensemble_plan(const double *cost, int n, int workers, int *assign);
 
 /* ---- allocation-free pressure solve -------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
