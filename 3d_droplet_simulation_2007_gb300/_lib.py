@@ -22,7 +22,8 @@ ERROR_NAMES = {0: "DSG_OK", -1: "DSG_E_ARG", -2: "DSG_E_CUDA", -3: "DSG_E_NOMEM"
                -4: "DSG_E_NOT_CONVERGED", -5: "DSG_E_NONFINITE", -6: "DSG_E_STATE"}
 
 FIELDS = ["cc", "p", "res", "rhs", "a", "b", "c", "ei", "u", "v", "w",
-          "s11", "s22", "s33", "s12", "s13", "s23", "rhon", "mun", "pprev", "pprev2"]
+          "s11", "s22", "s33", "s12", "s13", "s23", "rhon", "mun", "pprev", "pprev2",
+          "ktur", "eps", "mut"]
 FIELD_ID = {n: i for i, n in enumerate(FIELDS)}
 
 
@@ -108,6 +109,7 @@ SIGNATURES = [
     ("dsg_set_scalars", _i, [_vp, C.POINTER(DsgScalars)]),
     ("dsg_init_drop", _i, [_vp]),
     ("dsg_vofmethod", _i, [_vp]),
+    ("dsg_kepsmodel", _i, [_vp]),
     ("dsg_checktime", _i, [_vp]),
     ("dsg_csf", _i, [_vp]),
     ("dsg_solvelpres", _i, [_vp, _i, C.POINTER(DsgMgStats)]),

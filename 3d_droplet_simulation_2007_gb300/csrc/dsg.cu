@@ -718,6 +718,8 @@ int dsg_create(const dsg_config *cfg, dsg_ctx **out) {
     return dsg::set_error(nullptr, DSG_E_ARG, "grid %dx%dx%d too small", cfg->nx, cfg->ny, cfg->nz);
   if (cfg->mode < 0 || cfg->mode > DSG_MODE_LEARNED)
     return dsg::set_error(nullptr, DSG_E_ARG, "unknown mode %d", cfg->mode);
+  if (cfg->iturb != 0 && cfg->iturb != 3)
+    return dsg::set_error(nullptr, DSG_E_ARG, "iturb = %d is not available (0: laminar, 3: k-epsilon)", cfg->iturb);
   // memoryaloc, main.f:284-298 (generalised to sides that are not 2^k+2)
   const int ng = dsg::level_count(cfg->nx, cfg->ny, cfg->nz);
   if (ng < 1) return dsg::set_error(nullptr, DSG_E_ARG, "grid %dx%dx%d too small", cfg->nx, cfg->ny, cfg->nz);
@@ -895,6 +897,18 @@ int dsg_init_drop(dsg_ctx *ctx) {
                         ctx->stream));
   DSG_CK(ctx, dsg::calcrho(ctx->f[DSG_F_RHON], ctx->f[DSG_F_MUN], ctx->f[DSG_F_CC], d, s.rho1, s.rho2, s.mu1,
                            s.mu2, ctx->stream));
+  if (ctx->cfg.iturb == 3) {
+    // ktur = 0.00015 v^2 per phase (inijet, main.f:536-549), v the phase speed
+    const double v1 = sqrt(s.xvel1 * s.xvel1 + s.yvel1 * s.yvel1 + s.zvel1 * s.zvel1);
+    const double v2 = sqrt(s.xvel2 * s.xvel2 + s.yvel2 * s.yvel2 + s.zvel2 * s.zvel2);
+    const double dv = sqrt((s.xvel1 - s.xvel2) * (s.xvel1 - s.xvel2) + (s.yvel1 - s.yvel2) * (s.yvel1 - s.yvel2) +
+                           (s.zvel1 - s.zvel2) * (s.zvel1 - s.zvel2));
+    const double k1 = (double)0.00015f * v1 * v1;
+    const double g = v2 + dv * (double)0.01f;
+    const double k2 = (double)0.00015f * (g * g);
+    DSG_CK(ctx, dsg::keps_seed(ctx->f[DSG_F_KTUR], ctx->f[DSG_F_EPS], ctx->f[DSG_F_MUT], ctx->f[DSG_F_CC],
+                               ctx->f[DSG_F_RHON], ctx->f[DSG_F_MUN], d, k1, k2, ctx->stream));
+  }
   DSG_CK(ctx, cudaStreamSynchronize(ctx->stream));
   return DSG_OK;
 }
@@ -914,8 +928,23 @@ int dsg_vofmethod(dsg_ctx *ctx) {
   for (int q = 0; q < 3; q++)
     DSG_CK(ctx, dsg::swp(vel[order[q]], cc, s1, s2, s3, order[q], d, s.tauh, ctx->stream));
   DSG_CK(ctx, dsg::bc_c(cc, d, ctx->stream));
+  // turbulent diffusion of the volume fraction (main.f:820)
+  if (ctx->cfg.iturb != 0)
+    DSG_CK(ctx, dsg::fturbdif(cc, ctx->f[DSG_F_MUT], ctx->f[DSG_F_RHON], d, s.tauh2, ctx->stream));
   DSG_CK(ctx, dsg::calcrho(ctx->f[DSG_F_RHON], ctx->f[DSG_F_MUN], cc, d, s.rho1, s.rho2, s.mu1, s.mu2,
                            ctx->stream));
+  return DSG_OK;
+}
+
+// kepsmodel (main.f:39-40): the new values go through the pressure and
+// residual arrays, the scratch the reference passes.
+int dsg_kepsmodel(dsg_ctx *ctx) {
+  if (!ctx) return DSG_E_ARG;
+  if (ctx->cfg.iturb != 3) return DSG_OK;
+  const dsg_scalars &s = ctx->s;
+  DSG_CK(ctx, dsg::kepsmodel(ctx->f[DSG_F_KTUR], ctx->f[DSG_F_EPS], ctx->f[DSG_F_MUT], ctx->f[DSG_F_P],
+                             ctx->f[DSG_F_RES], ctx->f[DSG_F_MUN], ctx->f[DSG_F_RHON], ctx->f[DSG_F_U],
+                             ctx->f[DSG_F_V], ctx->f[DSG_F_W], ctx->fine(), s.h, s.tau, ctx->stream));
   return DSG_OK;
 }
 
@@ -1028,6 +1057,8 @@ int dsg_step(dsg_ctx *ctx, int t, dsg_mg_stats *stats) {
   if (!ctx) return DSG_E_ARG;
   DSG_CK(ctx, phase_mark(ctx, 0));
   int rc = dsg_vofmethod(ctx);
+  if (rc) return rc;
+  rc = dsg_kepsmodel(ctx);
   if (rc) return rc;
   DSG_CK(ctx, phase_mark(ctx, 1));
   rc = dsg_checktime(ctx);

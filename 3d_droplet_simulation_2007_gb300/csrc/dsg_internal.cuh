@@ -132,6 +132,13 @@ cudaError_t divergence(double *out, const double *u, const double *v, const doub
                        cudaStream_t st);
 cudaError_t project(double *u, double *v, double *w, const double *p, const double *a, const double *b,
                     const double *c, Dims d, cudaStream_t st);
+// turb.cu (k-epsilon, iturb = 3)
+cudaError_t keps_seed(double *ktur, double *eps, double *mut, const double *cc, const double *rhon,
+                      const double *mun, Dims d, double k1, double k2, cudaStream_t st);
+cudaError_t kepsmodel(double *ktur, double *eps, double *mut, double *kn, double *en, const double *mun,
+                      const double *rhon, const double *u, const double *v, const double *w, Dims d, double h,
+                      double tau, cudaStream_t st);
+cudaError_t fturbdif(double *cc, const double *mut, const double *rhon, Dims d, int tauh2, cudaStream_t st);
 // mg32.cu (mixed precision)
 cudaError_t relax32_n(int n, float *u, float h2, const float *rhs, const float *a, const float *b, const float *c,
                       const float *ei, Dims d, float omega, cudaStream_t st);

@@ -54,7 +54,10 @@ enum {
   DSG_F_RHON = 17, DSG_F_MUN = 18,
   DSG_F_PPREV = 19, /* previous-step pressure (build addition: the reference keeps none) */
   DSG_F_PPREV2 = 20, /* pressure of two steps back (kept while a network is attached) */
-  DSG_NFIELDS = 21
+  DSG_F_KTUR = 21,  /* k-epsilon state (iturb = 3), COMMON /turbulence/ input.h:36-42 */
+  DSG_F_EPS = 22,
+  DSG_F_MUT = 23,
+  DSG_NFIELDS = 24
 };
 
 /* The 38 positional values of inputdata.in (main.f:188-234) in file order,
@@ -140,6 +143,7 @@ int dsg_init_drop(dsg_ctx *ctx);
 /* VOFmethod(t) main.f:795-824 */
 int dsg_vofmethod(dsg_ctx *ctx);
 /* checktime(t) main.f:2152-2171 (one device max-reduction, one host read) */
+int dsg_kepsmodel(dsg_ctx *ctx); /* kepsmodel main.f:1888-2025 (iturb = 3; no-op for iturb = 0) */
 int dsg_checktime(dsg_ctx *ctx);
 /* csf(ccc,w11,w22,w33) main.f:2363-2481 */
 int dsg_csf(dsg_ctx *ctx);

@@ -34,6 +34,7 @@ struct ora_state {
   int lnx[32], lny[32], lnz[32];
   double *lv[32][8]; /* [level][CC,P,RES,RHS,A,B,C,EI] */
   double *u, *v, *w, *s11, *s22, *s33, *s12, *s13, *s23, *rhon, *mun;
+  double *ktur, *eps, *mut; /* /turbulence/ (input.h:36-42); cmu is 0.09 everywhere for iturb = 3 */
 };
 
 static double *zalloc(size_t n) { return (double *)calloc(n, sizeof(double)); }
@@ -779,6 +780,145 @@ static void calcrho(ora_state *st) {
 }
 
 /* VOFmethod, main.f:795-824 (laminar: fturbdif is not called) */
+/* ======================================================================= */
+/* k-epsilon turbulence (iturb = 3)                                          */
+/* ======================================================================= */
+
+/* Initial ktur, eps, mut of the drop (deviation: the reference never sets
+ * them for the drop, so kepsmodel divides 0/0 on its first step).  The
+ * values follow inijet's jet formulas (main.f:536-549): ktur = 0.00015 v^2
+ * with v the liquid speed in the liquid and (v2 + 0.01 |v1 - v2|) in the gas,
+ * eps = 0.09 rho ktur^2 / mu, mut = 0.09 rho ktur^2 / eps, with v the speed
+ * of the phase's velocity vector (inijet uses the x component, which is 0 for
+ * a drop falling along y) and the two phases mixed by the volume fraction.
+ * REAL literals as in the source (0.00015, 0.01, 0.09 single precision). */
+static void keps_seed(ora_state *st) {
+  const int nx = st->nx, ny = st->ny, nz = st->nz;
+  const ora_scalars *s = &st->s;
+  const double *cc = st->lv[s->ng][LCC];
+  const double v1 = sqrt(s->xvel1 * s->xvel1 + s->yvel1 * s->yvel1 + s->zvel1 * s->zvel1);
+  const double v2 = sqrt(s->xvel2 * s->xvel2 + s->yvel2 * s->yvel2 + s->zvel2 * s->zvel2);
+  const double dv = sqrt((s->xvel1 - s->xvel2) * (s->xvel1 - s->xvel2) + (s->yvel1 - s->yvel2) * (s->yvel1 - s->yvel2) +
+                         (s->zvel1 - s->zvel2) * (s->zvel1 - s->zvel2));
+  const double k1 = (double)0.00015f * v1 * v1;
+  const double g = v2 + dv * (double)0.01f;
+  const double k2 = (double)0.00015f * (g * g);
+  for (int k = 1; k <= nz; k++)
+    for (int j = 1; j <= ny; j++)
+      for (int i = 1; i <= nx; i++) {
+        const size_t q = IX(i, j, k);
+        const double kt = cc[q] * k1 + (1.0 - cc[q]) * k2;
+        st->ktur[q] = kt;
+        st->eps[q] = kt > 0.0 ? (double)0.09f * st->rhon[q] * kt * kt / st->mun[q] : 0.0;
+        st->mut[q] = kt > 0.0 ? (double)0.09f * st->rhon[q] * kt * kt / st->eps[q] : 0.0;
+      }
+}
+
+/* fturbdif, main.f:1239-1267: turbulent diffusion of the volume fraction in
+ * y and z, updated in place in the loop order i, j, k (cells (i,j-1,k) and
+ * (i,j,k-1) are already new when (i,j,k) is computed), then bc_c.  The
+ * FINDMIN/FMODMAX warning print has no effect on the state. */
+static void fturbdif(ora_state *st, double *cc) {
+  const int nx = st->nx, ny = st->ny, nz = st->nz;
+  const double *mut = st->mut, *rh = st->rhon;
+  const double ftr = 1.0 * (double)st->s.tauh2 * 1.0 / 2.0;
+  const size_t sy = (size_t)nx, sz = (size_t)nx * ny;
+  for (int i = 2; i <= nx - 1; i++)
+    for (int j = 2; j <= ny - 1; j++)
+      for (int k = 2; k <= nz - 1; k++) {
+        const size_t q = IX(i, j, k);
+        const double m0 = mut[q] / rh[q];
+        cc[q] = cc[q] + ftr * ((m0 + mut[q + sy] / rh[q + sy]) * (cc[q + sy] - cc[q]) -
+                               (m0 + mut[q - sy] / rh[q - sy]) * (cc[q] - cc[q - sy]) +
+                               (m0 + mut[q + sz] / rh[q + sz]) * (cc[q + sz] - cc[q]) -
+                               (m0 + mut[q - sz] / rh[q - sz]) * (cc[q] - cc[q - sz]));
+      }
+  bc_c(cc, nx, ny, nz);
+}
+
+/* kepsmodel, main.f:1888-2025 with iturb = 3: explicit update of ktur and eps
+ * (upwind convection, variable-coefficient diffusion, production from the
+ * strain of the staggered velocity), new values into the scratch arrays the
+ * reference passes (kturnew = the pressure array, epsnew = the residual
+ * array, main.f:39-40), then ktur, eps, mut = cmu rho k^2/eps on the
+ * interior and bc_scalar on all three. */
+static void kepsmodel(ora_state *st) {
+  const int nx = st->nx, ny = st->ny, nz = st->nz, ng = st->s.ng;
+  const double *u = st->u, *v = st->v, *w = st->w, *mun = st->mun, *rhon = st->rhon, *mut = st->mut;
+  double *ktur = st->ktur, *eps = st->eps;
+  double *kn = LV(ng, LU), *en = LV(ng, LRES);
+  const double sigk = 1.0, sige = 1.3, c1 = 1.44, c2 = 1.92, cmu = 0.09;
+  const double h = st->s.h, tau = st->s.tau, h2 = h * h, h22 = h2 * 2.0;
+  const size_t sy = (size_t)nx, sz = (size_t)nx * ny;
+  for (int j = 2; j <= ny - 1; j++)
+    for (int i = 2; i <= nx - 1; i++)
+      for (int k = 2; k <= nz - 1; k++) {
+        const size_t q = IX(i, j, k);
+        const double *K = ktur, *E = eps;
+        double conv = (dmax1(u[q + 1], 0.0) * K[q] + dmin1(u[q + 1], 0.0) * K[q + 1] -
+                       dmax1(u[q], 0.0) * K[q - 1] - dmin1(u[q], 0.0) * K[q] +
+                       dmax1(v[q + sy], 0.0) * K[q] + dmin1(v[q + sy], 0.0) * K[q + sy] -
+                       dmax1(v[q], 0.0) * K[q - sy] - dmin1(v[q], 0.0) * K[q] +
+                       dmax1(w[q + sz], 0.0) * K[q] + dmin1(w[q + sz], 0.0) * K[q + sz] -
+                       dmax1(w[q], 0.0) * K[q - sz] - dmin1(w[q], 0.0) * K[q]) / h;
+        double cip = mun[q + 1] + mun[q] + (mut[q] + mut[q + 1]) / sigk;
+        double cim = mun[q - 1] + mun[q] + (mut[q] + mut[q - 1]) / sigk;
+        double cjp = mun[q + sy] + mun[q] + (mut[q] + mut[q + sy]) / sigk;
+        double cjm = mun[q - sy] + mun[q] + (mut[q] + mut[q - sy]) / sigk;
+        double ckp = mun[q + sz] + mun[q] + (mut[q] + mut[q + sz]) / sigk;
+        double ckm = mun[q - sz] + mun[q] + (mut[q] + mut[q - sz]) / sigk;
+        double diff = 1.0 / (rhon[q] * h22) *
+                      (cip * (K[q + 1] - K[q]) - cim * (K[q] - K[q - 1]) + cjp * (K[q + sy] - K[q]) -
+                       cjm * (K[q] - K[q - sy]) + ckp * (K[q + sz] - K[q]) - ckm * (K[q] - K[q - sz]));
+        const double dudx = u[q + 1] - u[q];
+        const double dudy = 0.25 * (u[q] - u[q - sy] + u[q + 1] - u[q + 1 - sy] + u[q + sy] - u[q] +
+                                    u[q + 1 + sy] - u[q + 1]);
+        const double dudz = 0.25 * (u[q] - u[q - sz] + u[q + 1] - u[q + 1 - sz] + u[q + sz] - u[q] +
+                                    u[q + 1 + sz] - u[q + 1]);
+        const double dvdx = 0.25 * (v[q] - v[q - 1] + v[q + 1] - v[q] + v[q + sy] - v[q - 1 + sy] +
+                                    v[q + 1 + sy] - v[q + sy]);
+        const double dvdy = v[q + sy] - v[q];
+        const double dvdz = 0.25 * (v[q] - v[q - sz] + v[q + sz] - v[q] + v[q + sy] - v[q + sy - sz] +
+                                    v[q + sy + sz] - v[q + sy]);
+        const double dwdx = 0.25 * (w[q] - w[q - 1] + w[q + 1] - w[q] + w[q + sz] - w[q - 1 + sz] +
+                                    w[q + 1 + sz] - w[q + sz]);
+        const double dwdy = 0.25 * (w[q] - w[q - sy] + w[q + sz] - w[q - sy + sz] + w[q + sy] - w[q] +
+                                    w[q + sy + sz] - w[q + sz]);
+        const double dwdz = w[q + sz] - w[q];
+        double prod = mut[q] / rhon[q] / h2 *
+                      (2.0 * (dudx * dudx + dvdy * dvdy + dwdz * dwdz + dvdx * dudy + dwdx * dudz + dvdz * dwdy) +
+                       dudy * dudy + dudz * dudz + dvdx * dvdx + dvdz * dvdz + dwdx * dwdx + dwdy * dwdy);
+        kn[q] = K[q] + tau * (-conv + diff + prod - E[q]);
+        conv = (dmax1(u[q + 1], 0.0) * E[q] + dmin1(u[q + 1], 0.0) * E[q + 1] - dmax1(u[q], 0.0) * E[q - 1] -
+                dmin1(u[q], 0.0) * E[q] + dmax1(v[q + sy], 0.0) * E[q] + dmin1(v[q + sy], 0.0) * E[q + sy] -
+                dmax1(v[q], 0.0) * E[q - sy] - dmin1(v[q], 0.0) * E[q] + dmax1(w[q + sz], 0.0) * E[q] +
+                dmin1(w[q + sz], 0.0) * E[q + sz] - dmax1(w[q], 0.0) * E[q - sz] - dmin1(w[q], 0.0) * E[q]) /
+               h;
+        cip = mun[q + 1] + mun[q] + (mut[q] + mut[q + 1]) / sige;
+        cim = mun[q - 1] + mun[q] + (mut[q] + mut[q - 1]) / sige;
+        cjp = mun[q + sy] + mun[q] + (mut[q] + mut[q + sy]) / sige;
+        cjm = mun[q - sy] + mun[q] + (mut[q] + mut[q - sy]) / sige;
+        ckp = mun[q + sz] + mun[q] + (mut[q] + mut[q + sz]) / sige;
+        ckm = mun[q - sz] + mun[q] + (mut[q] + mut[q - sz]) / sige;
+        diff = 1.0 / (rhon[q] * h22) *
+               (cip * (E[q + 1] - E[q]) - cim * (E[q] - E[q - 1]) + cjp * (E[q + sy] - E[q]) -
+                cjm * (E[q] - E[q - sy]) + ckp * (E[q + sz] - E[q]) - ckm * (E[q] - E[q - sz]));
+        prod = prod * c1 * E[q] / K[q];
+        en[q] = E[q] + tau * (-conv + diff + prod - c2 * E[q] * E[q] / K[q]);
+      }
+  for (int j = 2; j <= ny - 1; j++)
+    for (int i = 2; i <= nx - 1; i++)
+      for (int k = 2; k <= nz - 1; k++) {
+        const size_t q = IX(i, j, k);
+        ktur[q] = kn[q];
+        eps[q] = en[q];
+        st->mut[q] = cmu * rhon[q] * ktur[q] * ktur[q] / eps[q];
+      }
+  ora_bc_scalar(ktur, nx, ny, nz);
+  ora_bc_scalar(eps, nx, ny, nz);
+  ora_bc_scalar(st->mut, nx, ny, nz);
+}
+
 void ora_vofmethod(ora_state *st) {
   const int ng = st->s.ng;
   double *cc = LV(ng, LCC), *s1 = LV(ng, LEI), *s2 = LV(ng, LRES), *s3 = LV(ng, LRHS);
@@ -798,6 +938,7 @@ void ora_vofmethod(ora_state *st) {
     ora_swp(st, st->w, cc, s1, s2, s3, 3);
   }
   bc_c(cc, st->nx, st->ny, st->nz);
+  if (st->in.iturb != 0) fturbdif(st, cc);
   calcrho(st);
 }
 
@@ -1206,6 +1347,7 @@ ora_state *ora_create(const ora_input *in) {
   st->s11 = zalloc(n); st->s22 = zalloc(n); st->s33 = zalloc(n);
   st->s12 = zalloc(n); st->s13 = zalloc(n); st->s23 = zalloc(n);
   st->rhon = zalloc(n); st->mun = zalloc(n);
+  st->ktur = zalloc(n); st->eps = zalloc(n); st->mut = zalloc(n);
   st->s.npre = in->npre; st->s.npost = in->npost; st->s.ntop = in->ntop; st->s.cycles = in->cycles;
   st->s.last_epsdiv = -1.0;
   nondim(st);
@@ -1226,6 +1368,7 @@ ora_state *ora_create(const ora_input *in) {
   bc_c(LV(ng, LCC), st->nx, st->ny, st->nz);
   bc_v(st);
   calcrho(st);
+  if (in->iturb == 3) keps_seed(st);
   return st;
 }
 
@@ -1236,6 +1379,7 @@ void ora_destroy(ora_state *st) {
   free(st->u); free(st->v); free(st->w);
   free(st->s11); free(st->s22); free(st->s33); free(st->s12); free(st->s13); free(st->s23);
   free(st->rhon); free(st->mun);
+  free(st->ktur); free(st->eps); free(st->mut);
   free(st);
 }
 
@@ -1265,6 +1409,9 @@ double *ora_field(ora_state *st, int id) {
     case ORA_S23: return st->s23;
     case ORA_RHON: return st->rhon;
     case ORA_MUN: return st->mun;
+    case ORA_KTUR: return st->ktur;
+    case ORA_EPS: return st->eps;
+    case ORA_MUT: return st->mut;
     default: return NULL;
   }
 }
@@ -1282,8 +1429,13 @@ void ora_get_scalars(const ora_state *st, ora_scalars *out) { *out = st->s; }
 void ora_set_scalars(ora_state *st, const ora_scalars *in) { st->s = *in; }
 
 /* main.f:19-73 loop body for surfacet=2 (CSF), hswitch=0, laminar */
+void ora_kepsmodel(ora_state *st) {
+  if (st->in.iturb == 3) kepsmodel(st);
+}
+
 void ora_step(ora_state *st, int t) {
   ora_vofmethod(st);
+  ora_kepsmodel(st);
   ora_checktime(st);
   ora_csf(st);
   ora_solvelpres(st, t);

@@ -32,7 +32,9 @@ enum {
   ORA_CC = 0, ORA_P = 1, ORA_RES = 2, ORA_RHS = 3, ORA_A = 4, ORA_B = 5,
   ORA_C = 6, ORA_EI = 7, ORA_U = 8, ORA_V = 9, ORA_W = 10, ORA_S11 = 11,
   ORA_S22 = 12, ORA_S33 = 13, ORA_S12 = 14, ORA_S13 = 15, ORA_S23 = 16,
-  ORA_RHON = 17, ORA_MUN = 18, ORA_NFIELDS = 19
+  ORA_RHON = 17, ORA_MUN = 18, ORA_NFIELDS = 19,
+  /* k-epsilon state (iturb = 3); 19, 20 are the GPU build's pressure history */
+  ORA_KTUR = 21, ORA_EPS = 22, ORA_MUT = 23
 };
 
 /* Pressure-solver modes. */
@@ -91,12 +93,13 @@ void ora_level_dims(const ora_state *st, int level, int *nx, int *ny, int *nz);
 void ora_get_scalars(const ora_state *st, ora_scalars *out);
 void ora_set_scalars(ora_state *st, const ora_scalars *in);
 
-void ora_vofmethod(ora_state *st);        /* main.f:795-824 */
+void ora_vofmethod(ora_state *st);        /* main.f:795-824 (+ fturbdif 1239-1267 when iturb != 0) */
+void ora_kepsmodel(ora_state *st);        /* main.f:1888-2025 when iturb = 3, else nothing */
 void ora_checktime(ora_state *st);        /* main.f:2152-2171 */
 void ora_csf(ora_state *st);              /* main.f:2363-2481 */
 void ora_solvelpres(ora_state *st, int t); /* main.f:3236-3439 */
 void ora_mglin(ora_state *st);            /* main.f:3645-3763 (+ tol mode) */
-void ora_step(ora_state *st, int t);      /* main.f:19-73 loop body, CSF, laminar */
+void ora_step(ora_state *st, int t);      /* main.f:19-73 loop body, CSF, laminar or k-epsilon */
 double ora_relres(ora_state *st);         /* ||rhs - L p|| / ||rhs|| on the fine level */
 
 /* ---- array-level routines (reference subroutine interfaces) ------------- */

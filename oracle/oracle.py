@@ -14,6 +14,7 @@ from . import build as _build
 FIELDS = ["cc", "p", "res", "rhs", "a", "b", "c", "ei", "u", "v", "w",
           "s11", "s22", "s33", "s12", "s13", "s23", "rhon", "mun"]
 FIELD_ID = {n: i for i, n in enumerate(FIELDS)}
+FIELD_ID.update({"ktur": 21, "eps": 22, "mut": 23})
 
 MODE_REF_EXACT = 0
 MODE_TOL_FP64 = 1
@@ -76,7 +77,7 @@ def load():
     lib.ora_level_dims.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
     lib.ora_get_scalars.argtypes = [vp, C.POINTER(OracleScalars)]
     lib.ora_set_scalars.argtypes = [vp, C.POINTER(OracleScalars)]
-    for fn in ("ora_vofmethod", "ora_checktime", "ora_csf", "ora_mglin"):
+    for fn in ("ora_vofmethod", "ora_kepsmodel", "ora_checktime", "ora_csf", "ora_mglin"):
         getattr(lib, fn).argtypes = [vp]
     lib.ora_solvelpres.argtypes = [vp, C.c_int]
     lib.ora_step.argtypes = [vp, C.c_int]
@@ -181,6 +182,9 @@ class Oracle:
 
     def vofmethod(self):
         self.lib.ora_vofmethod(self.h)
+
+    def kepsmodel(self):
+        self.lib.ora_kepsmodel(self.h)
 
     def checktime(self):
         self.lib.ora_checktime(self.h)

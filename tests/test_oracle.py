@@ -179,3 +179,20 @@ def test_golden_fixture(fname):
     assert got.keys() == ref["values"].keys()
     for k, v in ref["values"].items():
         assert got[k] == v, (fname, k, got[k], v)
+
+
+def test_keps_of_the_reference_diverges_on_the_drop(dsg):
+    """The reference's explicit k-epsilon model (iturb = 3) on the drop: the
+    eddy viscosity grows by orders of magnitude per step and the state
+    overflows on the third step.  Recorded so that a change of this
+    behaviour is noticed."""
+    from oracle import Oracle
+    ora = Oracle(dsg.config.droplet(32, mode=1, tol=1e-8, impact_speed=3.0).replace(iturb=3).as_dict())
+    mut0 = ora.field("mut").max()
+    ora.step(1)
+    ora.step(2)
+    mut2 = ora.field("mut").max()
+    assert np.isfinite(mut2) and mut2 > 100 * mut0
+    ora.step(3)
+    mut3 = ora.field("mut")
+    assert not np.isfinite(mut3).all() or mut3.max() > 1e10
