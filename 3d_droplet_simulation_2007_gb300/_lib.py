@@ -143,6 +143,14 @@ SIGNATURES = [
     ("dsg_net_grad_host", _i, [_vp, _vp, _vp, C.POINTER(C.c_float), _vp]),
     ("dsg_net_train_step", _i, [_vp, C.c_float, C.POINTER(C.c_float)]),
     ("dsg_attach_net", _i, [_vp, _vp, _i]),
+    ("dsg_snapshot", _i, [_vp, _i]),
+    ("dsg_snapshot_wait", _i, [_vp, _IP]),
+    ("dsg_snapshot_field", _i, [_vp, _i, _vp]),
+    ("dsg_write_tecplot", _i, [_vp, C.c_char_p]),
+    ("dsg_write_pressure_slice", _i, [_vp, C.c_char_p]),
+    ("dsg_savedata", _i, [_vp, C.c_char_p, _i]),
+    ("dsg_iniget", _i, [_vp, C.c_char_p, _IP]),
+    ("dsg_printout", _i, [_vp, _i, C.c_char_p]),
     ("dsg_ensemble_create", _i, [C.POINTER(DsgConfig), _i, _i, _PP]),
     ("dsg_ensemble_destroy", None, [_vp]),
     ("dsg_ensemble_size", _i, [_vp]),

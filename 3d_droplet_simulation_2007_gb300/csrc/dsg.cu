@@ -809,6 +809,7 @@ int dsg_create(const dsg_config *cfg, dsg_ctx **out) {
 void dsg_destroy(dsg_ctx *ctx) {
   if (!ctx) return;
   if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
+  dsg::snapshot_release(ctx);
   for (cudaEvent_t e : ctx->prof_ev) cudaEventDestroy(e);
   for (cudaEvent_t e : ctx->phase_ev) cudaEventDestroy(e);
   graph_release(ctx->g_first);
@@ -892,6 +893,14 @@ int dsg_init_drop(dsg_ctx *ctx) {
   DSG_CK(ctx, dsg::init_drop(ctx->f[DSG_F_CC], ctx->f[DSG_F_U], ctx->f[DSG_F_V], ctx->f[DSG_F_W], d, s.h, x0,
                              s.y0, s.z0, s.radius, s.yvel1, s.yvel2, s.zvel1, s.zvel2, amp, ctx->cfg.noise_seed,
                              ctx->stream));
+  return dsg::restart_state(ctx);
+}
+
+}  // extern "C"
+
+int dsg::restart_state(dsg_ctx *ctx) {
+  const dsg_scalars &s = ctx->s;
+  const Dims d = ctx->fine();
   DSG_CK(ctx, dsg::bc_c(ctx->f[DSG_F_CC], d, ctx->stream));
   DSG_CK(ctx, dsg::bc_v(ctx->f[DSG_F_U], ctx->f[DSG_F_V], ctx->f[DSG_F_W], ctx->red_partials, d, s.xvel2,
                         ctx->stream));
@@ -912,6 +921,8 @@ int dsg_init_drop(dsg_ctx *ctx) {
   DSG_CK(ctx, cudaStreamSynchronize(ctx->stream));
   return DSG_OK;
 }
+
+extern "C" {
 
 int dsg_vofmethod(dsg_ctx *ctx) {
   if (!ctx) return DSG_E_ARG;

@@ -252,6 +252,14 @@ struct dsg_ctx {
   std::vector<cudaEvent_t> phase_ev;  // phase markers of dsg_step (event pool)
   std::vector<int> phase_id;          // phase that starts at each marker, -1 = end
   size_t phase_used = 0;
+  // snapshot (io.cu): p, u, v, w, cc staged in HBM, copied to pinned host memory
+  static constexpr int kSnapFields = 5;
+  double *snap_dev = nullptr;
+  double *snap_host = nullptr;
+  cudaStream_t snap_stream = nullptr;
+  cudaEvent_t snap_ready = nullptr, snap_done = nullptr;
+  bool snap_pending = false;
+  int snap_t = -1;
   dsg::Dims fine() const { return dsg::Dims{nx, ny, nz}; }
   dsg::Dims level(int l) const { return dsg::Dims{lnx[l], lny[l], lnz[l]}; }
 };
@@ -259,6 +267,10 @@ struct dsg_ctx {
 namespace dsg {
 int set_error(dsg_ctx *ctx, int code, const char *fmt, ...);
 int cuda_fail(dsg_ctx *ctx, cudaError_t e, const char *where);
+// boundary conditions and derived fields after the state was loaded (the
+// restart branch of initialize, main.f:174-177), k-epsilon seeding included
+int restart_state(dsg_ctx *ctx);
+void snapshot_release(dsg_ctx *ctx);
 }  // namespace dsg
 
 #define DSG_CK(ctx, expr)                                   \

@@ -170,6 +170,40 @@ class Solver:
             self.step()
         return self.last_stats
 
+    # ---- snapshots and output files (printout, main.f:5020-5104) ------------
+    def snapshot(self, t=None):
+        """Stage p, u, v, w, cc now; the host copy overlaps the next steps."""
+        self._ck(self.lib.dsg_snapshot(self.ctx, self.t if t is None else t))
+
+    def snapshot_wait(self):
+        t = C.c_int()
+        self._ck(self.lib.dsg_snapshot_wait(self.ctx, C.byref(t)))
+        return t.value
+
+    def snapshot_field(self, name):
+        out = np.empty(self.shape, dtype=np.float64, order="F")
+        self._ck(self.lib.dsg_snapshot_field(self.ctx, _lib.FIELD_ID[name], out.ctypes.data))
+        return out
+
+    def write_tecplot(self, path):
+        self._ck(self.lib.dsg_write_tecplot(self.ctx, str(path).encode()))
+
+    def write_pressure_slice(self, path):
+        self._ck(self.lib.dsg_write_pressure_slice(self.ctx, str(path).encode()))
+
+    def savedata(self, path, t0=None):
+        self._ck(self.lib.dsg_savedata(self.ctx, str(path).encode(), self.t if t0 is None else t0))
+
+    def iniget(self, path):
+        """Load a restart file; returns its step index t0."""
+        t0 = C.c_int()
+        self._ck(self.lib.dsg_iniget(self.ctx, str(path).encode(), C.byref(t0)))
+        self.t = t0.value
+        return t0.value
+
+    def printout(self, t, directory=None):
+        self._ck(self.lib.dsg_printout(self.ctx, t, None if directory is None else str(directory).encode()))
+
     # ---- instrumentation ------------------------------------------------------
     def profile_enable(self, on=True):
         self._ck(self.lib.dsg_profile_enable(self.ctx, 1 if on else 0))

@@ -237,6 +237,32 @@ int dsg_bc_out(double *s, int nx, int ny, int nz, void *stream);
 /* filterc27 main.f:5473-5511 */
 int dsg_filterc27(const double *cc, double *cf, int nx, int ny, int nz, void *stream);
 
+/* ---- snapshots and output files ---------------------------------------------
+ * A snapshot stages p, u, v, w and cc of step t in device memory (ordered
+ * after the work already on the context stream) and copies them to pinned
+ * host memory on a separate stream, so the following steps overlap the copy.
+ * The writers use the last snapshot (waiting for its copy; taking one if
+ * there is none):
+ *   dsg_write_tecplot        printtecp, main.f:5105-5153 (X,Y,Z,U,V,W,CC)
+ *   dsg_write_pressure_slice printout's pressure plane, main.f:5074-5095
+ *   dsg_savedata / iniget    the unformatted restart file, main.f:5414-5467 /
+ *                            698-790, as a consistent pair (the reference's
+ *                            savedata writes a unit it did not open); iniget
+ *                            loads u, v, w, cc into a context of the same grid
+ *                            and applies bc_c, bc_v, calcrho (main.f:174-177)
+ *   dsg_printout             printout's schedule, main.f:5020-5104:
+ *                            main####.plt every ntecplot steps,
+ *                            pressure####.plt every 100 steps, save.dat at
+ *                            t = tsave, in directory dir (NULL: cwd). */
+int dsg_snapshot(dsg_ctx *ctx, int t);
+int dsg_snapshot_wait(dsg_ctx *ctx, int *t);
+int dsg_snapshot_field(dsg_ctx *ctx, int field, double *host); /* field in p, u, v, w, cc */
+int dsg_write_tecplot(dsg_ctx *ctx, const char *path);
+int dsg_write_pressure_slice(dsg_ctx *ctx, const char *path);
+int dsg_savedata(dsg_ctx *ctx, const char *path, int t0);
+int dsg_iniget(dsg_ctx *ctx, const char *path, int *t0);
+int dsg_printout(dsg_ctx *ctx, int t, const char *dir);
+
 /* ---- ensemble -------------------------------------------------------------
  * No counterpart in the reference (main.f runs one case per process).  An
  * ensemble holds n independent contexts (cfgs[i], each initialised as
