@@ -48,7 +48,9 @@ __device__ __forceinline__ Nb neighbours(const float *__restrict__ u, size_t q, 
 // colour, reads and writes its own colour and reads cc for the face
 // coefficients, all with full 32-byte sectors: 24 bytes per cell per relax.
 // Face coefficients are formed from the FP32 volume fraction as abcei does,
-// a = 1/(r1*(c_i+c_{i+1}) + r2), with bc_coef's a(1) = a(2).
+// a = 1/(r1*(c_i+c_{i+1}) + r2), with bc_coef's a(1) = a(2).  (Storing cc
+// colour-split as well, so that every load of a pass is a contiguous run, was
+// measured slower: 3.88 against 4.25 TB/s at 256^3.)
 struct Split {
   int hx, ny2, nz2;  // (nx-2)/2, ny-2, nz-2
   __host__ __device__ __forceinline__ size_t at(int m, int j, int k) const {
@@ -279,46 +281,86 @@ __global__ void k_addint32(float *__restrict__ uf, const float *__restrict__ uc,
 // prolongation, post-sweeps: mglin's recursion, main.f:3703-3759) inside one
 // block, with a block barrier between passes in place of a launch boundary.
 // The level arrays stay in L1/L2.
+// Threads 0..NT-1 of the block sweep level L n times; WARP: NT = 32 and the
+// passes are separated by warp barriers (levels of a few dozen cells), else
+// NT = blockDim.x and block barriers.
+template <bool WARP>
 __device__ void tail_relax(const TailLevel &L, int n, float omega) {
+  const int nt = WARP ? 32 : (int)blockDim.x;
   const Dims d = L.d;
   const int hx = (d.nx - 1) / 2;  // cells of one colour per row, rounded up
   const int ny2 = d.ny - 2;
   const int total = hx * ny2 * (d.nz - 2);
   for (int s = 0; s < n; s++)
     for (int colour = 0; colour < 2; colour++) {
-      for (int t = threadIdx.x; t < total; t += blockDim.x) {
+      for (int t = threadIdx.x; t < total; t += nt) {
         const int m = t % hx, r = t / hx;
         const int j = 2 + r % ny2, k = 2 + r / ny2;
         const int i = 2 + ((j + k + colour) & 1) + 2 * m;
         if (i <= d.nx - 1) relax32_cell(L.u, L.rhs, L.a, L.b, L.c, L.ei, d, i, j, k, L.h2, omega);
       }
-      __syncthreads();
+      if (WARP) __syncwarp(); else __syncthreads();
     }
 }
 
-__device__ void tail_body(const TailArgs &A) {
-  for (int l = A.top; l >= 2; l--) {
-    const TailLevel &F = A.lv[l], &C = A.lv[l - 1];
-    tail_relax(F, A.npre, A.omega);
-    const int cx = C.d.nx - 2, cy = C.d.ny - 2, total = cx * cy * (C.d.nz - 2);
-    const float h2i = 1.0f / F.h2;
-    for (int t = threadIdx.x; t < total; t += blockDim.x) {
-      const int ic = 2 + t % cx, r = t / cx;
-      resid_restrict32_cell(C.rhs, C.u, F.u, F.rhs, F.a, F.b, F.c, F.d, C.d, h2i, ic, 2 + r % cy, 2 + r / cy);
-    }
-    __syncthreads();
+// Residual of level F restricted into level C's rhs, C's correction zeroed.
+template <bool WARP>
+__device__ void tail_restrict(const TailLevel &F, const TailLevel &C) {
+  const int nt = WARP ? 32 : (int)blockDim.x;
+  const int cx = C.d.nx - 2, cy = C.d.ny - 2, total = cx * cy * (C.d.nz - 2);
+  const float h2i = 1.0f / F.h2;
+  for (int t = threadIdx.x; t < total; t += nt) {
+    const int ic = 2 + t % cx, r = t / cx;
+    resid_restrict32_cell(C.rhs, C.u, F.u, F.rhs, F.a, F.b, F.c, F.d, C.d, h2i, ic, 2 + r % cy, 2 + r / cy);
   }
-  tail_relax(A.lv[1], A.ntop, A.omega);
-  for (int l = 2; l <= A.top; l++) {
-    const TailLevel &F = A.lv[l], &C = A.lv[l - 1];
-    const int fx = F.d.nx - 2, fy = F.d.ny - 2, total = fx * fy * (F.d.nz - 2);
-    for (int t = threadIdx.x; t < total; t += blockDim.x) {
-      const int i = 2 + t % fx, r = t / fx;
-      const int j = 2 + r % fy, k = 2 + r / fy;
-      F.u[F.d.ix(i, j, k)] += C.u[C.d.ix((i >> 1) + 1, (j >> 1) + 1, (k >> 1) + 1)];
+  if (WARP) __syncwarp(); else __syncthreads();
+}
+
+// Level F's correction += injection of level C's.
+template <bool WARP>
+__device__ void tail_addint(const TailLevel &F, const TailLevel &C) {
+  const int nt = WARP ? 32 : (int)blockDim.x;
+  const int fx = F.d.nx - 2, fy = F.d.ny - 2, total = fx * fy * (F.d.nz - 2);
+  for (int t = threadIdx.x; t < total; t += nt) {
+    const int i = 2 + t % fx, r = t / fx;
+    const int j = 2 + r % fy, k = 2 + r / fy;
+    F.u[F.d.ix(i, j, k)] += C.u[C.d.ix((i >> 1) + 1, (j >> 1) + 1, (k >> 1) + 1)];
+  }
+  if (WARP) __syncwarp(); else __syncthreads();
+}
+
+// Levels with at most this many interior cells (6^3 nodes and below) run in
+// warp 0 alone, at most two cells per lane and pass.
+constexpr int kTailWarpCells = 64;
+
+__device__ void tail_body(const TailArgs &A) {
+  // lw: the largest level small enough for one warp (0: none)
+  int lw = 0;
+  for (int l = 1; l <= A.top; l++) {
+    const Dims d = A.lv[l].d;
+    if ((d.nx - 2) * (d.ny - 2) * (d.nz - 2) <= kTailWarpCells) lw = l;
+  }
+  for (int l = A.top; l > lw && l >= 2; l--) {
+    tail_relax<false>(A.lv[l], A.npre, A.omega);
+    tail_restrict<false>(A.lv[l], A.lv[l - 1]);
+  }
+  if (lw == 0) {
+    tail_relax<false>(A.lv[1], A.ntop, A.omega);
+  } else if (threadIdx.x < 32) {
+    for (int l = lw; l >= 2; l--) {
+      tail_relax<true>(A.lv[l], A.npre, A.omega);
+      tail_restrict<true>(A.lv[l], A.lv[l - 1]);
     }
-    __syncthreads();
-    tail_relax(F, A.npost, A.omega);
+    tail_relax<true>(A.lv[1], A.ntop, A.omega);
+    for (int l = 2; l <= lw; l++) {
+      tail_addint<true>(A.lv[l], A.lv[l - 1]);
+      tail_relax<true>(A.lv[l], A.npost, A.omega);
+    }
+  }
+  if (lw > 0) __syncthreads();
+  for (int l = (lw > 1 ? lw : 1) + 1; l <= A.top; l++) {
+    tail_addint<false>(A.lv[l], A.lv[l - 1]);
+    tail_relax<false>(A.lv[l], A.npost, A.omega);
   }
 }
 
@@ -461,12 +503,12 @@ __global__ void k_correct64(double *__restrict__ p, const float *__restrict__ ev
   p[q] = init ? e : p[q] + e;
 }
 
+// Coarse FP32 coefficients (acfromac) straight from the FP64 fine ones.
 __global__ void k_to32(float *__restrict__ dst, const double *__restrict__ src, size_t n) {
   for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
     dst[q] = (float)src[q];
 }
 
-// Coarse FP32 coefficients (acfromac) straight from the FP64 fine ones.
 __global__ void k_acfromac64to32(float *__restrict__ a, float *__restrict__ b, float *__restrict__ c,
                                  float *__restrict__ ei, const double *__restrict__ a2,
                                  const double *__restrict__ b2, const double *__restrict__ c2, Dims dc, Dims df) {
