@@ -85,6 +85,10 @@ class InputData:
     use_graphs: int = 1
     tail_nodes: int = 0
     warm_start: int = 0
+    # relaxation factor of the FP32 V-cycles (the mixed modes' preconditioner):
+    # 1.4 needed the fewest V-cycles on the 256^3 splash (sweep 1.0-1.5: 8-9
+    # V-cycles per step against 9-10 with the reference's OMEGA = 1.5)
+    mg32_omega: float = 1.4
 
     def as_dict(self):
         return asdict(self)

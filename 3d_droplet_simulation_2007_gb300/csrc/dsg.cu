@@ -187,6 +187,12 @@ int relres_host(dsg_ctx *ctx, double *out) {
 // ---- mixed precision: FP32 V-cycles inside FP64 defect correction ---------
 enum { U32 = 0, RHS32 = 1, A32 = 2, B32 = 3, C32 = 4, EI32 = 5 };
 
+// Relaxation factor of the FP32 V-cycle (a preconditioner of the FP64 defect
+// correction, so free to differ from the reference's OMEGA).
+inline float omega32(const dsg_ctx *ctx) {
+  return (float)(ctx->cfg.mg32_omega > 0.0 ? ctx->cfg.mg32_omega : ctx->cfg.omega);
+}
+
 inline float level_h2(dsg_ctx *ctx, int l) {
   const double h1 = ctx->s.lengthsize / (ctx->lnx[l] - 2);
   return (float)(h1 * h1);
@@ -238,7 +244,7 @@ cudaError_t relax32_level(dsg_ctx *ctx, int n, int l) {
     float r1, r2;
     phase_coefs(ctx, &r1, &r2);
     cudaError_t e =
-        dsg::relax32_split_n(n, f.u, f.r, L[A32], d, level_h2(ctx, l), (float)ctx->cfg.omega, r1, r2, ctx->stream);
+        dsg::relax32_split_n(n, f.u, f.r, L[A32], d, level_h2(ctx, l), omega32(ctx), r1, r2, ctx->stream);
     if (e != cudaSuccess) return e;
     return cudaEventRecordWithFlags(e1, ctx->stream, cudaEventRecordExternal);
   }
@@ -259,10 +265,10 @@ cudaError_t relax32_level(dsg_ctx *ctx, int n, int l) {
     FineSplit f = fine_split(ctx);
     float r1, r2;
     phase_coefs(ctx, &r1, &r2);
-    e = dsg::relax32_split_n(n, f.u, f.r, L[A32], d, level_h2(ctx, l), (float)ctx->cfg.omega, r1, r2, ctx->stream);
+    e = dsg::relax32_split_n(n, f.u, f.r, L[A32], d, level_h2(ctx, l), omega32(ctx), r1, r2, ctx->stream);
   } else {
     e = dsg::relax32_n(n, L[U32], level_h2(ctx, l), L[RHS32], L[A32], L[B32], L[C32], L[EI32], d,
-                       (float)ctx->cfg.omega, ctx->stream);
+                       omega32(ctx), ctx->stream);
   }
   if (timed) {
     cudaError_t r = cudaEventRecord(ctx->prof_ev[ctx->prof_used + 1], ctx->stream);
@@ -288,7 +294,7 @@ void tail_args(dsg_ctx *ctx, int top, dsg::TailArgs *A) {
   A->npre = ctx->s.npre;
   A->npost = ctx->s.npost;
   A->ntop = ctx->s.ntop;
-  A->omega = (float)ctx->cfg.omega;
+  A->omega = omega32(ctx);
 }
 
 int vcycle32(dsg_ctx *ctx, int j) {
@@ -572,12 +578,15 @@ int mixed_solve(dsg_ctx *ctx, dsg_mg_stats *s) {
     ctx->last_relres_net = r_net;
     s->relres_prev = r_prev;
     s->relres_net = r_net;
-  } else if (ctx->cfg.warm_start == 1) {
-    // previous-step pressure as the initial guess
+  } else if (ctx->cfg.warm_start == 1 || ctx->cfg.warm_start == 2) {
+    // previous-step pressure (1) or zero (2) as the initial guess
     rc = coef_hierarchy32(ctx);
     if (rc) return rc;
-    DSG_CK(ctx, cudaMemcpyAsync(ctx->lv[ng][1], ctx->f[DSG_F_PPREV], ctx->fine().count() * sizeof(double),
-                                cudaMemcpyDeviceToDevice, st));
+    if (ctx->cfg.warm_start == 1)
+      DSG_CK(ctx, cudaMemcpyAsync(ctx->lv[ng][1], ctx->f[DSG_F_PPREV], ctx->fine().count() * sizeof(double),
+                                  cudaMemcpyDeviceToDevice, st));
+    else
+      DSG_CK(ctx, cudaMemsetAsync(ctx->lv[ng][1], 0, ctx->fine().count() * sizeof(double), st));
     rc = defect_host(ctx, &r);
     if (rc) return rc;
   } else {

@@ -43,6 +43,10 @@ def parse():
     ap.add_argument("--inner", type=int, default=0,
                     help="FP32 V-cycles per FP64 defect (mixed modes; 0: adaptive)")
     ap.add_argument("--no-graphs", action="store_true", help="launch the mixed solve without CUDA graphs")
+    ap.add_argument("--start", type=int, default=None,
+                    help="initial guess of the mixed solve: 0 FMG, 1 previous pressure, 2 zero (default: config)")
+    ap.add_argument("--omega32", type=float, default=None,
+                    help="relaxation factor of the FP32 V-cycles (default: the library configuration's)")
     ap.add_argument("--tail-nodes", type=int, default=0,
                     help="largest FP32 level (nodes) of the single-block coarse tail (0: default, -1: off)")
     ap.add_argument("--e2e-steps", type=int, default=3)
@@ -62,11 +66,13 @@ def dist_env():
     return ws, rank, local
 
 
-def workload(dsg, n, mode, tol, inner=0, graphs=True, tail_nodes=0):
+def workload(dsg, n, mode, tol, inner=0, graphs=True, tail_nodes=0, omega32=None, start=None):
     cfg = dsg.config
-    return cfg.droplet(n, steps=1000, impact_speed=3.0, noise_si=1e-4, mode=mode, tol=tol,
-                       npre=4, npost=4, ntop=4).replace(inner_vcycles=inner, use_graphs=1 if graphs else 0,
-                                                        tail_nodes=tail_nodes)
+    inp = cfg.droplet(n, steps=1000, impact_speed=3.0, noise_si=1e-4, mode=mode, tol=tol,
+                      npre=4, npost=4, ntop=4).replace(inner_vcycles=inner, use_graphs=1 if graphs else 0,
+                                                       tail_nodes=tail_nodes)
+    inp = inp if omega32 is None else inp.replace(mg32_omega=omega32)
+    return inp if start is None else inp.replace(warm_start=start)
 
 
 def measured_peaks():
@@ -204,7 +210,8 @@ def run_gb300(args):
     dsg = importlib.import_module(PKG)
     dsg.load()
     mode = mode_of(dsg, args.mode)
-    inp = workload(dsg, args.n, mode, args.tol, args.inner, not args.no_graphs, args.tail_nodes)
+    inp = workload(dsg, args.n, mode, args.tol, args.inner, not args.no_graphs, args.tail_nodes, args.omega32,
+                   args.start)
     solver = dsg.Solver(inp)
     solver.set_stream(torch.cuda.current_stream().cuda_stream)
     for t in range(1, args.warmup + 1):

@@ -84,7 +84,9 @@ typedef struct dsg_config {
   int use_graphs;      /* capture the mixed-mode iterations in CUDA graphs (1) or launch directly (0) */
   int tail_nodes;      /* mixed modes: FP32 levels of at most this many nodes run in one single-block
                           launch per V-cycle (0: 18^3 = 5832; < 0: one launch per pass on every level) */
-  int warm_start;      /* DSG_MODE_TOL_MIXED: 0 = FP32 full-multigrid start, 1 = previous-step pressure */
+  int warm_start;      /* DSG_MODE_TOL_MIXED initial guess: 0 = FP32 full multigrid, 1 = previous-step
+                          pressure, 2 = zero */
+  double mg32_omega;   /* relaxation factor of the FP32 V-cycles of the mixed modes (<= 0: omega) */
 } dsg_config;
 
 /* Non-dimensional scalars and adaptive counters (COMMON /PHYSICS/, /DIFF/,
