@@ -23,7 +23,7 @@ ERROR_NAMES = {0: "DSG_OK", -1: "DSG_E_ARG", -2: "DSG_E_CUDA", -3: "DSG_E_NOMEM"
 
 FIELDS = ["cc", "p", "res", "rhs", "a", "b", "c", "ei", "u", "v", "w",
           "s11", "s22", "s33", "s12", "s13", "s23", "rhon", "mun", "pprev", "pprev2",
-          "ktur", "eps", "mut"]
+          "ktur", "eps", "mut", "hxmin", "hxmax", "hymin", "hymax", "hzmin", "hzmax"]
 FIELD_ID = {n: i for i, n in enumerate(FIELDS)}
 
 
@@ -110,6 +110,7 @@ SIGNATURES = [
     ("dsg_init_drop", _i, [_vp]),
     ("dsg_vofmethod", _i, [_vp]),
     ("dsg_kepsmodel", _i, [_vp]),
+    ("dsg_calch3d", _i, [_vp]),
     ("dsg_checktime", _i, [_vp]),
     ("dsg_csf", _i, [_vp]),
     ("dsg_solvelpres", _i, [_vp, _i, C.POINTER(DsgMgStats)]),

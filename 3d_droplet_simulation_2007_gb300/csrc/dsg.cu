@@ -727,6 +727,10 @@ int dsg_create(const dsg_config *cfg, dsg_ctx **out) {
     return dsg::set_error(nullptr, DSG_E_ARG, "grid %dx%dx%d too small", cfg->nx, cfg->ny, cfg->nz);
   if (cfg->mode < 0 || cfg->mode > DSG_MODE_LEARNED)
     return dsg::set_error(nullptr, DSG_E_ARG, "unknown mode %d", cfg->mode);
+  if (cfg->surfacet != 2 && cfg->surfacet != 5)
+    return dsg::set_error(nullptr, DSG_E_ARG, "surfacet = %d is not available (2: CSF, 5: SGIP)", cfg->surfacet);
+  if (cfg->hswitch != 0 && cfg->hswitch != 1)
+    return dsg::set_error(nullptr, DSG_E_ARG, "hswitch = %d is not available (0 or 1)", cfg->hswitch);
   if (cfg->iturb != 0 && cfg->iturb != 3)
     return dsg::set_error(nullptr, DSG_E_ARG, "iturb = %d is not available (0: laminar, 3: k-epsilon)", cfg->iturb);
   // memoryaloc, main.f:284-298 (generalised to sides that are not 2^k+2)
@@ -756,7 +760,7 @@ int dsg_create(const dsg_config *cfg, dsg_ctx **out) {
   const size_t fine = up((size_t)cfg->nx * cfg->ny * cfg->nz * sizeof(double));
   const int nextra = DSG_NFIELDS - 8 + 1;  // fine fields beyond the level arrays + ccf
   total += nextra * fine;
-  total += up(dsg::kRedBlocks * 4 * sizeof(double)) + up(16 * sizeof(double));
+  total += up(dsg::kRedBlocks * 4 * sizeof(double)) + up(16 * sizeof(double)) + up(sizeof(unsigned long long));
   cudaError_t e = cudaMalloc(&ctx->arena, total);
   if (e != cudaSuccess) {
     int rc = dsg::cuda_fail(ctx, e, "cudaMalloc(arena)");
@@ -786,6 +790,8 @@ int dsg_create(const dsg_config *cfg, dsg_ctx **out) {
   ctx->red_partials = (double *)p;
   p += up(dsg::kRedBlocks * 4 * sizeof(double));
   ctx->red_out = (double *)p;
+  p += up(16 * sizeof(double));
+  ctx->stop_flag = (unsigned long long *)p;
   e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMallocHost(&ctx->red_host, 16 * sizeof(double));
   if (e == cudaSuccess) e = cudaMemsetAsync(ctx->arena, 0, total, ctx->own_stream);
@@ -996,8 +1002,39 @@ int dsg_checktime(dsg_ctx *ctx) {
 int dsg_csf(dsg_ctx *ctx) {
   if (!ctx) return DSG_E_ARG;
   Tensor S(ctx);
+  if (ctx->cfg.surfacet == 5) {
+    double *H[6];
+    for (int m = 0; m < 6; m++) H[m] = ctx->f[DSG_F_HXMIN + m];
+    DSG_CK(ctx, dsg::sgip(ctx->f[DSG_F_CC], ctx->f[DSG_F_P], ctx->f[DSG_F_RES], ctx->f[DSG_F_RHS], ctx->ccf, S.p, H,
+                          ctx->f[DSG_F_U], ctx->f[DSG_F_W], ctx->fine(), ctx->s.tau, ctx->s.sigma, ctx->s.h,
+                          ctx->stream));
+    return DSG_OK;
+  }
   DSG_CK(ctx, dsg::csf(ctx->f[DSG_F_CC], ctx->f[DSG_F_P], ctx->f[DSG_F_RES], ctx->f[DSG_F_RHS], ctx->ccf, S.p,
                        ctx->fine(), ctx->s.tau, ctx->s.sigma, ctx->s.h, ctx->stream));
+  return DSG_OK;
+}
+
+// CalcH3d (main.f:30 with hswitch = 1).  The reference STOPs when a cell
+// matches none of the polygon cases; here the step returns DSG_E_STATE.
+int dsg_calch3d(dsg_ctx *ctx) {
+  if (!ctx) return DSG_E_ARG;
+  double *H[6];
+  for (int m = 0; m < 6; m++) H[m] = ctx->f[DSG_F_HXMIN + m];
+  DSG_CK(ctx, cudaMemsetAsync(ctx->stop_flag, 0, sizeof(unsigned long long), ctx->stream));
+  DSG_CK(ctx, dsg::calch3d(H, ctx->f[DSG_F_CC], ctx->fine(), ctx->stop_flag, ctx->stream));
+  DSG_CK(ctx, cudaMemcpyAsync(ctx->red_host + 15, ctx->stop_flag, sizeof(unsigned long long),
+                              cudaMemcpyDeviceToHost, ctx->stream));
+  DSG_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  unsigned long long v;
+  memcpy(&v, ctx->red_host + 15, sizeof v);
+  if (v) {
+    const long long q = (long long)(v & ((1ull << 48) - 1));
+    const int i = (int)(q % ctx->nx) + 1, j = (int)((q / ctx->nx) % ctx->ny) + 1, k = (int)(q / ((long long)ctx->nx * ctx->ny)) + 1;
+    return dsg::set_error(ctx, DSG_E_STATE, "CalcH3d: %s at cell (%d,%d,%d)",
+                          (v >> 48) == 1 ? "NO MATCH CASES FOUND" : "PROBLEM finding MIN and MAX unit vector components",
+                          i, j, k);
+  }
   return DSG_OK;
 }
 
@@ -1078,6 +1115,10 @@ int dsg_step(dsg_ctx *ctx, int t, dsg_mg_stats *stats) {
   DSG_CK(ctx, phase_mark(ctx, 0));
   int rc = dsg_vofmethod(ctx);
   if (rc) return rc;
+  if (ctx->cfg.hswitch == 1) {
+    rc = dsg_calch3d(ctx);
+    if (rc) return rc;
+  }
   rc = dsg_kepsmodel(ctx);
   if (rc) return rc;
   DSG_CK(ctx, phase_mark(ctx, 1));

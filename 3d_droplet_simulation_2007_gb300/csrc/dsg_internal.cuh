@@ -132,6 +132,11 @@ cudaError_t divergence(double *out, const double *u, const double *v, const doub
                        cudaStream_t st);
 cudaError_t project(double *u, double *v, double *w, const double *p, const double *a, const double *b,
                     const double *c, Dims d, cudaStream_t st);
+// sgip.cu (interface heights and the SGIP force, surfacet = 5)
+cudaError_t calch3d(double *const H[6], const double *cc, Dims d, unsigned long long *err, cudaStream_t st);
+cudaError_t sgip(const double *ccc, double *w11, double *w22, double *w33, double *ccf, double *const S[6],
+                 double *const H[6], const double *u, const double *w, Dims d, double tau, double sigma, double h,
+                 cudaStream_t st);
 // turb.cu (k-epsilon, iturb = 3)
 cudaError_t keps_seed(double *ktur, double *eps, double *mut, const double *cc, const double *rhon,
                       const double *mun, Dims d, double k1, double k2, cudaStream_t st);
@@ -226,6 +231,7 @@ struct dsg_ctx {
   double *red_partials;       // reduction partials (kRedBlocks * 4 doubles)
   double *red_out;            // device reduction results (8 doubles)
   double *red_host;           // pinned host mirror of red_out
+  unsigned long long *stop_flag;  // device: first cell where CalcH3d would STOP (code << 48 | index)
   void *arena;
   size_t arena_bytes;
   cudaStream_t stream;

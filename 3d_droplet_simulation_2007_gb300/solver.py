@@ -137,6 +137,12 @@ class Solver:
     def vofmethod(self):
         self._ck(self.lib.dsg_vofmethod(self.ctx))
 
+    def calch3d(self):
+        self._ck(self.lib.dsg_calch3d(self.ctx))
+
+    def kepsmodel(self):
+        self._ck(self.lib.dsg_kepsmodel(self.ctx))
+
     def checktime(self):
         self._ck(self.lib.dsg_checktime(self.ctx))
 

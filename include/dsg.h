@@ -57,7 +57,13 @@ enum {
   DSG_F_KTUR = 21,  /* k-epsilon state (iturb = 3), COMMON /turbulence/ input.h:36-42 */
   DSG_F_EPS = 22,
   DSG_F_MUT = 23,
-  DSG_NFIELDS = 24
+  DSG_F_HXMIN = 24, /* interface heights of CalcH3d (hswitch = 1): hxmin, hxmax, hymin, hymax, */
+  DSG_F_HXMAX = 25, /* hzmin, hzmax (COMMON /NEWW/, input.h:91-95) */
+  DSG_F_HYMIN = 26,
+  DSG_F_HYMAX = 27,
+  DSG_F_HZMIN = 28,
+  DSG_F_HZMAX = 29,
+  DSG_NFIELDS = 30
 };
 
 /* The 38 positional values of inputdata.in (main.f:188-234) in file order,
@@ -148,7 +154,8 @@ int dsg_vofmethod(dsg_ctx *ctx);
 int dsg_kepsmodel(dsg_ctx *ctx); /* kepsmodel main.f:1888-2025 (iturb = 3; no-op for iturb = 0) */
 int dsg_checktime(dsg_ctx *ctx);
 /* csf(ccc,w11,w22,w33) main.f:2363-2481 */
-int dsg_csf(dsg_ctx *ctx);
+int dsg_csf(dsg_ctx *ctx); /* csf main.f:2363-2481 (surfacet = 2) or SGIP 2835-3026 (surfacet = 5) */
+int dsg_calch3d(dsg_ctx *ctx); /* CalcH3d main.f:1312-1810 (the step calls it when hswitch = 1) */
 /* solvelpres(cc,w1..w3,a,b,c,ei,t) main.f:3236-3439, pressure solve per mode */
 int dsg_solvelpres(dsg_ctx *ctx, int t, dsg_mg_stats *stats);
 /* mglin(r1,r2) main.f:3645-3763 on the resident fine rhs and coefficients */

@@ -35,6 +35,9 @@ struct ora_state {
   double *lv[32][8]; /* [level][CC,P,RES,RHS,A,B,C,EI] */
   double *u, *v, *w, *s11, *s22, *s33, *s12, *s13, *s23, *rhon, *mun;
   double *ktur, *eps, *mut; /* /turbulence/ (input.h:36-42); cmu is 0.09 everywhere for iturb = 3 */
+  double *hx0, *hx1, *hy0, *hy1, *hz0, *hz1; /* hxmin, hxmax, hymin, hymax, hzmin, hzmax of CalcH3d */
+  int error;                                 /* a STOP of the reference (CalcH3d), 0 = none */
+  long long error_cell;
 };
 
 static double *zalloc(size_t n) { return (double *)calloc(n, sizeof(double)); }
@@ -781,6 +784,278 @@ static void calcrho(ora_state *st) {
 
 /* VOFmethod, main.f:795-824 (laminar: fturbdif is not called) */
 /* ======================================================================= */
+/* interface heights (CalcH3d) and the SGIP surface-tension force            */
+/* ======================================================================= */
+
+static inline double cube(double x) { return x * x * x; }
+
+/* CalcH3d for one cell (main.f:1312-1770): Youngs normal from the 27-point
+ * stencil, the heights of the PLIC polygon on the cell faces in the five
+ * geometric cases of the ordered normal (n1 <= n2 <= n3), then assigned to the
+ * axes.  h[6] = hxmin, hxmax, hymin, hymax, hzmin, hzmax.  Returns 0, or 1
+ * for "NO MATCH CASES FOUND" and 2 for "PROBLEM finding MIN and MAX unit
+ * vector components" (the reference STOPs on both). */
+static int h3d_cell(const double *c, size_t q, size_t sy, size_t sz, double h[6]) {
+#define C(di, dj, dk) c[q + (long)(di) + (long)(dj) * (long)sy + (long)(dk) * (long)sz]
+  double mm1, mm2;
+  mm1 = C(-1, -1, -1) + C(-1, -1, 1) + C(-1, 1, -1) + C(-1, 1, 1) +
+        2.0 * (C(-1, -1, 0) + C(-1, 1, 0) + C(-1, 0, -1) + C(-1, 0, 1)) + 4.0 * C(-1, 0, 0);
+  mm2 = C(1, -1, -1) + C(1, -1, 1) + C(1, 1, -1) + C(1, 1, 1) +
+        2.0 * (C(1, -1, 0) + C(1, 1, 0) + C(1, 0, -1) + C(1, 0, 1)) + 4.0 * C(1, 0, 0);
+  const double normx = mm1 - mm2;
+  mm1 = C(-1, -1, -1) + C(-1, -1, 1) + C(1, -1, -1) + C(1, -1, 1) +
+        2.0 * (C(-1, -1, 0) + C(1, -1, 0) + C(0, -1, -1) + C(0, -1, 1)) + 4.0 * C(0, -1, 0);
+  mm2 = C(-1, 1, -1) + C(-1, 1, 1) + C(1, 1, -1) + C(1, 1, 1) +
+        2.0 * (C(-1, 1, 0) + C(1, 1, 0) + C(0, 1, -1) + C(0, 1, 1)) + 4.0 * C(0, 1, 0);
+  const double normy = mm1 - mm2;
+  mm1 = C(-1, -1, -1) + C(-1, 1, -1) + C(1, -1, -1) + C(1, 1, -1) +
+        2.0 * (C(-1, 0, -1) + C(1, 0, -1) + C(0, -1, -1) + C(0, 1, -1)) + 4.0 * C(0, 0, -1);
+  mm2 = C(-1, -1, 1) + C(-1, 1, 1) + C(1, -1, 1) + C(1, 1, 1) +
+        2.0 * (C(-1, 0, 1) + C(1, 0, 1) + C(0, -1, 1) + C(0, 1, 1)) + 4.0 * C(0, 0, 1);
+  const double normz = mm1 - mm2;
+  const double cc = C(0, 0, 0);
+#undef C
+  const double den = sqrt(normx * normx + normy * normy + normz * normz + 1.e-50);
+  const double nix = normx / den, niy = normy / den, niz = normz / den;
+  const double ccnew = cc > 0.5 ? 1.0 - cc : cc;
+  const double absxn = fabs(nix), absyn = fabs(niy), abszn = fabs(niz);
+  const double n1 = dmin1(dmin1(absxn, absyn), abszn);
+  const double n3 = dmax1(dmax1(absxn, absyn), abszn);
+  const double n2 = absxn + absyn + abszn - n1 - n3;
+  const double clim1 = sqrt(2.0 * ccnew * n3 * n2);
+  double h1a, h1b, h2a, h2b, h3a, h3b, s1, s2, s3, diag;
+  if (n1 == 0.0 && n2 > 0.0 && ccnew <= clim1) {
+    s2 = sqrt(2.0 * ccnew * n3 / n2);
+    s3 = sqrt(2.0 * ccnew * n2 / n3);
+    h1a = s2 * s3 / 2.0; h1b = s2 * s3 / 2.0;
+    h2a = s3; h2b = 0.0;
+    h3a = s2; h3b = 0.0;
+  } else if (n1 == 0.0 && n2 > 0.0 && ccnew > clim1) {
+    h1a = cc; h1b = cc;
+    h2a = cc + n2 / (2.0 * n3); h2b = cc - n2 / (2.0 * n3);
+    h3a = 1.0; h3b = 0.0;
+  } else if (n1 == 0.0 && n2 == 0.0) {
+    h1a = ccnew; h1b = ccnew; h2a = ccnew; h2b = ccnew;
+    h3a = 1.0; h3b = 0.0;
+  } else if (6.0 * n2 * n3 * ccnew < n1 * n1) {  /* triangle, case (a) */
+    diag = pow(6.0 * n1 * n2 * n3 * ccnew, 1.0 / 3.0);
+    s1 = diag / n1; s2 = diag / n2; s3 = diag / n3;
+    h1a = (s2 * s3) / 2.0; h1b = 0.0;
+    h2a = (s1 * s3) / 2.0; h2b = 0.0;
+    h3a = (s1 * s2) / 2.0; h3b = 0.0;
+  } else if (6.0 * n2 * n3 * ccnew < 3.0 * (n2 * n2) - 3.0 * n1 * n2 + n1 * n1) {  /* quadrilateral A, (b) */
+    diag = (3.0 * n1 + sqrt(72.0 * n2 * n3 * ccnew - 3.0 * (n1 * n1))) / 6.0;
+    s1 = diag / n1; s2 = diag / n2; s3 = diag / n3;
+    const double t = (s1 - 1.0) / s1;
+    h1a = (s2 * s3) / 2.0; h1b = (s2 * s3) / 2.0 * (t * t);
+    h2a = s3 * (2.0 * s1 - 1.0) / (2.0 * s1); h2b = 0.0;
+    h3a = s2 * (2.0 * s1 - 1.0) / (2.0 * s1); h3b = 0.0;
+  } else if ((n1 + n2 >= n3 && 6.0 * n1 * n2 * n3 * ccnew < cube(n3) - cube(n3 - n1) - cube(n3 - n2)) ||
+             (n1 + n2 < n3 && 2.0 * n3 * ccnew < n1 + n2)) {  /* pentagon, (c): Newton-Raphson */
+    const double rsixn3 = 1.0 / (6.0 * n1 * n2 * n3);
+    diag = n2;
+    for (int loop = 1; loop <= 1000; loop++) {
+      const double delta = -(rsixn3 * (cube(diag) - cube(diag - n1) - cube(diag - n2)) - ccnew) /
+                           (3.0 * rsixn3 * (diag * diag - (diag - n1) * (diag - n1) - (diag - n2) * (diag - n2)));
+      diag = diag + delta;
+      if (fabs(delta) < 1.e-6) break;
+    }
+    s1 = diag / n1; s2 = diag / n2; s3 = diag / n3;
+    const double t1 = (s1 - 1.0) / s1, t2 = (s2 - 1.0) / s2;
+    h1a = s3 * (2.0 * s2 - 1.0) / (2.0 * s2); h1b = (s2 * s3) / 2.0 * (t1 * t1);
+    h2a = s3 * (2.0 * s1 - 1.0) / (2.0 * s1); h2b = (s1 * s3) / 2.0 * (t2 * t2);
+    h3a = 2.0 * (s1 + s2) - s1 / s2 - s2 / s1 - s1 * s2 - 1.0; h3b = 0.0;
+  } else if ((n1 + n2 > n3) && 6.0 * n1 * n2 * n3 * ccnew >= cube(n3) - cube(n3 - n1) - cube(n3 - n2)) {
+    /* hexagon, (d): Newton-Raphson */
+    const double rsixn3 = 1.0 / (6.0 * n1 * n2 * n3);
+    diag = n3;
+    for (int loop = 1; loop <= 1000; loop++) {
+      const double delta =
+          -(rsixn3 * (cube(diag) - cube(diag - n1) - cube(diag - n2) - cube(diag - n3)) - ccnew) /
+          (3.0 * rsixn3 *
+           (diag * diag - (diag - n1) * (diag - n1) - (diag - n2) * (diag - n2) - (diag - n3) * (diag - n3)));
+      diag = diag + delta;
+      if (fabs(delta) < 1.e-6) break;
+    }
+    s1 = diag / n1; s2 = diag / n2; s3 = diag / n3;
+    const double t1 = (s1 - 1.0) / s1, t2 = (s2 - 1.0) / s2, t3 = (s3 - 1.0) / s3;
+    h1a = 2.0 * (s2 + s3) - s2 / s3 - s3 / s2 - s2 * s3 - 1.0; h1b = (s2 * s3) / 2.0 * (t1 * t1);
+    h2a = 2.0 * (s1 + s3) - s1 / s3 - s3 / s1 - s1 * s3 - 1.0; h2b = (s1 * s3) / 2.0 * (t2 * t2);
+    h3a = 2.0 * (s1 + s2) - s1 / s2 - s2 / s1 - s1 * s2 - 1.0; h3b = (s1 * s2) / 2.0 * (t3 * t3);
+  } else if ((n1 + n2 < n3) && 6.0 * n1 * n2 * n3 * ccnew >= cube(n1 + n2) - cube(n1) - cube(n2)) {
+    /* quadrilateral B, (e) */
+    diag = 0.5 * (n1 + n2) + ccnew * n3;
+    s1 = diag / n1; s2 = diag / n2; s3 = diag / n3;
+    h1a = s3 * (2.0 * s2 - 1.0) / (2.0 * s2); h1b = s3 * (2.0 * s2 - 1.0) * (s1 - 1.0) / (2.0 * s1 * s2);
+    h2a = s3 * (2.0 * s1 - 1.0) / (2.0 * s1); h2b = s3 * (2.0 * s1 - 1.0) * (s2 - 1.0) / (2.0 * s1 * s2);
+    h3a = 1.0; h3b = 0.0;
+  } else {
+    return 1;
+  }
+  if (cc > 0.5) {
+    h1a = 1.0 - h1a; h1b = 1.0 - h1b; h2a = 1.0 - h2a; h2b = 1.0 - h2b; h3a = 1.0 - h3a; h3b = 1.0 - h3b;
+  }
+  /* assignment to the axes (the branches of main.f:1586-1735, including
+   * their use of niz's sign for y when z carries the smallest component) */
+#define SET(lo, hi, n, a, b) do { if ((n) < 0) { lo = (a); hi = (b); } else { lo = (b); hi = (a); } } while (0)
+  double hx0 = 0, hx1 = 0, hy0 = 0, hy1 = 0, hz0 = 0, hz1 = 0;
+  if (absxn == n1) {
+    SET(hx0, hx1, nix, h1a, h1b);
+    if (fabs(absyn - n2) < 1.e-6) { SET(hy0, hy1, niy, h2a, h2b); SET(hz0, hz1, niz, h3a, h3b); }
+    else if (fabs(abszn - n2) < 1.e-6) { SET(hy0, hy1, niy, h3a, h3b); SET(hz0, hz1, niz, h2a, h2b); }
+    else return 2;
+  } else if (absyn == n1) {
+    SET(hy0, hy1, niy, h1a, h1b);
+    if (fabs(absxn - n2) < 1.e-6) { SET(hx0, hx1, nix, h2a, h2b); SET(hz0, hz1, niz, h3a, h3b); }
+    else if (fabs(abszn - n2) < 1.e-6) { SET(hx0, hx1, nix, h3a, h3b); SET(hz0, hz1, niz, h2a, h2b); }
+    else return 2;
+  } else if (abszn == n1) {
+    SET(hz0, hz1, niz, h1a, h1b);
+    if (fabs(absxn - n2) < 1.e-6) { SET(hx0, hx1, nix, h2a, h2b); SET(hy0, hy1, niz, h3a, h3b); }
+    else if (fabs(absyn - n2) < 1.e-6) { SET(hx0, hx1, nix, h3a, h3b); SET(hy0, hy1, niz, h2a, h2b); }
+    else return 2;
+  }
+#undef SET
+  if (cc <= 0.5) {
+    double t;
+    t = hx0; hx0 = hx1; hx1 = t;
+    t = hy0; hy0 = hy1; hy1 = t;
+    t = hz0; hz0 = hz1; hz1 = t;
+  }
+  double *o[6] = {&hx0, &hx1, &hy0, &hy1, &hz0, &hz1};
+  for (int m = 0; m < 6; m++) {
+    double v = *o[m];
+    if (v < 0.0) v = 0.0;
+    if (v > 1.0) v = 1.0;
+    h[m] = v;
+  }
+  return 0;
+}
+
+/* CalcH3d, main.f:1312-1810: heights of every interior cell; ghosts untouched. */
+int ora_calch3d(ora_state *st) {
+  const int nx = st->nx, ny = st->ny, nz = st->nz;
+  const double *cc = st->lv[st->s.ng][LCC];
+  double *H[6] = {st->hx0, st->hx1, st->hy0, st->hy1, st->hz0, st->hz1};
+  for (int k = 2; k <= nz - 1; k++)
+    for (int j = 2; j <= ny - 1; j++)
+      for (int i = 2; i <= nx - 1; i++) {
+        const size_t q = IX(i, j, k);
+        double h[6];
+        const int rc = h3d_cell(cc, q, (size_t)nx, (size_t)nx * ny, h);
+        if (rc) {
+          if (!st->error) { st->error = rc; st->error_cell = (long long)q; }
+          return rc;
+        }
+        for (int m = 0; m < 6; m++) H[m][q] = h[m];
+      }
+  return 0;
+}
+
+/* SGIP, main.f:2835-3026: CSF-type force with the curvature of the filtered
+ * volume fraction (the terms summed in SGIP's own order) weighted by the jump
+ * of the mean interface height between neighbouring cells; on the wall plane
+ * j = 2 a contact-angle model sets the direction.  Same scratch aliasing as
+ * csf: w11 = pressure array, w22 = residual array, w33 = rhs array. */
+void ora_sgip(ora_state *st) {
+  const int nx = st->nx, ny = st->ny, nz = st->nz, ng = st->s.ng;
+  const size_t n = (size_t)nx * ny * nz;
+  double *ccc = LV(ng, LCC), *w11 = LV(ng, LU), *w22 = LV(ng, LRES), *w33 = LV(ng, LRHS);
+  double *ccf = zalloc(n);
+  memcpy(ccf, ccc, n * sizeof(double));
+  ora_filterc27(ccf, w22, nx, ny, nz);
+  memcpy(ccf, w22, n * sizeof(double));
+  ora_bc_out(ccf, nx, ny, nz);
+  if (st->s.sigma == 0.0) {
+    memset(st->s11, 0, n * 8); memset(st->s22, 0, n * 8); memset(st->s33, 0, n * 8);
+    memset(st->s12, 0, n * 8); memset(st->s13, 0, n * 8); memset(st->s23, 0, n * 8);
+    free(ccf);
+    return;
+  }
+  const double tau = st->s.tau, h = st->s.h;
+  const double sigh = 0.5 * (tau * tau) * st->s.sigma / (h * h * h);
+  for (int j = 2; j <= ny - 1; j++)
+    for (int i = 2; i <= nx - 1; i++)
+      for (int k = 2; k <= nz - 1; k++) {
+#define F(di, dj, dk) ccf[IX(i + (di), j + (dj), k + (dk))]
+        double t0, t1, t2;
+        t0 = F(1, 0, 0) - F(0, 0, 0);
+        t1 = F(0, 1, 0) - F(0, -1, 0) + F(1, 1, 0) - F(1, -1, 0);
+        t2 = F(0, 0, 1) - F(0, 0, -1) + F(1, 0, 1) - F(1, 0, -1);
+        const double nxu = sqrt(t0 * t0 + 0.0625 * (t1 * t1) + 0.0625 * (t2 * t2) + 1.e-50);
+        t0 = F(0, 0, 0) - F(-1, 0, 0);
+        t1 = F(-1, 1, 0) - F(-1, -1, 0) + F(0, 1, 0) - F(0, -1, 0);
+        t2 = F(-1, 0, 1) - F(-1, 0, -1) + F(0, 0, 1) - F(0, 0, -1);
+        const double nxd = sqrt(t0 * t0 + 0.0625 * (t1 * t1) + 0.0625 * (t2 * t2) + 1.e-50);
+        t0 = F(0, 1, 0) - F(0, 0, 0);
+        t1 = F(1, 1, 0) - F(-1, 1, 0) + F(1, 0, 0) - F(-1, 0, 0);
+        t2 = F(0, 1, 1) - F(0, 1, -1) + F(0, 0, 1) - F(0, 0, -1);
+        const double nyu = sqrt(t0 * t0 + 0.0625 * (t1 * t1) + 0.0625 * (t2 * t2) + 1.e-50);
+        t0 = F(0, 0, 0) - F(0, -1, 0);
+        t1 = F(1, 0, 0) - F(-1, 0, 0) + F(1, -1, 0) - F(-1, -1, 0);
+        t2 = F(0, 0, 1) - F(0, 0, -1) + F(0, -1, 1) - F(0, -1, -1);
+        const double nyd = sqrt(t0 * t0 + 0.0625 * (t1 * t1) + 0.0625 * (t2 * t2) + 1.e-50);
+        t0 = F(0, 0, 1) - F(0, 0, 0);
+        t1 = F(1, 0, 0) - F(-1, 0, 0) + F(1, 0, 1) - F(-1, 0, 1);
+        t2 = F(0, 1, 0) - F(0, -1, 0) + F(0, 1, 1) - F(0, -1, 1);
+        const double nzu = sqrt(t0 * t0 + 0.0625 * (t1 * t1) + 0.0625 * (t2 * t2) + 1.e-50);
+        t0 = F(0, 0, 0) - F(0, 0, -1);
+        t1 = F(1, 0, -1) - F(-1, 0, -1) + F(1, 0, 0) - F(-1, 0, 0);
+        t2 = F(0, 1, -1) - F(0, -1, -1) + F(0, 1, 0) - F(0, -1, 0);
+        const double nzd = sqrt(t0 * t0 + 0.0625 * (t1 * t1) + 0.0625 * (t2 * t2) + 1.e-50);
+        const double d1x = (F(1, 0, 0) - F(0, 0, 0)) / nxu;
+        const double d2x = (F(0, 0, 0) - F(-1, 0, 0)) / nxd;
+        const double d1y = (F(0, 1, 0) - F(0, 0, 0)) / nyu;
+        const double d2y = (F(0, 0, 0) - F(0, -1, 0)) / nyd;
+        const double d1z = (F(0, 0, 1) - F(0, 0, 0)) / nzu;
+        const double d2z = (F(0, 0, 0) - F(0, 0, -1)) / nzd;
+#undef F
+        w11[IX(i, j, k)] = -(d1x - d2x + d1y - d2y + d1z - d2z);
+      }
+  ora_bc_out(w11, nx, ny, nz);
+  const size_t sy = (size_t)nx, sz = (size_t)nx * ny;
+  for (int k = 2; k <= nz - 1; k++)
+    for (int j = 2; j <= ny - 1; j++)
+      for (int i = 2; i <= nx - 1; i++) {
+        const size_t q = IX(i, j, k);
+        const double Lx = (st->hx1[q] + st->hx0[q]) / 2.0, Lxd = (st->hx1[q - 1] + st->hx0[q - 1]) / 2.0;
+        const double Ly = (st->hy1[q] + st->hy0[q]) / 2.0, Lyd = (st->hy1[q - sy] + st->hy0[q - sy]) / 2.0;
+        const double Lz = (st->hz1[q] + st->hz0[q]) / 2.0, Lzd = (st->hz1[q - sz] + st->hz0[q - sz]) / 2.0;
+        st->s11[q] = sigh * (w11[q] + w11[q - 1]) * (ccf[q + 1] - ccf[q - 1]) * fabs(Lx - Lxd) / 2.0;
+        st->s22[q] = sigh * (w11[q] + w11[q - sy]) * (ccf[q + sy] - ccf[q - sy]) * fabs(Ly - Lyd) / 2.0;
+        st->s33[q] = sigh * (w11[q] + w11[q - sz]) * (ccf[q + sz] - ccf[q - sz]) * fabs(Lz - Lzd) / 2.0;
+        if (j == 2) {
+          /* contact angle from the contact-line speed (degrees; dsind/dcosd) */
+          const double mx = ccf[q + 1] - ccf[q - 1], mz = ccf[q + sz] - ccf[q - sz];
+          const double mmx = mx / sqrt(mz * mz + mx * mx + 1.e-50), mmz = mz / sqrt(mz * mz + mx * mx + 1.e-50);
+          double normv = mmx * st->u[q] + mmz * st->w[q];
+          normv = -normv;
+          double theta;
+          if (fabs(normv) > (double)0.1f) theta = normv > 0 ? 115.0 : 45.0;
+          else theta = 350.0 * normv + 80.0;
+          const double my = ccf[q + sy] - ccf[q - sy];
+          const double rad = theta * (3.14159265358979323846 / 180.0);
+          const double sind = sin(rad), mmy = cos(rad);
+          st->s11[q] = sigh * (w11[q] + w11[q - 1]) * mx * sind / 2.0;
+          st->s22[q] = sigh * (w11[q] + w11[q - sy]) * mmy * sqrt(mz * mz + mx * mx + my * my) * -1.0;
+          st->s33[q] = sigh * (w11[q] + w11[q - sz]) * mz * sind / 2.0;
+        }
+      }
+  ora_bc_out(st->s11, nx, ny, nz);
+  ora_bc_out(st->s22, nx, ny, nz);
+  ora_bc_out(st->s33, nx, ny, nz);
+  memcpy(w11, st->s11, n * 8);
+  memcpy(w22, st->s22, n * 8);
+  memcpy(w33, st->s33, n * 8);
+  free(ccf);
+}
+
+int ora_error(const ora_state *st, long long *cell) {
+  if (cell) *cell = st->error_cell;
+  return st->error;
+}
+
+/* ======================================================================= */
 /* k-epsilon turbulence (iturb = 3)                                          */
 /* ======================================================================= */
 
@@ -1348,6 +1623,8 @@ ora_state *ora_create(const ora_input *in) {
   st->s12 = zalloc(n); st->s13 = zalloc(n); st->s23 = zalloc(n);
   st->rhon = zalloc(n); st->mun = zalloc(n);
   st->ktur = zalloc(n); st->eps = zalloc(n); st->mut = zalloc(n);
+  st->hx0 = zalloc(n); st->hx1 = zalloc(n); st->hy0 = zalloc(n);
+  st->hy1 = zalloc(n); st->hz0 = zalloc(n); st->hz1 = zalloc(n);
   st->s.npre = in->npre; st->s.npost = in->npost; st->s.ntop = in->ntop; st->s.cycles = in->cycles;
   st->s.last_epsdiv = -1.0;
   nondim(st);
@@ -1380,6 +1657,7 @@ void ora_destroy(ora_state *st) {
   free(st->s11); free(st->s22); free(st->s33); free(st->s12); free(st->s13); free(st->s23);
   free(st->rhon); free(st->mun);
   free(st->ktur); free(st->eps); free(st->mut);
+  free(st->hx0); free(st->hx1); free(st->hy0); free(st->hy1); free(st->hz0); free(st->hz1);
   free(st);
 }
 
@@ -1412,6 +1690,12 @@ double *ora_field(ora_state *st, int id) {
     case ORA_KTUR: return st->ktur;
     case ORA_EPS: return st->eps;
     case ORA_MUT: return st->mut;
+    case ORA_HXMIN: return st->hx0;
+    case ORA_HXMAX: return st->hx1;
+    case ORA_HYMIN: return st->hy0;
+    case ORA_HYMAX: return st->hy1;
+    case ORA_HZMIN: return st->hz0;
+    case ORA_HZMAX: return st->hz1;
     default: return NULL;
   }
 }
@@ -1428,15 +1712,19 @@ void ora_level_dims(const ora_state *st, int level, int *nx, int *ny, int *nz) {
 void ora_get_scalars(const ora_state *st, ora_scalars *out) { *out = st->s; }
 void ora_set_scalars(ora_state *st, const ora_scalars *in) { st->s = *in; }
 
-/* main.f:19-73 loop body for surfacet=2 (CSF), hswitch=0, laminar */
+/* main.f:19-73 loop body: VOFmethod, CalcH3d (hswitch = 1), kepsmodel
+ * (iturb = 3), checktime, csf (surfacet = 2) or SGIP (surfacet = 5),
+ * solvelpres.  A STOP of CalcH3d ends the step (ora_error reports it). */
 void ora_kepsmodel(ora_state *st) {
   if (st->in.iturb == 3) kepsmodel(st);
 }
 
 void ora_step(ora_state *st, int t) {
   ora_vofmethod(st);
+  if (st->in.hswitch == 1 && ora_calch3d(st)) return;
   ora_kepsmodel(st);
   ora_checktime(st);
-  ora_csf(st);
+  if (st->in.surfacet == 5) ora_sgip(st);
+  else ora_csf(st);
   ora_solvelpres(st, t);
 }

@@ -34,7 +34,9 @@ enum {
   ORA_S22 = 12, ORA_S33 = 13, ORA_S12 = 14, ORA_S13 = 15, ORA_S23 = 16,
   ORA_RHON = 17, ORA_MUN = 18, ORA_NFIELDS = 19,
   /* k-epsilon state (iturb = 3); 19, 20 are the GPU build's pressure history */
-  ORA_KTUR = 21, ORA_EPS = 22, ORA_MUT = 23
+  ORA_KTUR = 21, ORA_EPS = 22, ORA_MUT = 23,
+  /* interface heights of CalcH3d (hswitch = 1) */
+  ORA_HXMIN = 24, ORA_HXMAX = 25, ORA_HYMIN = 26, ORA_HYMAX = 27, ORA_HZMIN = 28, ORA_HZMAX = 29
 };
 
 /* Pressure-solver modes. */
@@ -96,10 +98,13 @@ void ora_set_scalars(ora_state *st, const ora_scalars *in);
 void ora_vofmethod(ora_state *st);        /* main.f:795-824 (+ fturbdif 1239-1267 when iturb != 0) */
 void ora_kepsmodel(ora_state *st);        /* main.f:1888-2025 when iturb = 3, else nothing */
 void ora_checktime(ora_state *st);        /* main.f:2152-2171 */
+int ora_calch3d(ora_state *st);           /* main.f:1312-1810; nonzero: the reference STOPs */
+void ora_sgip(ora_state *st);             /* main.f:2835-3026 */
+int ora_error(const ora_state *st, long long *cell); /* STOP code of the last step (0: none) */
 void ora_csf(ora_state *st);              /* main.f:2363-2481 */
 void ora_solvelpres(ora_state *st, int t); /* main.f:3236-3439 */
 void ora_mglin(ora_state *st);            /* main.f:3645-3763 (+ tol mode) */
-void ora_step(ora_state *st, int t);      /* main.f:19-73 loop body, CSF, laminar or k-epsilon */
+void ora_step(ora_state *st, int t);      /* main.f:19-73 loop body (CSF or SGIP, laminar or k-epsilon) */
 double ora_relres(ora_state *st);         /* ||rhs - L p|| / ||rhs|| on the fine level */
 
 /* ---- array-level routines (reference subroutine interfaces) ------------- */

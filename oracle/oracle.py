@@ -14,7 +14,8 @@ from . import build as _build
 FIELDS = ["cc", "p", "res", "rhs", "a", "b", "c", "ei", "u", "v", "w",
           "s11", "s22", "s33", "s12", "s13", "s23", "rhon", "mun"]
 FIELD_ID = {n: i for i, n in enumerate(FIELDS)}
-FIELD_ID.update({"ktur": 21, "eps": 22, "mut": 23})
+FIELD_ID.update({"ktur": 21, "eps": 22, "mut": 23, "hxmin": 24, "hxmax": 25, "hymin": 26, "hymax": 27,
+                 "hzmin": 28, "hzmax": 29})
 
 MODE_REF_EXACT = 0
 MODE_TOL_FP64 = 1
@@ -77,7 +78,11 @@ def load():
     lib.ora_level_dims.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
     lib.ora_get_scalars.argtypes = [vp, C.POINTER(OracleScalars)]
     lib.ora_set_scalars.argtypes = [vp, C.POINTER(OracleScalars)]
-    for fn in ("ora_vofmethod", "ora_kepsmodel", "ora_checktime", "ora_csf", "ora_mglin"):
+    lib.ora_calch3d.argtypes = [vp]
+    lib.ora_calch3d.restype = C.c_int
+    lib.ora_error.argtypes = [vp, C.POINTER(C.c_longlong)]
+    lib.ora_error.restype = C.c_int
+    for fn in ("ora_vofmethod", "ora_kepsmodel", "ora_checktime", "ora_csf", "ora_sgip", "ora_mglin"):
         getattr(lib, fn).argtypes = [vp]
     lib.ora_solvelpres.argtypes = [vp, C.c_int]
     lib.ora_step.argtypes = [vp, C.c_int]
@@ -185,6 +190,16 @@ class Oracle:
 
     def kepsmodel(self):
         self.lib.ora_kepsmodel(self.h)
+
+    def calch3d(self):
+        return self.lib.ora_calch3d(self.h)
+
+    def sgip(self):
+        self.lib.ora_sgip(self.h)
+
+    def error(self):
+        cell = C.c_longlong()
+        return self.lib.ora_error(self.h, C.byref(cell)), cell.value
 
     def checktime(self):
         self.lib.ora_checktime(self.h)
