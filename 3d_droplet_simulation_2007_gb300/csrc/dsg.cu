@@ -727,8 +727,9 @@ int dsg_create(const dsg_config *cfg, dsg_ctx **out) {
     return dsg::set_error(nullptr, DSG_E_ARG, "grid %dx%dx%d too small", cfg->nx, cfg->ny, cfg->nz);
   if (cfg->mode < 0 || cfg->mode > DSG_MODE_LEARNED)
     return dsg::set_error(nullptr, DSG_E_ARG, "unknown mode %d", cfg->mode);
-  if (cfg->surfacet != 2 && cfg->surfacet != 5)
-    return dsg::set_error(nullptr, DSG_E_ARG, "surfacet = %d is not available (2: CSF, 5: SGIP)", cfg->surfacet);
+  if (cfg->surfacet != 2 && cfg->surfacet != 5 && cfg->surfacet != 6)
+    return dsg::set_error(nullptr, DSG_E_ARG, "surfacet = %d is not available (2: CSF, 5: SGIP, 6: SGIP2)",
+                          cfg->surfacet);
   if (cfg->hswitch != 0 && cfg->hswitch != 1)
     return dsg::set_error(nullptr, DSG_E_ARG, "hswitch = %d is not available (0 or 1)", cfg->hswitch);
   if (cfg->iturb != 0 && cfg->iturb != 3)
@@ -1002,12 +1003,16 @@ int dsg_checktime(dsg_ctx *ctx) {
 int dsg_csf(dsg_ctx *ctx) {
   if (!ctx) return DSG_E_ARG;
   Tensor S(ctx);
-  if (ctx->cfg.surfacet == 5) {
+  if (ctx->cfg.surfacet == 5 || ctx->cfg.surfacet == 6) {
     double *H[6];
     for (int m = 0; m < 6; m++) H[m] = ctx->f[DSG_F_HXMIN + m];
-    DSG_CK(ctx, dsg::sgip(ctx->f[DSG_F_CC], ctx->f[DSG_F_P], ctx->f[DSG_F_RES], ctx->f[DSG_F_RHS], ctx->ccf, S.p, H,
-                          ctx->f[DSG_F_U], ctx->f[DSG_F_W], ctx->fine(), ctx->s.tau, ctx->s.sigma, ctx->s.h,
-                          ctx->stream));
+    if (ctx->cfg.surfacet == 5)
+      DSG_CK(ctx, dsg::sgip(ctx->f[DSG_F_CC], ctx->f[DSG_F_P], ctx->f[DSG_F_RES], ctx->f[DSG_F_RHS], ctx->ccf, S.p,
+                            H, ctx->f[DSG_F_U], ctx->f[DSG_F_W], ctx->fine(), ctx->s.tau, ctx->s.sigma, ctx->s.h,
+                            ctx->stream));
+    else
+      DSG_CK(ctx, dsg::sgip2(ctx->f[DSG_F_CC], ctx->f[DSG_F_P], ctx->f[DSG_F_RES], ctx->f[DSG_F_RHS], ctx->ccf, S.p,
+                             H, ctx->fine(), ctx->s.tau, ctx->s.sigma, ctx->s.h, ctx->stream));
     return DSG_OK;
   }
   DSG_CK(ctx, dsg::csf(ctx->f[DSG_F_CC], ctx->f[DSG_F_P], ctx->f[DSG_F_RES], ctx->f[DSG_F_RHS], ctx->ccf, S.p,

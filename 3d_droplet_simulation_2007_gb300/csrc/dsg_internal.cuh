@@ -137,6 +137,8 @@ cudaError_t calch3d(double *const H[6], const double *cc, Dims d, unsigned long 
 cudaError_t sgip(const double *ccc, double *w11, double *w22, double *w33, double *ccf, double *const S[6],
                  double *const H[6], const double *u, const double *w, Dims d, double tau, double sigma, double h,
                  cudaStream_t st);
+cudaError_t sgip2(const double *ccc, double *w11, double *w22, double *w33, double *ccf, double *const S[6],
+                  double *const H[6], Dims d, double tau, double sigma, double h, cudaStream_t st);
 // turb.cu (k-epsilon, iturb = 3)
 cudaError_t keps_seed(double *ktur, double *eps, double *mut, const double *cc, const double *rhon,
                       const double *mun, Dims d, double k1, double k2, cudaStream_t st);

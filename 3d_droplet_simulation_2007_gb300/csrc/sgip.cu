@@ -1,6 +1,7 @@
 // sgip.cu -- interface heights (CalcH3d, main.f:1312-1810) and the SGIP
-// surface-tension force (main.f:2835-3026): the reference's default surface
-// tension (surfacet = 5 with hswitch = 1 in its inputdata.in).  FP64 without
+// surface-tension forces (SGIP, main.f:2835-3026: the reference's default
+// surface tension, surfacet = 5 with hswitch = 1 in its inputdata.in; SGIP2,
+// main.f:3029-3166, surfacet = 6).  FP64 without
 // FP contraction, the reference's operation order: the height case chosen for
 // a cell depends on exact comparisons, so the arithmetic matches the oracle's
 // bit for bit.
@@ -312,6 +313,25 @@ __global__ void k_sgip_force(double *__restrict__ s11, double *__restrict__ s22,
   s33[q] = sigh * (kap[q] + kap[q - sz]) * mz * sind / 2.0;
 }
 
+// SGIP2's face forces (main.f:3124-3140): central differences of the mean
+// heights, no wall model.
+__global__ void k_sgip2_force(double *__restrict__ s11, double *__restrict__ s22, double *__restrict__ s33,
+                              const double *__restrict__ f, const double *__restrict__ kap, Heights H, Dims d,
+                              double sigh) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
+  const int k = blockIdx.z + 2;
+  if (i > d.nx - 1 || j > d.ny - 1) return;
+  const size_t q = d.ix(i, j, k);
+  const size_t sy = d.sy(), sz = d.sz();
+  const double Lxu = (H.p[1][q + 1] + H.p[0][q + 1]) / 2.0, Lxd = (H.p[1][q - 1] + H.p[0][q - 1]) / 2.0;
+  const double Lyu = (H.p[3][q + sy] + H.p[2][q + sy]) / 2.0, Lyd = (H.p[3][q - sy] + H.p[2][q - sy]) / 2.0;
+  const double Lzu = (H.p[5][q + sz] + H.p[4][q + sz]) / 2.0, Lzd = (H.p[5][q - sz] + H.p[4][q - sz]) / 2.0;
+  s11[q] = sigh * (kap[q + 1] + kap[q - 1]) * (f[q + 1] - f[q - 1]) * (Lxu - Lxd) * 0.25;
+  s22[q] = sigh * (kap[q + sy] + kap[q - sy]) * (f[q + sy] - f[q - sy]) * (Lyu - Lyd) * 0.25;
+  s33[q] = sigh * (kap[q + sz] + kap[q - sz]) * (f[q + sz] - f[q - sz]) * (Lzu - Lzd) * 0.25;
+}
+
 const dim3 kBlk(32, 4, 1);
 
 }  // namespace
@@ -321,6 +341,34 @@ cudaError_t calch3d(double *const H[6], const double *cc, Dims d, unsigned long 
   for (int m = 0; m < 6; m++) h.p[m] = H[m];
   DSG_COUNT k_calch3d<<<interior_grid(d, kBlk), kBlk, 0, st>>>(h, cc, d, err);
   return cudaGetLastError();
+}
+
+// SGIP2 (main.f:3029-3166): three filter passes (each filterc27 into the
+// residual array, copied back, bc_out), sigh = 0.5 tau sigma / h^2, SGIP's
+// curvature, SGIP2's forces.
+cudaError_t sgip2(const double *ccc, double *w11, double *w22, double *w33, double *ccf, double *const S[6],
+                  double *const H[6], Dims d, double tau, double sigma, double h, cudaStream_t st) {
+  const size_t bytes = d.count() * sizeof(double);
+  cudaError_t e;
+  for (int pass = 0; pass < 3; pass++) {
+    if ((e = filterc27(pass == 0 ? ccc : ccf, w22, d, st)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(ccf, w22, bytes, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
+    if ((e = bc_out(ccf, d, st)) != cudaSuccess) return e;
+  }
+  if (sigma == 0.0) {
+    for (int m = 0; m < 6; m++)
+      if ((e = cudaMemsetAsync(S[m], 0, bytes, st)) != cudaSuccess) return e;
+    return cudaSuccess;
+  }
+  const double sigh = 0.5 * tau * sigma / (h * h);
+  DSG_COUNT k_sgip_curvature<<<interior_grid(d, kBlk), kBlk, 0, st>>>(w11, ccf, d);
+  if ((e = bc_out(w11, d, st)) != cudaSuccess) return e;
+  Heights hh;
+  for (int m = 0; m < 6; m++) hh.p[m] = H[m];
+  DSG_COUNT k_sgip2_force<<<interior_grid(d, kBlk), kBlk, 0, st>>>(S[0], S[1], S[2], ccf, w11, hh, d, sigh);
+  if ((e = cudaMemcpyAsync(w11, S[0], bytes, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyAsync(w22, S[1], bytes, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
+  return cudaMemcpyAsync(w33, S[2], bytes, cudaMemcpyDeviceToDevice, st);
 }
 
 // SGIP with the reference's scratch aliasing (as csf): w11 = pressure array,

@@ -154,7 +154,8 @@ int dsg_vofmethod(dsg_ctx *ctx);
 int dsg_kepsmodel(dsg_ctx *ctx); /* kepsmodel main.f:1888-2025 (iturb = 3; no-op for iturb = 0) */
 int dsg_checktime(dsg_ctx *ctx);
 /* csf(ccc,w11,w22,w33) main.f:2363-2481 */
-int dsg_csf(dsg_ctx *ctx); /* csf main.f:2363-2481 (surfacet = 2) or SGIP 2835-3026 (surfacet = 5) */
+/* csf main.f:2363-2481 (surfacet = 2), SGIP 2835-3026 (surfacet = 5) or SGIP2 3029-3166 (surfacet = 6) */
+int dsg_csf(dsg_ctx *ctx);
 int dsg_calch3d(dsg_ctx *ctx); /* CalcH3d main.f:1312-1810 (the step calls it when hswitch = 1) */
 /* solvelpres(cc,w1..w3,a,b,c,ei,t) main.f:3236-3439, pressure solve per mode */
 int dsg_solvelpres(dsg_ctx *ctx, int t, dsg_mg_stats *stats);

@@ -952,28 +952,9 @@ int ora_calch3d(ora_state *st) {
   return 0;
 }
 
-/* SGIP, main.f:2835-3026: CSF-type force with the curvature of the filtered
- * volume fraction (the terms summed in SGIP's own order) weighted by the jump
- * of the mean interface height between neighbouring cells; on the wall plane
- * j = 2 a contact-angle model sets the direction.  Same scratch aliasing as
- * csf: w11 = pressure array, w22 = residual array, w33 = rhs array. */
-void ora_sgip(ora_state *st) {
-  const int nx = st->nx, ny = st->ny, nz = st->nz, ng = st->s.ng;
-  const size_t n = (size_t)nx * ny * nz;
-  double *ccc = LV(ng, LCC), *w11 = LV(ng, LU), *w22 = LV(ng, LRES), *w33 = LV(ng, LRHS);
-  double *ccf = zalloc(n);
-  memcpy(ccf, ccc, n * sizeof(double));
-  ora_filterc27(ccf, w22, nx, ny, nz);
-  memcpy(ccf, w22, n * sizeof(double));
-  ora_bc_out(ccf, nx, ny, nz);
-  if (st->s.sigma == 0.0) {
-    memset(st->s11, 0, n * 8); memset(st->s22, 0, n * 8); memset(st->s33, 0, n * 8);
-    memset(st->s12, 0, n * 8); memset(st->s13, 0, n * 8); memset(st->s23, 0, n * 8);
-    free(ccf);
-    return;
-  }
-  const double tau = st->s.tau, h = st->s.h;
-  const double sigh = 0.5 * (tau * tau) * st->s.sigma / (h * h * h);
+/* SGIP's (and SGIP2's) curvature: csf's formula with the transverse
+ * differences summed in SGIP's order (main.f:2880-2913, 3064-3097). */
+static void sgip_curvature(double *w11, const double *ccf, int nx, int ny, int nz) {
   for (int j = 2; j <= ny - 1; j++)
     for (int i = 2; i <= nx - 1; i++)
       for (int k = 2; k <= nz - 1; k++) {
@@ -1012,6 +993,31 @@ void ora_sgip(ora_state *st) {
 #undef F
         w11[IX(i, j, k)] = -(d1x - d2x + d1y - d2y + d1z - d2z);
       }
+}
+
+/* SGIP, main.f:2835-3026: CSF-type force with the curvature of the filtered
+ * volume fraction (the terms summed in SGIP's own order) weighted by the jump
+ * of the mean interface height between neighbouring cells; on the wall plane
+ * j = 2 a contact-angle model sets the direction.  Same scratch aliasing as
+ * csf: w11 = pressure array, w22 = residual array, w33 = rhs array. */
+void ora_sgip(ora_state *st) {
+  const int nx = st->nx, ny = st->ny, nz = st->nz, ng = st->s.ng;
+  const size_t n = (size_t)nx * ny * nz;
+  double *ccc = LV(ng, LCC), *w11 = LV(ng, LU), *w22 = LV(ng, LRES), *w33 = LV(ng, LRHS);
+  double *ccf = zalloc(n);
+  memcpy(ccf, ccc, n * sizeof(double));
+  ora_filterc27(ccf, w22, nx, ny, nz);
+  memcpy(ccf, w22, n * sizeof(double));
+  ora_bc_out(ccf, nx, ny, nz);
+  if (st->s.sigma == 0.0) {
+    memset(st->s11, 0, n * 8); memset(st->s22, 0, n * 8); memset(st->s33, 0, n * 8);
+    memset(st->s12, 0, n * 8); memset(st->s13, 0, n * 8); memset(st->s23, 0, n * 8);
+    free(ccf);
+    return;
+  }
+  const double tau = st->s.tau, h = st->s.h;
+  const double sigh = 0.5 * (tau * tau) * st->s.sigma / (h * h * h);
+  sgip_curvature(w11, ccf, nx, ny, nz);
   ora_bc_out(w11, nx, ny, nz);
   const size_t sy = (size_t)nx, sz = (size_t)nx * ny;
   for (int k = 2; k <= nz - 1; k++)
@@ -1044,6 +1050,48 @@ void ora_sgip(ora_state *st) {
   ora_bc_out(st->s11, nx, ny, nz);
   ora_bc_out(st->s22, nx, ny, nz);
   ora_bc_out(st->s33, nx, ny, nz);
+  memcpy(w11, st->s11, n * 8);
+  memcpy(w22, st->s22, n * 8);
+  memcpy(w33, st->s33, n * 8);
+  free(ccf);
+}
+
+/* SGIP2, main.f:3029-3166: three filter passes, sigh = 0.5 tau sigma / h^2,
+ * SGIP's curvature, central differences of the mean heights (no wall model,
+ * no bc_out of the forces). */
+void ora_sgip2(ora_state *st) {
+  const int nx = st->nx, ny = st->ny, nz = st->nz, ng = st->s.ng;
+  const size_t n = (size_t)nx * ny * nz;
+  double *ccc = LV(ng, LCC), *w11 = LV(ng, LU), *w22 = LV(ng, LRES), *w33 = LV(ng, LRHS);
+  double *ccf = zalloc(n);
+  memcpy(ccf, ccc, n * sizeof(double));
+  for (int pass = 0; pass < 3; pass++) {
+    ora_filterc27(ccf, w22, nx, ny, nz);
+    memcpy(ccf, w22, n * sizeof(double));
+    ora_bc_out(ccf, nx, ny, nz);
+  }
+  if (st->s.sigma == 0.0) {
+    memset(st->s11, 0, n * 8); memset(st->s22, 0, n * 8); memset(st->s33, 0, n * 8);
+    memset(st->s12, 0, n * 8); memset(st->s13, 0, n * 8); memset(st->s23, 0, n * 8);
+    free(ccf);
+    return;
+  }
+  const double tau = st->s.tau, h = st->s.h;
+  const double sigh = 0.5 * tau * st->s.sigma / (h * h);
+  sgip_curvature(w11, ccf, nx, ny, nz);
+  ora_bc_out(w11, nx, ny, nz);
+  const size_t sy = (size_t)nx, sz = (size_t)nx * ny;
+  for (int k = 2; k <= nz - 1; k++)
+    for (int j = 2; j <= ny - 1; j++)
+      for (int i = 2; i <= nx - 1; i++) {
+        const size_t q = IX(i, j, k);
+        const double Lxu = (st->hx1[q + 1] + st->hx0[q + 1]) / 2.0, Lxd = (st->hx1[q - 1] + st->hx0[q - 1]) / 2.0;
+        const double Lyu = (st->hy1[q + sy] + st->hy0[q + sy]) / 2.0, Lyd = (st->hy1[q - sy] + st->hy0[q - sy]) / 2.0;
+        const double Lzu = (st->hz1[q + sz] + st->hz0[q + sz]) / 2.0, Lzd = (st->hz1[q - sz] + st->hz0[q - sz]) / 2.0;
+        st->s11[q] = sigh * (w11[q + 1] + w11[q - 1]) * (ccf[q + 1] - ccf[q - 1]) * (Lxu - Lxd) * 0.25;
+        st->s22[q] = sigh * (w11[q + sy] + w11[q - sy]) * (ccf[q + sy] - ccf[q - sy]) * (Lyu - Lyd) * 0.25;
+        st->s33[q] = sigh * (w11[q + sz] + w11[q - sz]) * (ccf[q + sz] - ccf[q - sz]) * (Lzu - Lzd) * 0.25;
+      }
   memcpy(w11, st->s11, n * 8);
   memcpy(w22, st->s22, n * 8);
   memcpy(w33, st->s33, n * 8);
@@ -1725,6 +1773,7 @@ void ora_step(ora_state *st, int t) {
   ora_kepsmodel(st);
   ora_checktime(st);
   if (st->in.surfacet == 5) ora_sgip(st);
+  else if (st->in.surfacet == 6) ora_sgip2(st);
   else ora_csf(st);
   ora_solvelpres(st, t);
 }

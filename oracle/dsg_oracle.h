@@ -100,6 +100,7 @@ void ora_kepsmodel(ora_state *st);        /* main.f:1888-2025 when iturb = 3, el
 void ora_checktime(ora_state *st);        /* main.f:2152-2171 */
 int ora_calch3d(ora_state *st);           /* main.f:1312-1810; nonzero: the reference STOPs */
 void ora_sgip(ora_state *st);             /* main.f:2835-3026 */
+void ora_sgip2(ora_state *st);            /* main.f:3029-3166 */
 int ora_error(const ora_state *st, long long *cell); /* STOP code of the last step (0: none) */
 void ora_csf(ora_state *st);              /* main.f:2363-2481 */
 void ora_solvelpres(ora_state *st, int t); /* main.f:3236-3439 */

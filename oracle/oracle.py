@@ -82,7 +82,7 @@ def load():
     lib.ora_calch3d.restype = C.c_int
     lib.ora_error.argtypes = [vp, C.POINTER(C.c_longlong)]
     lib.ora_error.restype = C.c_int
-    for fn in ("ora_vofmethod", "ora_kepsmodel", "ora_checktime", "ora_csf", "ora_sgip", "ora_mglin"):
+    for fn in ("ora_vofmethod", "ora_kepsmodel", "ora_checktime", "ora_csf", "ora_sgip", "ora_sgip2", "ora_mglin"):
         getattr(lib, fn).argtypes = [vp]
     lib.ora_solvelpres.argtypes = [vp, C.c_int]
     lib.ora_step.argtypes = [vp, C.c_int]

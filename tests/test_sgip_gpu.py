@@ -18,8 +18,8 @@ pytestmark = pytest.mark.gpu
 HEIGHTS = ["hxmin", "hxmax", "hymin", "hymax", "hzmin", "hzmax"]
 
 
-def _cfg(dsg, n, mode, **kw):
-    return dsg.config.droplet(n, mode=mode, tol=1e-9, impact_speed=3.0, **kw).replace(surfacet=5, hswitch=1)
+def _cfg(dsg, n, mode, surfacet=5, **kw):
+    return dsg.config.droplet(n, mode=mode, tol=1e-9, impact_speed=3.0, **kw).replace(surfacet=surfacet, hswitch=1)
 
 
 def test_heights_match_oracle(gpu_lib):
@@ -42,11 +42,12 @@ def test_heights_match_oracle(gpu_lib):
     assert interface > 100
 
 
-@pytest.mark.parametrize("n,mode,steps", [(32, 0, 16), (32, 1, 12), (24, 1, 6)])
-def test_sgip_step_parity(gpu_lib, n, mode, steps):
+@pytest.mark.parametrize("n,mode,steps,surfacet", [(32, 0, 16, 5), (32, 1, 12, 5), (24, 1, 6, 5), (32, 0, 12, 6)])
+def test_sgip_step_parity(gpu_lib, n, mode, steps, surfacet):
+    """SGIP (surfacet = 5) and SGIP2 (surfacet = 6) whole steps."""
     dsg = gpu_lib
     from oracle import Oracle
-    inp = _cfg(dsg, n, mode)
+    inp = _cfg(dsg, n, mode, surfacet)
     ora, gpu = Oracle(inp.as_dict()), dsg.Solver(inp)
     wall = 0.0
     for t in range(1, steps + 1):
@@ -62,7 +63,7 @@ def test_sgip_step_parity(gpu_lib, n, mode, steps):
         vg, vo = gpu.liquid_volume(), ora.liquid_volume()
         assert abs(vg - vo) <= 1e-12 * abs(vo)
         wall = max(wall, float(np.abs(ora.field("s22")[:, 1, :]).max()))
-    if n == 32 and mode == 0:
+    if n == 32 and mode == 0 and surfacet == 5:
         assert wall > 0.0  # the contact-angle branch on the wall plane ran
 
 
@@ -82,6 +83,6 @@ def test_calch3d_stop_is_an_error(gpu_lib):
 
 def test_surface_tension_options(gpu_lib):
     dsg = gpu_lib
-    for bad in (dict(surfacet=3), dict(hswitch=2)):
+    for bad in (dict(surfacet=3), dict(surfacet=1), dict(hswitch=2)):
         with pytest.raises(dsg.DsgError):
             dsg.Solver(dsg.config.droplet(16).replace(**bad))
