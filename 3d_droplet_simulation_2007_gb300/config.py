@@ -89,6 +89,8 @@ class InputData:
     # 1.4 needed the fewest V-cycles on the 256^3 splash (sweep 1.0-1.5: 8-9
     # V-cycles per step against 9-10 with the reference's OMEGA = 1.5)
     mg32_omega: float = 1.4
+    mg32_npre: int = 0
+    mg32_npost: int = 0
 
     def as_dict(self):
         return asdict(self)

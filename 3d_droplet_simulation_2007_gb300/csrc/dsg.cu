@@ -193,6 +193,11 @@ inline float omega32(const dsg_ctx *ctx) {
   return (float)(ctx->cfg.mg32_omega > 0.0 ? ctx->cfg.mg32_omega : ctx->cfg.omega);
 }
 
+// Sweeps of the FP32 V-cycle: the reference's (adaptive) NPRE/NPOST unless
+// the configuration fixes them.
+inline int pre32(const dsg_ctx *ctx) { return ctx->cfg.mg32_npre > 0 ? ctx->cfg.mg32_npre : ctx->s.npre; }
+inline int post32(const dsg_ctx *ctx) { return ctx->cfg.mg32_npost > 0 ? ctx->cfg.mg32_npost : ctx->s.npost; }
+
 inline float level_h2(dsg_ctx *ctx, int l) {
   const double h1 = ctx->s.lengthsize / (ctx->lnx[l] - 2);
   return (float)(h1 * h1);
@@ -291,8 +296,8 @@ void tail_args(dsg_ctx *ctx, int top, dsg::TailArgs *A) {
     A->lv[l] = dsg::TailLevel{L[U32], L[RHS32], L[A32], L[B32], L[C32], L[EI32], ctx->level(l), level_h2(ctx, l)};
   }
   A->top = top;
-  A->npre = ctx->s.npre;
-  A->npost = ctx->s.npost;
+  A->npre = pre32(ctx);
+  A->npost = post32(ctx);
   A->ntop = ctx->s.ntop;
   A->omega = omega32(ctx);
 }
@@ -307,7 +312,7 @@ int vcycle32(dsg_ctx *ctx, int j) {
   for (int jj = j; jj >= 2 && jj > jt; jj--) {
     float **L = ctx->lv32[jj];
     float **Lc = ctx->lv32[jj - 1];
-    DSG_CK(ctx, relax32_level(ctx, ctx->s.npre, jj));
+    DSG_CK(ctx, relax32_level(ctx, pre32(ctx), jj));
     if (jj == ng) {
       FineSplit f = fine_split(ctx);
       DSG_CK(ctx, dsg::resid_restrict32_split(Lc[RHS32], Lc[U32], f.u, f.r, L[A32], ctx->level(jj),
@@ -331,7 +336,7 @@ int vcycle32(dsg_ctx *ctx, int j) {
     } else {
       DSG_CK(ctx, dsg::addint32(ctx->lv32[jj][U32], ctx->lv32[jj - 1][U32], ctx->level(jj), st));
     }
-    DSG_CK(ctx, relax32_level(ctx, ctx->s.npost, jj));
+    DSG_CK(ctx, relax32_level(ctx, post32(ctx), jj));
   }
   return DSG_OK;
 }
@@ -500,7 +505,7 @@ int mixed_solve(dsg_ctx *ctx, dsg_mg_stats *s) {
   // the measured reduction per V-cycle predicts are needed to reach tol
   const int fixed = ctx->cfg.inner_vcycles;
   int inner = fixed > 0 ? (fixed < dsg_ctx::kMaxInner ? fixed : dsg_ctx::kMaxInner) : 2;
-  int key[6] = {ctx->s.npre, ctx->s.npost, ctx->s.ntop, ctx->cfg.cycles, 0, ctx->prof ? 1 : 0};
+  int key[6] = {pre32(ctx), post32(ctx), ctx->s.ntop, ctx->cfg.cycles, 0, ctx->prof ? 1 : 0};
   // start: FP32 coefficient hierarchy, FP32 FMG guess, first FP64 defect
   auto first = [&]() -> int {
     int q = coef_hierarchy32(ctx);
@@ -608,7 +613,7 @@ int mixed_solve(dsg_ctx *ctx, dsg_mg_stats *s) {
     key[4] = inner;
     rc = run(ctx->g_iter[inner], iterate);
     if (rc) return rc;
-    s->fine_sweeps += inner * (ctx->s.npre + ctx->s.npost);
+    s->fine_sweeps += inner * (pre32(ctx) + post32(ctx));
     n += inner;
     const double r_old = r;
     rc = defect_read(ctx, &r);

@@ -34,7 +34,7 @@ UNIT = "time-steps/s"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=256, help="interior cells per side")
@@ -45,6 +45,8 @@ def parse():
     ap.add_argument("--no-graphs", action="store_true", help="launch the mixed solve without CUDA graphs")
     ap.add_argument("--start", type=int, default=None,
                     help="initial guess of the mixed solve: 0 FMG, 1 previous pressure, 2 zero (default: config)")
+    ap.add_argument("--sweeps32", type=str, default=None,
+                    help="pre,post sweeps of the FP32 V-cycles (default: the configuration's)")
     ap.add_argument("--omega32", type=float, default=None,
                     help="relaxation factor of the FP32 V-cycles (default: the library configuration's)")
     ap.add_argument("--tail-nodes", type=int, default=0,
@@ -66,13 +68,17 @@ def dist_env():
     return ws, rank, local
 
 
-def workload(dsg, n, mode, tol, inner=0, graphs=True, tail_nodes=0, omega32=None, start=None):
+def workload(dsg, n, mode, tol, inner=0, graphs=True, tail_nodes=0, omega32=None, start=None, sweeps32=None):
     cfg = dsg.config
     inp = cfg.droplet(n, steps=1000, impact_speed=3.0, noise_si=1e-4, mode=mode, tol=tol,
                       npre=4, npost=4, ntop=4).replace(inner_vcycles=inner, use_graphs=1 if graphs else 0,
                                                        tail_nodes=tail_nodes)
     inp = inp if omega32 is None else inp.replace(mg32_omega=omega32)
-    return inp if start is None else inp.replace(warm_start=start)
+    inp = inp if start is None else inp.replace(warm_start=start)
+    if sweeps32:
+        a, b = (int(x) for x in sweeps32.split(","))
+        inp = inp.replace(mg32_npre=a, mg32_npost=b)
+    return inp
 
 
 def measured_peaks():
@@ -112,7 +118,11 @@ class Clocks:
                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q, "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+                 "-lms", "50"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            # the timed region starts once the sampler is producing samples
+            t0 = time.time()
+            while time.time() - t0 < 5.0 and os.path.getsize(self.path) == 0 and self.proc.poll() is None:
+                time.sleep(0.02)
         except Exception:
             self.proc = None
 
@@ -211,7 +221,7 @@ def run_gb300(args):
     dsg.load()
     mode = mode_of(dsg, args.mode)
     inp = workload(dsg, args.n, mode, args.tol, args.inner, not args.no_graphs, args.tail_nodes, args.omega32,
-                   args.start)
+                   args.start, args.sweeps32)
     solver = dsg.Solver(inp)
     solver.set_stream(torch.cuda.current_stream().cuda_stream)
     for t in range(1, args.warmup + 1):

@@ -93,6 +93,8 @@ typedef struct dsg_config {
   int warm_start;      /* DSG_MODE_TOL_MIXED initial guess: 0 = FP32 full multigrid, 1 = previous-step
                           pressure, 2 = zero */
   double mg32_omega;   /* relaxation factor of the FP32 V-cycles of the mixed modes (<= 0: omega) */
+  int mg32_npre;       /* pre-/post-sweeps of the FP32 V-cycles (<= 0: the adaptive NPRE/NPOST) */
+  int mg32_npost;
 } dsg_config;
 
 /* Non-dimensional scalars and adaptive counters (COMMON /PHYSICS/, /DIFF/,
