@@ -108,6 +108,21 @@ class Ensemble:
         return bw.value
 
 
+def member_cost(inp):
+    """Cost model of one member's step: launch-bound floor + interior cells."""
+    return float((inp.nx - 2) * (inp.ny - 2) * (inp.nz - 2)) + 2.0e6
+
+
+def shard(inputs, rank, world):
+    """Indices of the members that rank `rank` of `world` steps: members are
+    independent, so the ensemble splits across GPUs with no data exchange,
+    balanced longest-processing-time-first on the cost model."""
+    if world <= 1:
+        return list(range(len(inputs)))
+    owner = plan([member_cost(x) for x in inputs], world)
+    return [i for i in range(len(inputs)) if owner[i] == rank]
+
+
 def plan(costs, workers):
     """Worker of each member under the longest-processing-time-first plan."""
     lib = _lib.load()

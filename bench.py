@@ -206,6 +206,16 @@ def time_steps(torch, solver, k, t0):
     return e0.elapsed_time(e1), stats
 
 
+def max_over_ranks(x, dist, device=None):
+    """The largest value of x over all ranks (x itself without a process group)."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_gb300(args):
     import numpy as np
     import torch
@@ -240,11 +250,7 @@ def run_gb300(args):
     if dist:
         dist.barrier()
     clk = clocks.stop()
-    ms_max = ms
-    if dist:
-        tt = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms_max = float(tt.item())
+    ms_max = max_over_ranks(ms, dist, "cuda")
     value = ws * args.steps / (ms_max / 1e3)
     vcycles = [s["vcycles"] for s in stats]
 
@@ -336,15 +342,22 @@ def run_ensemble(args):
     of 48-160^3 cells, Weber 50-800, mixed-precision pressure to tol.  The
     members run on their own streams from a pool of host threads; the timed
     region is bracketed by a synchronisation of every member's stream and
-    measured with the host clock (the work spans many streams)."""
+    measured with the host clock (the work spans many streams).  With N
+    ranks the members are sharded across the GPUs by cost (no data-path
+    collective); the time is the slowest rank's."""
     import torch
     ws, rank, local = dist_env()
     torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     dsg = importlib.import_module(PKG)
     lib = dsg.load()
     cfgs = dsg.ensemble.study_configs(args.ensemble, tol=args.tol)
+    mine = dsg.ensemble.shard(cfgs, rank, ws)
     cells = sum((c.nx - 2) * (c.ny - 2) * (c.nz - 2) for c in cfgs)
-    with dsg.Ensemble(cfgs, workers=max(args.workers, 1)) as e:
+    with dsg.Ensemble([cfgs[i] for i in mine], workers=max(args.workers, 1)) as e:
         tuned = e.autotune(steps_per_trial=2) if args.workers <= 0 else None
         for _ in range(args.warmup):
             e.step()
@@ -352,12 +365,17 @@ def run_ensemble(args):
         def timed(k):
             for i in range(e.n):
                 e.member(i).synchronize()
+            if dist:
+                dist.barrier()
             l0 = lib.dsg_launch_count()
             t0 = time.perf_counter()
             stats = [e.step() for _ in range(k)]
             for i in range(e.n):
                 e.member(i).synchronize()
-            return time.perf_counter() - t0, lib.dsg_launch_count() - l0, stats
+            el = time.perf_counter() - t0
+            if dist:
+                dist.barrier()
+            return el, lib.dsg_launch_count() - l0, stats
 
         clocks = Clocks(local)
         clocks.start()
@@ -366,21 +384,27 @@ def run_ensemble(args):
         workers = e.workers
         e.set_workers(1)
         el1, _, _ = timed(1)
+    el = max_over_ranks(el, dist, "cuda")
+    el1 = max_over_ranks(el1, dist, "cuda")
     value = args.ensemble * args.steps / el
     if rank == 0:
         line = {"metric": "member time-steps/s, droplet-study ensemble", "value": value,
-                "unit": "member-steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-                "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True, "scaling": "weak",
+                "unit": "member-steps/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True, "scaling": "strong",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": {"workload": "%d droplets on wall, interior sides 48/64/96/128/160, Weber 50-800 "
                                        "log-uniform, D = 2 mm, mixed-precision pressure to %.0e"
                                        % (args.ensemble, args.tol),
                            "cells_per_step": cells, "workers": workers, "autotuned": tuned is not None,
+                           "members_rank0": len(mine),
+                           "parallelism": "members sharded by cost over %d GPU(s)" % ws,
                            "timing": "host clock between synchronisations of all member streams"},
                 "one_worker_value": args.ensemble / el1,
-                "vcycles_mean": float(sum(s["vcycles"] for st in stats for s in st) / (len(stats) * args.ensemble)),
+                "vcycles_mean": float(sum(s["vcycles"] for st in stats for s in st) / max(1, len(stats) * e.n)),
                 "gpu_launches": launches, "clocks": clk}
         print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
     return 0
 
 
