@@ -258,64 +258,108 @@ __global__ void __launch_bounds__(256) k_conv3_wgrad(const bf16 *__restrict__ X,
   }
 }
 
-// ---- elementwise kernels ------------------------------------------------------
-// 2x2x2 average pooling, channels-last bf16.
+// The elementwise kernels below move 8 channels (16 bytes of bf16) per thread
+// with 32-bit voxel indices; C is a multiple of 8 and every level has fewer
+// than 2^32 channel groups.
+struct V8 {
+  float f[8];
+};
+
+__device__ __forceinline__ V8 load8(const bf16 *p) {
+  const uint4 r = *reinterpret_cast<const uint4 *>(p);
+  const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&r);
+  V8 v;
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+    const float2 f = __bfloat1622float2(h[c]);
+    v.f[2 * c] = f.x;
+    v.f[2 * c + 1] = f.y;
+  }
+  return v;
+}
+
+__device__ __forceinline__ void store8(bf16 *p, const V8 &v) {
+  uint4 r;
+  __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(&r);
+#pragma unroll
+  for (int c = 0; c < 4; c++) h[c] = __floats2bfloat162_rn(v.f[2 * c], v.f[2 * c + 1]);
+  *reinterpret_cast<uint4 *>(p) = r;
+}
+
+// 2x2x2 average pooling, channels-last bf16: Y at half resolution.
 __global__ void k_pool(const bf16 *__restrict__ X, bf16 *__restrict__ Y, int W, int H, int D, int C) {
-  const int Wc = W / 2, Hc = H / 2, Dc = D / 2;
-  const size_t n = (size_t)Wc * Hc * Dc * C;
-  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
-    const int c = (int)(q % C);
-    size_t v = q / C;
-    const int x = (int)(v % Wc), y = (int)((v / Wc) % Hc), z = (int)(v / ((size_t)Wc * Hc));
-    float s = 0.f;
+  const unsigned C8 = C / 8, Wc = W / 2, Hc = H / 2, Dc = D / 2;
+  const unsigned n = Wc * Hc * Dc * C8;
+  for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    const unsigned g = q % C8, v = q / C8;
+    const unsigned x = v % Wc, y = (v / Wc) % Hc, z = v / (Wc * Hc);
+    V8 s;
+#pragma unroll
+    for (int c = 0; c < 8; c++) s.f[c] = 0.f;
     for (int k = 0; k < 8; k++) {
-      const int xx = 2 * x + (k & 1), yy = 2 * y + ((k >> 1) & 1), zz = 2 * z + (k >> 2);
-      s += __bfloat162float(X[(((size_t)zz * H + yy) * W + xx) * C + c]);
+      const unsigned xx = 2 * x + (k & 1), yy = 2 * y + ((k >> 1) & 1), zz = 2 * z + (k >> 2);
+      const V8 a = load8(X + ((size_t)((zz * H + yy) * W + xx)) * C + g * 8);
+#pragma unroll
+      for (int c = 0; c < 8; c++) s.f[c] += a.f[c];
     }
-    Y[q] = __float2bfloat16(0.125f * s);
+#pragma unroll
+    for (int c = 0; c < 8; c++) s.f[c] = 0.125f * s.f[c];
+    store8(Y + (size_t)q * 8, s);
   }
 }
 
 // Y = up(A) + B: A at half resolution, Y/B at full, channels-last bf16.
 __global__ void k_upadd(const bf16 *__restrict__ A, const bf16 *__restrict__ B, bf16 *__restrict__ Y, int W, int H,
                         int D, int C) {
-  const size_t n = (size_t)W * H * D * C;
-  const int Wc = W / 2, Hc = H / 2;
-  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
-    const int c = (int)(q % C);
-    size_t v = q / C;
-    const int x = (int)(v % W), y = (int)((v / W) % H), z = (int)(v / ((size_t)W * H));
-    const float a = __bfloat162float(A[(((size_t)(z >> 1) * Hc + (y >> 1)) * Wc + (x >> 1)) * C + c]);
-    Y[q] = __float2bfloat16(a + __bfloat162float(B[q]));
+  const unsigned C8 = C / 8, Wc = W / 2, Hc = H / 2;
+  const unsigned n = (unsigned)W * H * D * C8;
+  for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    const unsigned g = q % C8, v = q / C8;
+    const unsigned x = v % W, y = (v / W) % H, z = v / (W * H);
+    const V8 a = load8(A + ((size_t)(((z >> 1) * Hc + (y >> 1)) * Wc + (x >> 1))) * C + g * 8);
+    V8 b = load8(B + (size_t)q * 8);
+#pragma unroll
+    for (int c = 0; c < 8; c++) b.f[c] = a.f[c] + b.f[c];
+    store8(Y + (size_t)q * 8, b);
   }
 }
 
 // Backward of Y = up(A) + B: dB = dY, dA = sum over the 8 children (FP32).
 __global__ void k_upadd_back(const bf16 *__restrict__ dY, float *__restrict__ dA, int W, int H, int D, int C) {
-  const int Wc = W / 2, Hc = H / 2, Dc = D / 2;
-  const size_t n = (size_t)Wc * Hc * Dc * C;
-  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
-    const int c = (int)(q % C);
-    size_t v = q / C;
-    const int x = (int)(v % Wc), y = (int)((v / Wc) % Hc), z = (int)(v / ((size_t)Wc * Hc));
-    float s = 0.f;
+  const unsigned C8 = C / 8, Wc = W / 2, Hc = H / 2, Dc = D / 2;
+  const unsigned n = Wc * Hc * Dc * C8;
+  for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    const unsigned g = q % C8, v = q / C8;
+    const unsigned x = v % Wc, y = (v / Wc) % Hc, z = v / (Wc * Hc);
+    float s[8];
+#pragma unroll
+    for (int c = 0; c < 8; c++) s[c] = 0.f;
     for (int k = 0; k < 8; k++) {
-      const int xx = 2 * x + (k & 1), yy = 2 * y + ((k >> 1) & 1), zz = 2 * z + (k >> 2);
-      s += __bfloat162float(dY[(((size_t)zz * H + yy) * W + xx) * C + c]);
+      const unsigned xx = 2 * x + (k & 1), yy = 2 * y + ((k >> 1) & 1), zz = 2 * z + (k >> 2);
+      const V8 a = load8(dY + ((size_t)((zz * H + yy) * W + xx)) * C + g * 8);
+#pragma unroll
+      for (int c = 0; c < 8; c++) s[c] += a.f[c];
     }
-    dA[q] = s;
+    float4 *o = reinterpret_cast<float4 *>(dA + (size_t)q * 8);
+    o[0] = make_float4(s[0], s[1], s[2], s[3]);
+    o[1] = make_float4(s[4], s[5], s[6], s[7]);
   }
 }
 
 // Backward of pooling: dX(child) += dY(parent)/8 (accumulates into an FP32 buffer).
 __global__ void k_pool_back_acc(const bf16 *__restrict__ dY, float *__restrict__ dX, int W, int H, int D, int C) {
-  const size_t n = (size_t)W * H * D * C;
-  const int Wc = W / 2, Hc = H / 2;
-  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
-    const int c = (int)(q % C);
-    size_t v = q / C;
-    const int x = (int)(v % W), y = (int)((v / W) % H), z = (int)(v / ((size_t)W * H));
-    dX[q] += 0.125f * __bfloat162float(dY[(((size_t)(z >> 1) * Hc + (y >> 1)) * Wc + (x >> 1)) * C + c]);
+  const unsigned C8 = C / 8, Wc = W / 2, Hc = H / 2;
+  const unsigned n = (unsigned)W * H * D * C8;
+  for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    const unsigned g = q % C8, v = q / C8;
+    const unsigned x = v % W, y = (v / W) % H, z = v / (W * H);
+    const V8 a = load8(dY + ((size_t)(((z >> 1) * Hc + (y >> 1)) * Wc + (x >> 1))) * C + g * 8);
+    float4 *o = reinterpret_cast<float4 *>(dX + (size_t)q * 8);
+    float4 o0 = o[0], o1 = o[1];
+    o0.x += 0.125f * a.f[0], o0.y += 0.125f * a.f[1], o0.z += 0.125f * a.f[2], o0.w += 0.125f * a.f[3];
+    o1.x += 0.125f * a.f[4], o1.y += 0.125f * a.f[5], o1.z += 0.125f * a.f[6], o1.w += 0.125f * a.f[7];
+    o[0] = o0;
+    o[1] = o1;
   }
 }
 
@@ -325,21 +369,57 @@ __global__ void k_relu_back(const float *__restrict__ dacc, const bf16 *__restri
   __shared__ float sb[64];
   if (threadIdx.x < 64) sb[threadIdx.x] = 0.f;
   __syncthreads();
-  const size_t n = nvox * C;
-  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
-    float g = dacc[q];
-    if (relu && !(__bfloat162float(act[q]) > 0.f)) g = 0.f;
-    G[q] = __float2bfloat16(g);
-    atomicAdd(&sb[q % C], g);
+  const unsigned C8 = C / 8;
+  const unsigned n = (unsigned)nvox * C8;
+  float part[8];
+#pragma unroll
+  for (int c = 0; c < 8; c++) part[c] = 0.f;
+  // a thread always handles the same channel group when blockDim*gridDim is a multiple of C8
+  const unsigned stride = gridDim.x * blockDim.x;
+  const unsigned q0 = blockIdx.x * blockDim.x + threadIdx.x;
+  for (unsigned q = q0; q < n; q += stride) {
+    const float4 *d = reinterpret_cast<const float4 *>(dacc + (size_t)q * 8);
+    const float4 d0 = d[0], d1 = d[1];
+    float g[8] = {d0.x, d0.y, d0.z, d0.w, d1.x, d1.y, d1.z, d1.w};
+    if (relu) {
+      const V8 a = load8(act + (size_t)q * 8);
+#pragma unroll
+      for (int c = 0; c < 8; c++)
+        if (!(a.f[c] > 0.f)) g[c] = 0.f;
+    }
+    V8 o;
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+      o.f[c] = g[c];
+      part[c] += g[c];
+    }
+    store8(G + (size_t)q * 8, o);
+  }
+  // lanes l and l + C8 hold the same channel group: reduce over them first
+  for (int off = 16; off >= (int)C8; off >>= 1)
+#pragma unroll
+    for (int c = 0; c < 8; c++) part[c] += __shfl_xor_sync(0xffffffffu, part[c], off);
+  if ((threadIdx.x & 31) < C8 && q0 < n) {
+    const unsigned grp = q0 % C8;  // constant over the loop: stride % C8 == 0
+#pragma unroll
+    for (int c = 0; c < 8; c++) atomicAdd(&sb[grp * 8 + c], part[c]);
   }
   __syncthreads();
   if (threadIdx.x < C) atomicAdd(&dbias[threadIdx.x], sb[threadIdx.x]);
 }
 
-// bf16 -> float accumulate: dst += src.
+// bf16 -> float accumulate: dst += src (n a multiple of 8).
 __global__ void k_acc_bf16(float *__restrict__ dst, const bf16 *__restrict__ src, size_t n) {
-  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
-    dst[q] += __bfloat162float(src[q]);
+  const unsigned n8 = (unsigned)(n / 8);
+  for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < n8; q += gridDim.x * blockDim.x) {
+    const V8 a = load8(src + (size_t)q * 8);
+    float4 *o = reinterpret_cast<float4 *>(dst + (size_t)q * 8);
+    float4 o0 = o[0], o1 = o[1];
+    o0.x += a.f[0], o0.y += a.f[1], o0.z += a.f[2], o0.w += a.f[3];
+    o1.x += a.f[4], o1.y += a.f[5], o1.z += a.f[6], o1.w += a.f[7];
+    o[0] = o0;
+    o[1] = o1;
+  }
 }
 
 // Output layer loss: y (float, 8 padded channels, channel 0 used), target t.
@@ -655,17 +735,17 @@ int repack(dsg_net *n, cudaStream_t st) {
 
 int forward(dsg_net *n, cudaStream_t st) {
   NCK(n, conv_fwd(n, 0, n->x0, n->e1, st));
-  DSG_COUNT k_pool<<<eblocks(vox(n, 1) * 16), 256, 0, st>>>(n->e1, n->p1, n->W[0], n->H[0], n->D[0], 16);
+  DSG_COUNT k_pool<<<eblocks(vox(n, 1) * 2), 256, 0, st>>>(n->e1, n->p1, n->W[0], n->H[0], n->D[0], 16);
   NCK(n, conv_fwd(n, 1, n->p1, n->e2, st));
-  DSG_COUNT k_pool<<<eblocks(vox(n, 2) * 32), 256, 0, st>>>(n->e2, n->p2, n->W[1], n->H[1], n->D[1], 32);
+  DSG_COUNT k_pool<<<eblocks(vox(n, 2) * 4), 256, 0, st>>>(n->e2, n->p2, n->W[1], n->H[1], n->D[1], 32);
   NCK(n, conv_fwd(n, 2, n->p2, n->e3, st));
-  DSG_COUNT k_pool<<<eblocks(vox(n, 3) * 64), 256, 0, st>>>(n->e3, n->p3, n->W[2], n->H[2], n->D[2], 64);
+  DSG_COUNT k_pool<<<eblocks(vox(n, 3) * 8), 256, 0, st>>>(n->e3, n->p3, n->W[2], n->H[2], n->D[2], 64);
   NCK(n, conv_fwd(n, 3, n->p3, n->e4, st));
-  DSG_COUNT k_upadd<<<eblocks(vox(n, 2) * 64), 256, 0, st>>>(n->e4, n->e3, n->u3, n->W[2], n->H[2], n->D[2], 64);
+  DSG_COUNT k_upadd<<<eblocks(vox(n, 2) * 8), 256, 0, st>>>(n->e4, n->e3, n->u3, n->W[2], n->H[2], n->D[2], 64);
   NCK(n, conv_fwd(n, 4, n->u3, n->d3, st));
-  DSG_COUNT k_upadd<<<eblocks(vox(n, 1) * 32), 256, 0, st>>>(n->d3, n->e2, n->u2, n->W[1], n->H[1], n->D[1], 32);
+  DSG_COUNT k_upadd<<<eblocks(vox(n, 1) * 4), 256, 0, st>>>(n->d3, n->e2, n->u2, n->W[1], n->H[1], n->D[1], 32);
   NCK(n, conv_fwd(n, 5, n->u2, n->d2, st));
-  DSG_COUNT k_upadd<<<eblocks(vox(n, 0) * 16), 256, 0, st>>>(n->d2, n->e1, n->u1, n->W[0], n->H[0], n->D[0], 16);
+  DSG_COUNT k_upadd<<<eblocks(vox(n, 0) * 2), 256, 0, st>>>(n->d2, n->e1, n->u1, n->W[0], n->H[0], n->D[0], 16);
   NCK(n, conv_fwd(n, 6, n->u1, n->yout, st));
   NCK(n, cudaGetLastError());
   return DSG_OK;
@@ -683,7 +763,7 @@ int layer_back(dsg_net *n, int l, const float *dacc, const bf16 *act_out, const 
   // G into gbuf (coutp channels); the bias gradient of padded channels is dropped
   NCK(n, cudaMemsetAsync(wscratch, 0, (size_t)64 * sizeof(float), st));
   const int gc = grad_ch(l);
-  DSG_COUNT k_relu_back<<<eblocks(nv * gc), 256, 0, st>>>(dacc, act_out, n->gbuf, wscratch, nv, gc, L.relu ? 1 : 0);
+  DSG_COUNT k_relu_back<<<eblocks(nv * gc / 8), 256, 0, st>>>(dacc, act_out, n->gbuf, wscratch, nv, gc, L.relu ? 1 : 0);
   NCK(n, cudaMemcpyAsync(dbias, wscratch, L.cout * sizeof(float), cudaMemcpyDeviceToDevice, st));
   float *wpad = wscratch + 64;
   const size_t wn = (size_t)27 * L.cinp * gc;
@@ -708,25 +788,25 @@ int backward(dsg_net *n, cudaStream_t st) {
   NCK(n, cudaMemsetAsync(n->acc_e3, 0, v2 * 64 * sizeof(float), st));
   // D1: y = conv6(u1), u1 = up(d2) + e1
   if ((rc = layer_back(n, 6, n->dy_out, nullptr, n->u1, n->gbuf2, ws, st))) return rc;
-  DSG_COUNT k_acc_bf16<<<eblocks(v0 * 16), 256, 0, st>>>(n->acc_e1, n->gbuf2, v0 * 16);
-  DSG_COUNT k_upadd_back<<<eblocks(v1 * 16), 256, 0, st>>>(n->gbuf2, n->tmp, n->W[0], n->H[0], n->D[0], 16);
+  DSG_COUNT k_acc_bf16<<<eblocks(v0 * 2), 256, 0, st>>>(n->acc_e1, n->gbuf2, v0 * 16);
+  DSG_COUNT k_upadd_back<<<eblocks(v1 * 2), 256, 0, st>>>(n->gbuf2, n->tmp, n->W[0], n->H[0], n->D[0], 16);
   // D2: d2 = relu(conv5(u2)), u2 = up(d3) + e2
   if ((rc = layer_back(n, 5, n->tmp, n->d2, n->u2, n->gbuf2, ws, st))) return rc;
-  DSG_COUNT k_acc_bf16<<<eblocks(v1 * 32), 256, 0, st>>>(n->acc_e2, n->gbuf2, v1 * 32);
-  DSG_COUNT k_upadd_back<<<eblocks(v2 * 32), 256, 0, st>>>(n->gbuf2, n->tmp, n->W[1], n->H[1], n->D[1], 32);
+  DSG_COUNT k_acc_bf16<<<eblocks(v1 * 4), 256, 0, st>>>(n->acc_e2, n->gbuf2, v1 * 32);
+  DSG_COUNT k_upadd_back<<<eblocks(v2 * 4), 256, 0, st>>>(n->gbuf2, n->tmp, n->W[1], n->H[1], n->D[1], 32);
   // D3: d3 = relu(conv4(u3)), u3 = up(e4) + e3
   if ((rc = layer_back(n, 4, n->tmp, n->d3, n->u3, n->gbuf2, ws, st))) return rc;
-  DSG_COUNT k_acc_bf16<<<eblocks(v2 * 64), 256, 0, st>>>(n->acc_e3, n->gbuf2, v2 * 64);
-  DSG_COUNT k_upadd_back<<<eblocks(v3 * 64), 256, 0, st>>>(n->gbuf2, n->tmp, n->W[2], n->H[2], n->D[2], 64);
+  DSG_COUNT k_acc_bf16<<<eblocks(v2 * 8), 256, 0, st>>>(n->acc_e3, n->gbuf2, v2 * 64);
+  DSG_COUNT k_upadd_back<<<eblocks(v3 * 8), 256, 0, st>>>(n->gbuf2, n->tmp, n->W[2], n->H[2], n->D[2], 64);
   // E4: e4 = relu(conv3(p3)), p3 = pool(e3)
   if ((rc = layer_back(n, 3, n->tmp, n->e4, n->p3, n->gbuf2, ws, st))) return rc;
-  DSG_COUNT k_pool_back_acc<<<eblocks(v2 * 64), 256, 0, st>>>(n->gbuf2, n->acc_e3, n->W[2], n->H[2], n->D[2], 64);
+  DSG_COUNT k_pool_back_acc<<<eblocks(v2 * 8), 256, 0, st>>>(n->gbuf2, n->acc_e3, n->W[2], n->H[2], n->D[2], 64);
   // E3: e3 = relu(conv2(p2)), p2 = pool(e2)
   if ((rc = layer_back(n, 2, n->acc_e3, n->e3, n->p2, n->gbuf2, ws, st))) return rc;
-  DSG_COUNT k_pool_back_acc<<<eblocks(v1 * 32), 256, 0, st>>>(n->gbuf2, n->acc_e2, n->W[1], n->H[1], n->D[1], 32);
+  DSG_COUNT k_pool_back_acc<<<eblocks(v1 * 4), 256, 0, st>>>(n->gbuf2, n->acc_e2, n->W[1], n->H[1], n->D[1], 32);
   // E2: e2 = relu(conv1(p1)), p1 = pool(e1)
   if ((rc = layer_back(n, 1, n->acc_e2, n->e2, n->p1, n->gbuf2, ws, st))) return rc;
-  DSG_COUNT k_pool_back_acc<<<eblocks(v0 * 16), 256, 0, st>>>(n->gbuf2, n->acc_e1, n->W[0], n->H[0], n->D[0], 16);
+  DSG_COUNT k_pool_back_acc<<<eblocks(v0 * 2), 256, 0, st>>>(n->gbuf2, n->acc_e1, n->W[0], n->H[0], n->D[0], 16);
   // E1: e1 = relu(conv0(x0)); no input gradient
   if ((rc = layer_back(n, 0, n->acc_e1, n->e1, n->x0, nullptr, ws, st))) return rc;
   NCK(n, cudaGetLastError());

@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 reference point")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned warm-start point")
     ap.add_argument("--ensemble", type=int, default=0,
                     help="time the droplet-study ensemble of this many members instead (48-160^3 grids)")
     ap.add_argument("--workers", type=int, default=0, help="ensemble host threads (0: autotune)")
@@ -266,6 +267,26 @@ def run_gb300(args):
         plain = {"value": args.steps / (pms / 1e3), "vcycles": [s["vcycles"] for s in pst]}
         ps.close()
 
+    # the learned warm start (committed weights), same workload, as a measured
+    # secondary point: the headline uses the faster FMG start
+    learned = None
+    if not args.no_learned and mode == dsg.config.MODE_TOL_MIXED:
+        lmod = importlib.import_module(PKG + ".learned")
+        if os.path.exists(lmod.WEIGHTS):
+            net = lmod.Net(args.n).load()
+            ls = dsg.Solver(inp.replace(mode=dsg.config.MODE_LEARNED))
+            ls.set_stream(torch.cuda.current_stream().cuda_stream)
+            net.attach(ls)
+            for t in range(1, args.warmup + 1):
+                ls.step(t)
+            lms, lst = time_steps(torch, ls, args.steps, args.warmup + 1)
+            learned = {"value": args.steps / (lms / 1e3), "vcycles": [s["vcycles"] for s in lst],
+                       "fallbacks": sum(s["fallback"] for s in lst),
+                       "relres_init_median": float(np.median([s["relres_init"] for s in lst]))}
+            lmod.detach(ls)
+            ls.close()
+            net.close()
+
     # end to end through the public API: pinned host state in, results out
     e2e = None
     if not args.no_e2e:
@@ -331,6 +352,8 @@ def run_gb300(args):
                 "cpu_baseline": cb, "e2e": e2e, "clocks": clk}
         if plain:
             line["plain_fp64"] = plain
+        if learned:
+            line["learned_warm_start"] = learned
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

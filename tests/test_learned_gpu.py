@@ -16,6 +16,8 @@ from conftest import relerr
 pytestmark = pytest.mark.gpu
 
 SHAPES = [(16, 16, 16), (8, 16, 24)]  # (D, H, W)
+# large enough for the z-marching conv columns: 4 planes per CTA at 64^3, 8 at 32x256x256
+DEEP_SHAPES = [(64, 64, 64), (32, 256, 256)]
 
 
 def _net(dsg, shape, seed=3):
@@ -63,6 +65,37 @@ def test_gradients_match_oracle(gpu_lib, shape):
     loss, g = net.loss_grad(x, t)
     loss_ref, g_ref, _ = NO.loss_and_grad(p.astype(np.float64), x.astype(np.float64), t.astype(np.float64))
     assert abs(loss - loss_ref) <= 1e-2 * loss_ref
+    off = 0
+    for l, (ci, co, _) in enumerate(NO.LAYERS):
+        n = 27 * ci * co + co
+        a, b = g[off:off + n].astype(np.float64), g_ref[off:off + n]
+        off += n
+        err = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+        cos = float(a @ b / max(np.linalg.norm(a) * np.linalg.norm(b), 1e-30))
+        assert err < 3e-2 and cos > 0.999, (l, err, cos)
+
+
+@pytest.mark.parametrize("shape", DEEP_SHAPES)
+def test_forward_deep_columns_match_oracle(gpu_lib, shape):
+    net, _ = _net(gpu_lib, shape, seed=11)
+    p = net.params.copy()
+    p += (np.random.default_rng(12).standard_normal(p.size) * 0.02).astype(np.float32)
+    net.params = p
+    x, _ = _inputs(shape, 13)
+    y = net.forward(x)
+    y_ref, _ = NO.forward(p.astype(np.float64), x.astype(np.float64), bf16=True)
+    assert relerr(y, y_ref) < 2e-2, relerr(y, y_ref)
+
+
+def test_gradients_deep_columns_match_oracle(gpu_lib):
+    shape = DEEP_SHAPES[0]
+    net, _ = _net(gpu_lib, shape, seed=14)
+    p = net.params.copy()
+    p += (np.random.default_rng(15).standard_normal(p.size) * 0.02).astype(np.float32)
+    net.params = p
+    x, t = _inputs(shape, 16)
+    _, g = net.loss_grad(x, t)
+    _, g_ref, _ = NO.loss_and_grad(p.astype(np.float64), x.astype(np.float64), t.astype(np.float64))
     off = 0
     for l, (ci, co, _) in enumerate(NO.LAYERS):
         n = 27 * ci * co + co
