@@ -20,10 +20,11 @@ __global__ void k_curvature(double *__restrict__ kap, const double *__restrict__
   // Uniform 19-point neighbourhood (bulk liquid or gas): every difference is
   // +0, every d is 0/sqrt(1e-50) = +0 and kappa = -(+0) = -0 exactly.
   const double f0 = F(0, 0, 0);
-  if (F(1, 0, 0) == f0 && F(-1, 0, 0) == f0 && F(0, 1, 0) == f0 && F(0, -1, 0) == f0 && F(0, 0, 1) == f0 &&
-      F(0, 0, -1) == f0 && F(1, 1, 0) == f0 && F(1, -1, 0) == f0 && F(-1, 1, 0) == f0 && F(-1, -1, 0) == f0 &&
-      F(1, 0, 1) == f0 && F(1, 0, -1) == f0 && F(-1, 0, 1) == f0 && F(-1, 0, -1) == f0 && F(0, 1, 1) == f0 &&
-      F(0, 1, -1) == f0 && F(0, -1, 1) == f0 && F(0, -1, -1) == f0) {
+#define EQ(di, dj, dk) same_bits(F(di, dj, dk), f0)
+  if (EQ(1, 0, 0) && EQ(-1, 0, 0) && EQ(0, 1, 0) && EQ(0, -1, 0) && EQ(0, 0, 1) && EQ(0, 0, -1) && EQ(1, 1, 0) &&
+      EQ(1, -1, 0) && EQ(-1, 1, 0) && EQ(-1, -1, 0) && EQ(1, 0, 1) && EQ(1, 0, -1) && EQ(-1, 0, 1) && EQ(-1, 0, -1) &&
+      EQ(0, 1, 1) && EQ(0, 1, -1) && EQ(0, -1, 1) && EQ(0, -1, -1)) {
+#undef EQ
     kap[q] = -0.0;
     return;
   }

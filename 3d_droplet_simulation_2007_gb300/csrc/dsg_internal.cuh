@@ -37,6 +37,19 @@ struct Dims {
   __host__ __device__ __forceinline__ size_t sz() const { return (size_t)nx * ny; }
 };
 
+// Bit-pattern tests of doubles on the integer pipe.  GB300's FP64 comparisons
+// issue on the FP64 pipe (as slow as its FMAs), and the exact fast paths test
+// up to 27 values per cell.  same_bits differs from == only for +0/-0 and
+// NaN: a -0 then takes the general path, which computes exactly what the
+// reference computes.
+__device__ __forceinline__ bool same_bits(double a, double b) {
+  return __double_as_longlong(a) == __double_as_longlong(b);
+}
+__device__ __forceinline__ bool is_zero_bits(double a) { return __double_as_longlong(a) == 0LL; }
+__device__ __forceinline__ bool is_one_bits(double a) { return __double_as_longlong(a) == 0x3FF0000000000000LL; }
+// a > 0 for a finite double (positive bit patterns order like the values)
+__device__ __forceinline__ bool positive_bits(double a) { return __double_as_longlong(a) > 0LL; }
+
 __device__ __forceinline__ double dmax1(double a, double b) { return a >= b ? a : b; }
 __device__ __forceinline__ double dmin1(double a, double b) { return a <= b ? a : b; }
 

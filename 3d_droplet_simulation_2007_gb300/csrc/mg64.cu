@@ -230,11 +230,11 @@ __global__ void k_abc(double *__restrict__ a, double *__restrict__ b, double *__
   const double c0 = cc[q], cx = cc[q + 1], cy = cc[q + d.sy()], cz = cc[q + d.sz()];
   // Faces between two bulk cells of the same phase take the precomputed
   // 1/(r1*(c+c)+r2) (same operations, evaluated once on the host).
-  const bool bulk = (c0 == 0.0 || c0 == 1.0);
-  const double kb = c0 == 0.0 ? k_gas : k_liq;
-  a[q] = (bulk && cx == c0) ? kb : 1.0 / (r1 * (c0 + cx) + r2);
-  b[q] = (bulk && cy == c0) ? kb : 1.0 / (r1 * (c0 + cy) + r2);
-  c[q] = (bulk && cz == c0) ? kb : 1.0 / (r1 * (c0 + cz) + r2);
+  const bool gas = is_zero_bits(c0), bulk = gas || is_one_bits(c0);
+  const double kb = gas ? k_gas : k_liq;
+  a[q] = (bulk && same_bits(cx, c0)) ? kb : 1.0 / (r1 * (c0 + cx) + r2);
+  b[q] = (bulk && same_bits(cy, c0)) ? kb : 1.0 / (r1 * (c0 + cy) + r2);
+  c[q] = (bulk && same_bits(cz, c0)) ? kb : 1.0 / (r1 * (c0 + cz) + r2);
 }
 
 // bc_coef: face 0 = a x-faces (all j,k), 1 = b(i,1,k) (i,k interior),
@@ -267,8 +267,9 @@ __global__ void k_ei(double *__restrict__ ei, const double *__restrict__ a, cons
   const size_t q = d.ix(i, j, k);
   const double s0 = a[q], s1 = a[q - 1], s2 = b[q], s3 = b[q - d.sy()], s4 = c[q], s5 = c[q - d.sz()];
   // Six equal bulk faces: the precomputed 1/(k+k+k+k+k+k).
-  if (s0 == s1 && s0 == s2 && s0 == s3 && s0 == s4 && s0 == s5 && (s0 == k_gas || s0 == k_liq)) {
-    ei[q] = s0 == k_gas ? e_gas : e_liq;
+  if (same_bits(s0, s1) && same_bits(s0, s2) && same_bits(s0, s3) && same_bits(s0, s4) && same_bits(s0, s5) &&
+      (same_bits(s0, k_gas) || same_bits(s0, k_liq))) {
+    ei[q] = same_bits(s0, k_gas) ? e_gas : e_liq;
     return;
   }
   ei[q] = 1.0 / (s0 + s1 + s2 + s3 + s4 + s5);
@@ -287,16 +288,17 @@ __global__ void k_filterc27(const double *__restrict__ cc, double *__restrict__ 
   // Uniform 27-point neighbourhood of 0 or 1: the partial sums are exact
   // multiples of the value, so the weighted sum equals the precomputed one.
   const double c0 = C(0, 0, 0);
-  if (c0 == 0.0 || c0 == 1.0) {
+  const bool gas = is_zero_bits(c0);
+  if (gas || is_one_bits(c0)) {
     bool uni = true;
 #pragma unroll
     for (int dk = -1; dk <= 1; dk++)
 #pragma unroll
       for (int dj = -1; dj <= 1; dj++)
 #pragma unroll
-        for (int di = -1; di <= 1; di++) uni = uni && (C(di, dj, dk) == c0);
+        for (int di = -1; di <= 1; di++) uni = uni && same_bits(C(di, dj, dk), c0);
     if (uni) {
-      double x = c0 == 0.0 ? 0.0 : w0 * 1.0 + w1 * 6.0 + w2 * 12.0 + w3 * 8.0;
+      double x = gas ? 0.0 : w0 * 1.0 + w1 * 6.0 + w2 * 12.0 + w3 * 8.0;
       if (x > 1.0) x = 1.0;
       cf[q] = x;
       return;

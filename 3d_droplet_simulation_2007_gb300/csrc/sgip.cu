@@ -232,10 +232,11 @@ __global__ void k_sgip_curvature(double *__restrict__ kap, const double *__restr
 #define F(di, dj, dk) f[q + (long)(di) + (long)(dj) * sy + (long)(dk) * sz]
   // uniform 19-point neighbourhood: every difference +0, kappa = -0 exactly
   const double f0 = F(0, 0, 0);
-  if (F(1, 0, 0) == f0 && F(-1, 0, 0) == f0 && F(0, 1, 0) == f0 && F(0, -1, 0) == f0 && F(0, 0, 1) == f0 &&
-      F(0, 0, -1) == f0 && F(1, 1, 0) == f0 && F(1, -1, 0) == f0 && F(-1, 1, 0) == f0 && F(-1, -1, 0) == f0 &&
-      F(1, 0, 1) == f0 && F(1, 0, -1) == f0 && F(-1, 0, 1) == f0 && F(-1, 0, -1) == f0 && F(0, 1, 1) == f0 &&
-      F(0, 1, -1) == f0 && F(0, -1, 1) == f0 && F(0, -1, -1) == f0) {
+#define EQ(di, dj, dk) same_bits(F(di, dj, dk), f0)
+  if (EQ(1, 0, 0) && EQ(-1, 0, 0) && EQ(0, 1, 0) && EQ(0, -1, 0) && EQ(0, 0, 1) && EQ(0, 0, -1) && EQ(1, 1, 0) &&
+      EQ(1, -1, 0) && EQ(-1, 1, 0) && EQ(-1, -1, 0) && EQ(1, 0, 1) && EQ(1, 0, -1) && EQ(-1, 0, 1) && EQ(-1, 0, -1) &&
+      EQ(0, 1, 1) && EQ(0, 1, -1) && EQ(0, -1, 1) && EQ(0, -1, -1)) {
+#undef EQ
     kap[q] = -0.0;
     return;
   }

@@ -113,11 +113,11 @@ __global__ void k_swp_flux(const double *__restrict__ us, const double *__restri
   const double a2 = us[q + sd] * tauh;
   const double c0 = cc[q];
   double f1 = 0.0, f2 = 0.0, f3 = 0.0;
-  if (c0 == 1.0) {
+  if (is_one_bits(c0)) {
     f1 = dmax1(-a1, 0.0);
     f2 = 1.0 - dmax1(a1, 0.0) + dmin1(a2, 0.0);
     f3 = dmax1(a2, 0.0);
-  } else if (c0 > 0.0) {
+  } else if (positive_bits(c0)) {
 #define C(di, dj, dk) cc[q + (long)(di) + (long)(dj) * sy + (long)(dk) * sz]
     double mm1, mm2, mx, my, mz;
     mm1 = C(-1, -1, -1) + C(-1, -1, 1) + C(-1, 1, -1) + C(-1, 1, 1) +
