@@ -766,7 +766,8 @@ int dsg_create(const dsg_config *cfg, dsg_ctx **out) {
   const size_t fine = up((size_t)cfg->nx * cfg->ny * cfg->nz * sizeof(double));
   const int nextra = DSG_NFIELDS - 8 + 1;  // fine fields beyond the level arrays + ccf
   total += nextra * fine;
-  total += up(dsg::kRedBlocks * 4 * sizeof(double)) + up(16 * sizeof(double)) + up(sizeof(unsigned long long));
+  total += up(dsg::kRedBlocks * 4 * sizeof(double)) + up(16 * sizeof(double)) + up(sizeof(unsigned long long)) +
+           up(sizeof(unsigned));
   cudaError_t e = cudaMalloc(&ctx->arena, total);
   if (e != cudaSuccess) {
     int rc = dsg::cuda_fail(ctx, e, "cudaMalloc(arena)");
@@ -798,6 +799,8 @@ int dsg_create(const dsg_config *cfg, dsg_ctx **out) {
   ctx->red_out = (double *)p;
   p += up(16 * sizeof(double));
   ctx->stop_flag = (unsigned long long *)p;
+  p += up(sizeof(unsigned long long));
+  ctx->iface_count = (unsigned *)p;
   e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMallocHost(&ctx->red_host, 16 * sizeof(double));
   if (e == cudaSuccess) e = cudaMemsetAsync(ctx->arena, 0, total, ctx->own_stream);
@@ -958,7 +961,8 @@ int dsg_vofmethod(dsg_ctx *ctx) {
   else if (s.tswap % 2 == 0) { order[0] = 2; order[1] = 3; order[2] = 1; }
   else { order[0] = 1; order[1] = 2; order[2] = 3; }
   for (int q = 0; q < 3; q++)
-    DSG_CK(ctx, dsg::swp(vel[order[q]], cc, s1, s2, s3, order[q], d, s.tauh, ctx->stream));
+    DSG_CK(ctx, dsg::swp(vel[order[q]], cc, s1, s2, s3, order[q], d, s.tauh, reinterpret_cast<unsigned *>(ctx->ccf),
+                         ctx->iface_count, ctx->stream));
   DSG_CK(ctx, dsg::bc_c(cc, d, ctx->stream));
   // turbulent diffusion of the volume fraction (main.f:820)
   if (ctx->cfg.iturb != 0)

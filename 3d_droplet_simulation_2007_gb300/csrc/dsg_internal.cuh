@@ -122,8 +122,9 @@ cudaError_t fill_zero(double *f, size_t n, cudaStream_t st);
 
 // vof.cu
 cudaError_t bc_c(double *cc, Dims d, cudaStream_t st);
+// list/count: scratch of the interface-cell list (>= interior cells) and its length
 cudaError_t swp(const double *us, double *cc, double *vof1, double *vof2, double *vof3, int dir, Dims d,
-                double tauh, cudaStream_t st);
+                double tauh, unsigned *list, unsigned *count, cudaStream_t st);
 cudaError_t calcrho(double *rhon, double *mun, const double *cc, Dims d, double rho1, double rho2,
                     double mu1, double mu2, cudaStream_t st);
 // csf.cu (S = {S11,S22,S33,S12,S13,S23})
@@ -247,6 +248,7 @@ struct dsg_ctx {
   double *red_out;            // device reduction results (8 doubles)
   double *red_host;           // pinned host mirror of red_out
   unsigned long long *stop_flag;  // device: first cell where CalcH3d would STOP (code << 48 | index)
+  unsigned *iface_count;          // device: length of the VOF sweep's interface-cell list (held in ccf)
   void *arena;
   size_t arena_bytes;
   cudaStream_t stream;

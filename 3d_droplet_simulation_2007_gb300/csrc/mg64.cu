@@ -390,13 +390,23 @@ __global__ void k_fold(const double *__restrict__ partials, double *__restrict__
 }
 
 // Interior cell of flat interior index t (i fastest).
+// Interior cell t -> (i, j, k) with 32-bit division (interior counts stay
+// below 2^32; 64-bit division is a long instruction sequence).
 __device__ __forceinline__ size_t interior_cell(size_t t, Dims d, int &i, int &j, int &k) {
-  const size_t ni = (size_t)(d.nx - 2), nj = (size_t)(d.ny - 2);
-  i = (int)(t % ni) + 2;
-  const size_t r = t / ni;
-  j = (int)(r % nj) + 2;
-  k = (int)(r / nj) + 2;
+  const unsigned ni = (unsigned)(d.nx - 2), nj = (unsigned)(d.ny - 2), tt = (unsigned)t;
+  const unsigned r = tt / ni;
+  i = (int)(tt - r * ni) + 2;
+  const unsigned kk = r / nj;
+  j = (int)(r - kk * nj) + 2;
+  k = (int)kk + 2;
   return d.ix(i, j, k);
+}
+
+// |x| as an ordered integer: the bit pattern of a non-negative double orders
+// like its value, so maxima of |x| run on the integer pipe (a NaN is the
+// largest pattern and propagates).
+__device__ __forceinline__ long long abs_bits(double x) {
+  return __double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFLL;
 }
 
 __global__ void k_relres_partial(double *__restrict__ partials, const double *__restrict__ u,
@@ -433,14 +443,15 @@ __global__ void k_sum_partial(double *__restrict__ partials, const double *__res
 __global__ void k_absmax3_partial(double *__restrict__ partials, const double *__restrict__ f0,
                                   const double *__restrict__ f1, const double *__restrict__ f2, Dims d) {
   const size_t n = (size_t)(d.nx - 2) * (d.ny - 2) * (d.nz - 2);
-  double v[1] = {0.0};
+  long long m = 0;
   for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
     int i, j, k;
     const size_t q = interior_cell(t, d, i, j, k);
-    v[0] = fmax(v[0], fabs(f0[q]));
-    if (f1) v[0] = fmax(v[0], fabs(f1[q]));
-    if (f2) v[0] = fmax(v[0], fabs(f2[q]));
+    m = max(m, abs_bits(f0[q]));
+    if (f1) m = max(m, abs_bits(f1[q]));
+    if (f2) m = max(m, abs_bits(f2[q]));
   }
+  double v[1] = {__longlong_as_double(m)};
   block_max_store<1>(v, partials);
 }
 
@@ -449,13 +460,14 @@ __global__ void k_divmax_partial(double *__restrict__ partials, const double *__
                                  double hi2) {
   const size_t n = (size_t)(d.nx - 2) * (d.ny - 2) * (d.nz - 2);
   const size_t sy = d.sy(), sz = d.sz();
-  double v[1] = {-1.0};
+  long long m = 0;
   for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
     int i, j, k;
     const size_t q = interior_cell(t, d, i, j, k);
     const double dv = (u[q + 1] - u[q] + v_[q + sy] - v_[q] + w[q + sz] - w[q]) * hi2;
-    v[0] = fmax(v[0], fabs(dv));
+    m = max(m, abs_bits(dv));
   }
+  double v[1] = {__longlong_as_double(m)};
   block_max_store<1>(v, partials);
 }
 
