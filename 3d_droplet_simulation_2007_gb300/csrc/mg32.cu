@@ -430,10 +430,10 @@ __global__ void k_defect64(float *__restrict__ r_ev, float *__restrict__ r_od, S
   const size_t sy = d.sy(), sz = d.sz();
   double rr = 0.0, bb = 0.0;
   for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
-    const size_t ni = (size_t)(d.nx - 2), nj = (size_t)(d.ny - 2);
-    const int i = (int)(t % ni) + 2;
-    const size_t rem = t / ni;
-    const int j = (int)(rem % nj) + 2, k = (int)(rem / nj) + 2;
+    const unsigned ni = (unsigned)(d.nx - 2), nj = (unsigned)(d.ny - 2), tt = (unsigned)t;  // < 2^32 cells
+    const unsigned rem = tt / ni, kk = rem / nj;
+    const int i = (int)(tt - rem * ni) + 2;
+    const int j = (int)(rem - kk * nj) + 2, k = (int)kk + 2;
     const size_t q = d.ix(i, j, k);
     const double uc = p[q];
     const double xp = (i + 1 == d.nx) ? 0.0 : p[q + 1];

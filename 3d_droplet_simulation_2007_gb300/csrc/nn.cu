@@ -557,9 +557,10 @@ __global__ void k_sumsq(const double *__restrict__ f, double *__restrict__ sums,
   const size_t n = (size_t)(d.nx - 2) * (d.ny - 2) * (d.nz - 2);
   double s = 0.0;
   for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
-    const int i = (int)(t % (d.nx - 2)) + 2;
-    const size_t r = t / (d.nx - 2);
-    const int j = (int)(r % (d.ny - 2)) + 2, k = (int)(r / (d.ny - 2)) + 2;
+    const unsigned ni = (unsigned)(d.nx - 2), nj = (unsigned)(d.ny - 2), tt = (unsigned)t;
+    const unsigned r = tt / ni, kk = r / nj;
+    const int i = (int)(tt - r * ni) + 2;
+    const int j = (int)(r - kk * nj) + 2, k = (int)kk + 2;
     const double v = f[d.ix(i, j, k)];
     s += v * v;
   }

@@ -249,7 +249,9 @@ __global__ void k_swp_update(double *__restrict__ cc, const double *__restrict__
   const size_t q = d.ix(i, j, k);
   const size_t sd = D == 1 ? 1 : (D == 2 ? d.sy() : d.sz());
   const double x = vof3[q - sd] + vof2[q] + vof1[q + sd];
-  cc[q] = dmax1(0.0, dmin1(1.0, x));
+  // dmax1(0, dmin1(1, x)) on the bit patterns (same result for every non-NaN x)
+  const double y = __double_as_longlong(x) >= 0x3FF0000000000000LL ? 1.0 : x;
+  cc[q] = __double_as_longlong(y) <= 0LL ? 0.0 : y;
 }
 
 // bc_c, three ordered steps (main.f:4340-4395 without the dead filter block).
