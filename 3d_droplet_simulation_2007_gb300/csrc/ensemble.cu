@@ -57,8 +57,10 @@ using Clock = std::chrono::steady_clock;
 // launch latency on this path), bandwidth-bound above.
 double model_cost(const dsg_ctx *c) { return (double)(c->nx - 2) * (c->ny - 2) * (c->nz - 2) + 2.0e6; }
 
-void worker_main(dsg_ensemble *e, int w) {
-  long long seen = 0;
+// A worker starts at generation gen0 (the ensemble's generation when the pool
+// was built): it steps only for generations announced after that.
+void worker_main(dsg_ensemble *e, int w, long long gen0) {
+  long long seen = gen0;
   for (;;) {
     std::vector<int> mine;
     int t;
@@ -132,7 +134,7 @@ int dsg_ensemble_set_workers(dsg_ensemble *e, int workers) {
   e->workers = workers;
   e->busy = 0;
   try {
-    for (int w = 0; w < workers; w++) e->th.emplace_back(worker_main, e, w);
+    for (int w = 0; w < workers; w++) e->th.emplace_back(worker_main, e, w, e->gen);
   } catch (...) {
     stop_workers(e);
     e->workers = 0;

@@ -155,16 +155,19 @@ __global__ void k_resid_restrict32_split(float *__restrict__ rhs_c, float *__res
 }
 
 // Fine (split) u = or += injection of the coarse correction.
+// One thread per colour-split index (m, j, k): its even and odd cells are
+// i = 2+2m and 3+2m in some order, both children of coarse cell m+2 along x,
+// so both arrays are updated with coalesced accesses.
 __global__ void k_prolong32_split(float *__restrict__ ue, float *__restrict__ uo, const float *__restrict__ uc,
                                   Dims df, Split sp, Dims dc, int add) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
   const int k = blockIdx.z + 2;
-  if (i > df.nx - 1 || j > df.ny - 1) return;
-  const float v = uc[dc.ix((i >> 1) + 1, (j >> 1) + 1, (k >> 1) + 1)];
-  float *dst = ((i + j + k) & 1) ? uo : ue;
-  const size_t q = sp.at((i - 2) >> 1, j, k);
-  dst[q] = add ? dst[q] + v : v;
+  if (m >= sp.hx || j > df.ny - 1) return;
+  const float v = uc[dc.ix(m + 2, (j >> 1) + 1, (k >> 1) + 1)];
+  const size_t q = sp.at(m, j, k);
+  ue[q] = add ? ue[q] + v : v;
+  uo[q] = add ? uo[q] + v : v;
 }
 
 // 8-cell mean of the split fine rhs into the coarse interior (rstrct).
@@ -576,7 +579,9 @@ cudaError_t resid_restrict32_split(float *rhs_c, float *u_c, float *const u[2], 
 cudaError_t prolong32_split(float *const u[2], const float *uc, Dims df, int add, cudaStream_t st) {
   const Dims dc{df.nx / 2 + 1, df.ny / 2 + 1, df.nz / 2 + 1};
   const Split sp{(df.nx - 2) >> 1, df.ny - 2, df.nz - 2};
-  DSG_COUNT k_prolong32_split<<<interior_grid(df, kBlk), kBlk, 0, st>>>(u[0], u[1], uc, df, sp, dc, add);
+  const dim3 grid((unsigned)((sp.hx + kBlk.x - 1) / kBlk.x), (unsigned)((df.ny - 2 + kBlk.y - 1) / kBlk.y),
+                  (unsigned)(df.nz - 2));
+  DSG_COUNT k_prolong32_split<<<grid, kBlk, 0, st>>>(u[0], u[1], uc, df, sp, dc, add);
   return cudaGetLastError();
 }
 
