@@ -198,6 +198,10 @@ inline float omega32(const dsg_ctx *ctx) {
 inline int pre32(const dsg_ctx *ctx) { return ctx->cfg.mg32_npre > 0 ? ctx->cfg.mg32_npre : ctx->s.npre; }
 inline int post32(const dsg_ctx *ctx) { return ctx->cfg.mg32_npost > 0 ? ctx->cfg.mg32_npost : ctx->s.npost; }
 
+// Prolongation of the FP32 V-cycles and FMG start: trilinear unless the
+// configuration asks for the reference's injection.
+inline int tri32(const dsg_ctx *ctx) { return ctx->cfg.mg32_prolong == 1 ? 0 : 1; }
+
 inline float level_h2(dsg_ctx *ctx, int l) {
   const double h1 = ctx->s.lengthsize / (ctx->lnx[l] - 2);
   return (float)(h1 * h1);
@@ -300,6 +304,7 @@ void tail_args(dsg_ctx *ctx, int top, dsg::TailArgs *A) {
   A->npost = post32(ctx);
   A->ntop = ctx->s.ntop;
   A->omega = omega32(ctx);
+  A->tri = tri32(ctx);
 }
 
 int vcycle32(dsg_ctx *ctx, int j) {
@@ -332,9 +337,9 @@ int vcycle32(dsg_ctx *ctx, int j) {
   for (int jj = jt >= 1 ? jt + 1 : 2; jj <= j; jj++) {
     if (jj == ng) {
       FineSplit f = fine_split(ctx);
-      DSG_CK(ctx, dsg::prolong32_split(f.u, ctx->lv32[jj - 1][U32], ctx->level(jj), 1, st));
+      DSG_CK(ctx, dsg::prolong32_split(f.u, ctx->lv32[jj - 1][U32], ctx->level(jj), 1, tri32(ctx), st));
     } else {
-      DSG_CK(ctx, dsg::addint32(ctx->lv32[jj][U32], ctx->lv32[jj - 1][U32], ctx->level(jj), st));
+      DSG_CK(ctx, dsg::prolong32(ctx->lv32[jj][U32], ctx->lv32[jj - 1][U32], ctx->level(jj), 1, tri32(ctx), st));
     }
     DSG_CK(ctx, relax32_level(ctx, post32(ctx), jj));
   }
@@ -470,9 +475,9 @@ int fmg32(dsg_ctx *ctx) {
   DSG_CK(ctx, relax32_level(ctx, ctx->s.ntop, 1));
   for (int j = 2; j <= ng; j++) {
     if (j == ng)
-      DSG_CK(ctx, dsg::prolong32_split(f.u, ctx->lv32[j - 1][U32], ctx->level(j), 0, st));
+      DSG_CK(ctx, dsg::prolong32_split(f.u, ctx->lv32[j - 1][U32], ctx->level(j), 0, tri32(ctx), st));
     else
-      DSG_CK(ctx, dsg::interp32(ctx->lv32[j][U32], ctx->lv32[j - 1][U32], ctx->level(j), st));
+      DSG_CK(ctx, dsg::prolong32(ctx->lv32[j][U32], ctx->lv32[j - 1][U32], ctx->level(j), 0, tri32(ctx), st));
     for (int c = 0; c < ctx->cfg.cycles; c++) {
       int rc = vcycle32(ctx, j);
       if (rc) return rc;

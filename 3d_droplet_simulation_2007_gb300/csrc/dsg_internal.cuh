@@ -165,8 +165,8 @@ cudaError_t relax32_n(int n, float *u, float h2, const float *rhs, const float *
                       const float *ei, Dims d, float omega, cudaStream_t st);
 cudaError_t resid_restrict32(float *rhs_c, float *u_c, const float *u, const float *rhs, const float *a,
                              const float *b, const float *c, Dims df, float h2i, cudaStream_t st);
-cudaError_t addint32(float *uf, const float *uc, Dims df, cudaStream_t st);
-cudaError_t interp32(float *uf, const float *uc, Dims df, cudaStream_t st);
+// fine u = (add = 0) or += (add = 1) the coarse correction, trilinear (tri) or injected
+cudaError_t prolong32(float *uf, const float *uc, Dims df, int add, int tri, cudaStream_t st);
 cudaError_t restrict32(float *uc, const float *uf, Dims dc, cudaStream_t st);
 cudaError_t acfromac32(float *a, float *b, float *c, float *ei, const float *a2, const float *b2, const float *c2,
                        Dims dc, cudaStream_t st);
@@ -185,6 +185,7 @@ struct TailArgs {
   TailLevel lv[kTailMaxLevels + 1];  // 1..top
   int top, npre, npost, ntop;
   float omega;
+  int tri;  // trilinear prolongation (else injection)
 };
 cudaError_t vtail32(const TailArgs &args, cudaStream_t st);
 // finest level in colour-split storage ({even, odd} arrays of (nx-2)/2 x (ny-2) x (nz-2))
@@ -192,7 +193,7 @@ cudaError_t relax32_split_n(int n, float *const u[2], float *const rhs[2], const
                             float omega, float r1, float r2, cudaStream_t st);
 cudaError_t resid_restrict32_split(float *rhs_c, float *u_c, float *const u[2], float *const rhs[2], const float *cc,
                                    Dims df, float h2i, float r1, float r2, cudaStream_t st);
-cudaError_t prolong32_split(float *const u[2], const float *uc, Dims df, int add, cudaStream_t st);
+cudaError_t prolong32_split(float *const u[2], const float *uc, Dims df, int add, int tri, cudaStream_t st);
 cudaError_t restrict32_split(float *uc, float *const rhs[2], Dims dc, cudaStream_t st);
 cudaError_t split_from64(float *const dst[2], const double *src, Dims d, cudaStream_t st);
 cudaError_t defect64(float *const r32[2], double *out2, double *partials, const double *p, const double *rhs,

@@ -95,6 +95,8 @@ typedef struct dsg_config {
   double mg32_omega;   /* relaxation factor of the FP32 V-cycles of the mixed modes (<= 0: omega) */
   int mg32_npre;       /* pre-/post-sweeps of the FP32 V-cycles (<= 0: the adaptive NPRE/NPOST) */
   int mg32_npost;
+  int mg32_prolong;    /* prolongation of the FP32 V-cycles and FMG start: 0 = trilinear, 1 = the
+                          reference's piecewise-constant injection (interp/addint) */
 } dsg_config;
 
 /* Non-dimensional scalars and adaptive counters (COMMON /PHYSICS/, /DIFF/,

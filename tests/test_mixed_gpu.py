@@ -25,13 +25,15 @@ def _sync_state(gpu, ora):
     gpu.set_scalars(s)
 
 
-@pytest.mark.parametrize("n", [16, 32])
-def test_mixed_matches_fp64_oracle(gpu_lib, n):
+@pytest.mark.parametrize("n,prolong", [(16, 0), (32, 0), (32, 1)])
+def test_mixed_matches_fp64_oracle(gpu_lib, n, prolong):
+    """prolong 0: trilinear FP32 prolongation, 1: the reference's injection."""
     dsg = gpu_lib
     from oracle import Oracle
     tol = 1e-10
     ora = Oracle(dsg.config.droplet(n, mode=dsg.config.MODE_TOL_FP64, tol=tol).as_dict())
-    gpu = dsg.Solver(dsg.config.droplet(n, mode=dsg.config.MODE_TOL_MIXED, tol=tol), init=False)
+    gpu = dsg.Solver(dsg.config.droplet(n, mode=dsg.config.MODE_TOL_MIXED, tol=tol).replace(mg32_prolong=prolong),
+                     init=False)
     for t in range(1, 6):
         _sync_state(gpu, ora)
         ora.step(t)
@@ -57,14 +59,15 @@ def test_mixed_free_run_volume(gpu_lib):
     assert relerr(gpu.field("p"), ora.field("p")) < 1e-5
 
 
-@pytest.mark.parametrize("n,tail", [(32, 0), (48, 0), (64, 0), (64, 10 ** 6)])
-def test_coarse_tail_is_bit_identical(gpu_lib, n, tail):
+@pytest.mark.parametrize("n,tail,prolong", [(32, 0, 0), (48, 0, 0), (64, 0, 0), (64, 10 ** 6, 0), (64, 10 ** 6, 1)])
+def test_coarse_tail_is_bit_identical(gpu_lib, n, tail, prolong):
     """The single-block coarse tail computes the same bits as one launch per
     pass, with fewer launches.  tail=10**6 runs every level below the finest
-    in the tail kernel."""
+    in the tail kernel.  prolong: 0 trilinear, 1 injection."""
     dsg = gpu_lib
     lib = dsg.load()
-    base = dsg.config.droplet(n, mode=dsg.config.MODE_TOL_MIXED, tol=1e-9, impact_speed=2.0)
+    base = dsg.config.droplet(n, mode=dsg.config.MODE_TOL_MIXED, tol=1e-9, impact_speed=2.0).replace(
+        mg32_prolong=prolong)
     runs = {}
     for key, tn in (("pass", -1), ("tail", tail)):
         with dsg.Solver(base.replace(tail_nodes=tn)) as s:
