@@ -95,6 +95,8 @@ class InputData:
     mg32_npre: int = 5
     mg32_npost: int = 5
     mg32_prolong: int = 0
+    # V-cycles per level of the FP32 FMG start (0: cycles)
+    mg32_fmg_cycles: int = 0
 
     def as_dict(self):
         return asdict(self)

@@ -478,7 +478,8 @@ int fmg32(dsg_ctx *ctx) {
       DSG_CK(ctx, dsg::prolong32_split(f.u, ctx->lv32[j - 1][U32], ctx->level(j), 0, tri32(ctx), st));
     else
       DSG_CK(ctx, dsg::prolong32(ctx->lv32[j][U32], ctx->lv32[j - 1][U32], ctx->level(j), 0, tri32(ctx), st));
-    for (int c = 0; c < ctx->cfg.cycles; c++) {
+    const int cycles = ctx->cfg.mg32_fmg_cycles > 0 ? ctx->cfg.mg32_fmg_cycles : ctx->cfg.cycles;
+    for (int c = 0; c < cycles; c++) {
       int rc = vcycle32(ctx, j);
       if (rc) return rc;
     }
@@ -744,6 +745,10 @@ int dsg_create(const dsg_config *cfg, dsg_ctx **out) {
     return dsg::set_error(nullptr, DSG_E_ARG, "hswitch = %d is not available (0 or 1)", cfg->hswitch);
   if (cfg->iturb != 0 && cfg->iturb != 3)
     return dsg::set_error(nullptr, DSG_E_ARG, "iturb = %d is not available (0: laminar, 3: k-epsilon)", cfg->iturb);
+  // the kernels index cells with 32-bit offsets (a grid of 2^31 nodes would
+  // need over 500 GB of fields)
+  if ((size_t)cfg->nx * cfg->ny * cfg->nz >= ((size_t)1 << 31))
+    return dsg::set_error(nullptr, DSG_E_ARG, "grid %dx%dx%d has 2^31 nodes or more", cfg->nx, cfg->ny, cfg->nz);
   // memoryaloc, main.f:284-298 (generalised to sides that are not 2^k+2)
   const int ng = dsg::level_count(cfg->nx, cfg->ny, cfg->nz);
   if (ng < 1) return dsg::set_error(nullptr, DSG_E_ARG, "grid %dx%dx%d too small", cfg->nx, cfg->ny, cfg->nz);
