@@ -87,16 +87,20 @@ class InputData:
     warm_start: int = 0
     # FP32 V-cycles of the mixed modes (the FP64 defect correction's inner
     # solver): trilinear prolongation (0; 1 = the reference's injection),
-    # relaxation factor 1.6 and 5 pre-/post-sweeps.  Fastest in a sweep on the
-    # 256^3 splash: 5 V-cycles and 19.4 ms per step, against 8-9 V-cycles and
-    # 22.5 ms with injection, V(4,4), omega 1.4 (omega 1.3-1.8 and V(3,3) to
-    # V(8,8) measured).
-    mg32_omega: float = 1.6
-    mg32_npre: int = 5
-    mg32_npost: int = 5
+    # relaxation factor 1.5, 3 pre-/post-sweeps on the finest level and 8 on
+    # the coarser ones (mg32_fine_npre/npost below).  Fastest in sweeps on the
+    # 256^3 splash: 4 V-cycles and 17.2 ms per step, against 5 V-cycles and
+    # 18.8 ms with V(5,5) on every level at omega 1.6, and 8-9 V-cycles and
+    # 22.5 ms with injection, V(4,4), omega 1.4.
+    mg32_omega: float = 1.5
+    mg32_npre: int = 8
+    mg32_npost: int = 8
     mg32_prolong: int = 0
     # V-cycles per level of the FP32 FMG start (0: cycles)
     mg32_fmg_cycles: int = 0
+    # sweeps of the FP32 V-cycles on the finest level (0: mg32_npre/mg32_npost)
+    mg32_fine_npre: int = 3
+    mg32_fine_npost: int = 3
 
     def as_dict(self):
         return asdict(self)

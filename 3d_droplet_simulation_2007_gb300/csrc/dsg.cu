@@ -198,6 +198,15 @@ inline float omega32(const dsg_ctx *ctx) {
 inline int pre32(const dsg_ctx *ctx) { return ctx->cfg.mg32_npre > 0 ? ctx->cfg.mg32_npre : ctx->s.npre; }
 inline int post32(const dsg_ctx *ctx) { return ctx->cfg.mg32_npost > 0 ? ctx->cfg.mg32_npost : ctx->s.npost; }
 
+// Sweeps on level l: the finest level may have its own counts (its sweeps
+// cost 8x a coarse level's).
+inline int pre32(const dsg_ctx *ctx, int l) {
+  return (l == ctx->ng && ctx->cfg.mg32_fine_npre > 0) ? ctx->cfg.mg32_fine_npre : pre32(ctx);
+}
+inline int post32(const dsg_ctx *ctx, int l) {
+  return (l == ctx->ng && ctx->cfg.mg32_fine_npost > 0) ? ctx->cfg.mg32_fine_npost : post32(ctx);
+}
+
 // Prolongation of the FP32 V-cycles and FMG start: trilinear unless the
 // configuration asks for the reference's injection.
 inline int tri32(const dsg_ctx *ctx) { return ctx->cfg.mg32_prolong == 1 ? 0 : 1; }
@@ -317,7 +326,7 @@ int vcycle32(dsg_ctx *ctx, int j) {
   for (int jj = j; jj >= 2 && jj > jt; jj--) {
     float **L = ctx->lv32[jj];
     float **Lc = ctx->lv32[jj - 1];
-    DSG_CK(ctx, relax32_level(ctx, pre32(ctx), jj));
+    DSG_CK(ctx, relax32_level(ctx, pre32(ctx, jj), jj));
     if (jj == ng) {
       FineSplit f = fine_split(ctx);
       DSG_CK(ctx, dsg::resid_restrict32_split(Lc[RHS32], Lc[U32], f.u, f.r, L[A32], ctx->level(jj),
@@ -341,7 +350,7 @@ int vcycle32(dsg_ctx *ctx, int j) {
     } else {
       DSG_CK(ctx, dsg::prolong32(ctx->lv32[jj][U32], ctx->lv32[jj - 1][U32], ctx->level(jj), 1, tri32(ctx), st));
     }
-    DSG_CK(ctx, relax32_level(ctx, post32(ctx), jj));
+    DSG_CK(ctx, relax32_level(ctx, post32(ctx, jj), jj));
   }
   return DSG_OK;
 }
@@ -619,7 +628,7 @@ int mixed_solve(dsg_ctx *ctx, dsg_mg_stats *s) {
     key[4] = inner;
     rc = run(ctx->g_iter[inner], iterate);
     if (rc) return rc;
-    s->fine_sweeps += inner * (pre32(ctx) + post32(ctx));
+    s->fine_sweeps += inner * (pre32(ctx, ctx->ng) + post32(ctx, ctx->ng));
     n += inner;
     const double r_old = r;
     rc = defect_read(ctx, &r);

@@ -98,6 +98,9 @@ typedef struct dsg_config {
   int mg32_prolong;    /* prolongation of the FP32 V-cycles and FMG start: 0 = trilinear, 1 = the
                           reference's piecewise-constant injection (interp/addint) */
   int mg32_fmg_cycles; /* V-cycles per level of the FP32 FMG start (<= 0: CYCLES) */
+  int mg32_fine_npre;  /* pre-/post-sweeps of the FP32 V-cycles on the finest level (<= 0: as on the
+                          other levels) */
+  int mg32_fine_npost;
 } dsg_config;
 
 /* Non-dimensional scalars and adaptive counters (COMMON /PHYSICS/, /DIFF/,
