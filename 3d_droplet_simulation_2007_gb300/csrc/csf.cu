@@ -72,9 +72,21 @@ __global__ void k_csf_force(double *__restrict__ s11, double *__restrict__ s22, 
   if (i > d.nx - 1 || j > d.ny - 1) return;
   const size_t q = d.ix(i, j, k);
   const double kq = kap[q], fq = f[q];
-  s11[q] = sigh * (fq - f[q - 1]) * kq;
-  s22[q] = sigh * (fq - f[q - d.sy()]) * kq;
-  s33[q] = sigh * (fq - f[q - d.sz()]) * kq;
+  const double fx = f[q - 1], fy = f[q - d.sy()], fz = f[q - d.sz()];
+  if (same_bits(fx, fq) && same_bits(fy, fq) && same_bits(fz, fq)) {
+    // bulk cell: every difference is +0, so each force is (sigh * +0) * kappa,
+    // a zero whose sign is sign(sigh) xor sign(kappa) (kappa is finite),
+    // formed on the integer pipe
+    const double z = __longlong_as_double((__double_as_longlong(sigh) ^ __double_as_longlong(kq)) &
+                                          (long long)0x8000000000000000ULL);
+    s11[q] = z;
+    s22[q] = z;
+    s33[q] = z;
+    return;
+  }
+  s11[q] = sigh * (fq - fx) * kq;
+  s22[q] = sigh * (fq - fy) * kq;
+  s33[q] = sigh * (fq - fz) * kq;
 }
 
 // bc_tensor, three ordered steps.

@@ -194,18 +194,22 @@ __global__ void k_swp_flux(const double *__restrict__ us, const double *__restri
     if (iface) list[base + __popc(mask & ((1u << lane) - 1u))] = (unsigned)q;
   }
   if (!inside || iface) return;
+  if (!is_one_bits(c0)) {
+    // empty cell: no flux.  It returns before the velocity loads and the
+    // FP64 arithmetic of full cells, which the compiler otherwise if-converts
+    // so that every cell executes them (measured: 9 FP64 operations per cell
+    // and 279 us per y/z sweep at 256^3, against 101 us).
+    vof1[q] = 0.0;
+    vof2[q] = 0.0;
+    vof3[q] = 0.0;
+    return;
+  }
   const long sd = D == 1 ? 1 : (D == 2 ? (long)d.sy() : (long)d.sz());
   const double a1 = us[q] * tauh;
   const double a2 = us[q + sd] * tauh;
-  double f1 = 0.0, f2 = 0.0, f3 = 0.0;
-  if (is_one_bits(c0)) {
-    f1 = dmax1(-a1, 0.0);
-    f2 = 1.0 - dmax1(a1, 0.0) + dmin1(a2, 0.0);
-    f3 = dmax1(a2, 0.0);
-  }
-  vof1[q] = f1;
-  vof2[q] = f2;
-  vof3[q] = f3;
+  vof1[q] = dmax1(-a1, 0.0);
+  vof2[q] = 1.0 - dmax1(a1, 0.0) + dmin1(a2, 0.0);
+  vof3[q] = dmax1(a2, 0.0);
 }
 
 // Sweep fluxes, pass 2: the listed interface cells, one per thread.
