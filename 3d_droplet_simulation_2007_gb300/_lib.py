@@ -118,6 +118,7 @@ SIGNATURES = [
     ("dsg_solvelpres", _i, [_vp, _i, C.POINTER(DsgMgStats)]),
     ("dsg_mglin", _i, [_vp, C.POINTER(DsgMgStats)]),
     ("dsg_step", _i, [_vp, _i, C.POINTER(DsgMgStats)]),
+    ("dsg_step_host", _i, [_vp, _i, C.POINTER(DsgMgStats), _i, _IP, C.POINTER(_vp), _i, _IP, C.POINTER(_vp)]),
     ("dsg_liquid_volume", _i, [_vp, _DPP]),
     ("dsg_max_divergence", _i, [_vp, _DPP]),
     ("dsg_relres", _i, [_vp, _DPP]),

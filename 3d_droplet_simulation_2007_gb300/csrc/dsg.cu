@@ -853,6 +853,15 @@ void dsg_destroy(dsg_ctx *ctx) {
   if (!ctx) return;
   if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
   dsg::snapshot_release(ctx);
+  if (ctx->xfer_stream) {
+    cudaStreamSynchronize(ctx->xfer_stream);
+    cudaStreamDestroy(ctx->xfer_stream);
+  }
+  for (int q = 0; q < dsg_ctx::kStepPhases; q++) {
+    if (ctx->xfer_in[q]) cudaEventDestroy(ctx->xfer_in[q]);
+    if (ctx->xfer_done[q]) cudaEventDestroy(ctx->xfer_done[q]);
+  }
+  if (ctx->xfer_start) cudaEventDestroy(ctx->xfer_start);
   for (cudaEvent_t e : ctx->prof_ev) cudaEventDestroy(e);
   for (cudaEvent_t e : ctx->phase_ev) cudaEventDestroy(e);
   graph_release(ctx->g_first);
@@ -1143,10 +1152,25 @@ int dsg_solvelpres(dsg_ctx *ctx, int t, dsg_mg_stats *stats) {
   return mg_rc;
 }
 
-int dsg_step(dsg_ctx *ctx, int t, dsg_mg_stats *stats) {
-  if (!ctx) return DSG_E_ARG;
+}  // extern "C"
+
+namespace {
+
+// Phases of a time step in the order of the main.f:19-73 loop body: VOF
+// (VOFmethod, CalcH3d, kepsmodel), CFL (checktime), surface tension (csf /
+// sgip / sgip2) and pressure (solvelpres).
+enum { PH_VOF = 0, PH_CFL = 1, PH_CSF = 2, PH_PRES = 3 };
+
+// One time step; hook(phase, after) runs before (after = false) and after
+// (after = true) each phase and may add stream dependencies.  A pressure
+// solve that stops at its cycle cap still completes the step and its
+// DSG_E_NOT_CONVERGED is returned after the last hook.
+template <class Hook>
+int step_phases(dsg_ctx *ctx, int t, dsg_mg_stats *stats, Hook &&hook) {
+  int rc = hook(PH_VOF, false);
+  if (rc) return rc;
   DSG_CK(ctx, phase_mark(ctx, 0));
-  int rc = dsg_vofmethod(ctx);
+  rc = dsg_vofmethod(ctx);
   if (rc) return rc;
   if (ctx->cfg.hswitch == 1) {
     rc = dsg_calch3d(ctx);
@@ -1154,15 +1178,121 @@ int dsg_step(dsg_ctx *ctx, int t, dsg_mg_stats *stats) {
   }
   rc = dsg_kepsmodel(ctx);
   if (rc) return rc;
+  if ((rc = hook(PH_VOF, true)) || (rc = hook(PH_CFL, false))) return rc;
   DSG_CK(ctx, phase_mark(ctx, 1));
   rc = dsg_checktime(ctx);
   if (rc) return rc;
+  if ((rc = hook(PH_CFL, true)) || (rc = hook(PH_CSF, false))) return rc;
   DSG_CK(ctx, phase_mark(ctx, 2));
   rc = dsg_csf(ctx);
   if (rc) return rc;
+  if ((rc = hook(PH_CSF, true)) || (rc = hook(PH_PRES, false))) return rc;
   rc = dsg_solvelpres(ctx, t, stats);
+  if (rc && rc != DSG_E_NOT_CONVERGED) return rc;
   DSG_CK(ctx, phase_mark(ctx, -1));
-  return rc;
+  const int rh = hook(PH_PRES, true);
+  return rh ? rh : rc;
+}
+
+// First phase that reads or writes field f: a field copied in from the host
+// must have arrived before that phase starts.  (The stress components S12,
+// S13, S23 are first read by solvelpres's stress update; with sigma = 0 the
+// surface-tension phase already zeroes all six.)
+int first_touch(const dsg_ctx *ctx, int f) {
+  switch (f) {
+    case DSG_F_S11: case DSG_F_S22: case DSG_F_S33:
+      return PH_CSF;
+    case DSG_F_S12: case DSG_F_S13: case DSG_F_S23:
+      return ctx->s.sigma == 0.0 ? PH_CSF : PH_PRES;
+    case DSG_F_A: case DSG_F_B: case DSG_F_C: case DSG_F_PPREV: case DSG_F_PPREV2:
+      return PH_PRES;
+    default:
+      return PH_VOF;
+  }
+}
+
+// Last phase that writes field f: it can be copied out once that phase is done.
+int last_write(int f) {
+  switch (f) {
+    case DSG_F_CC: case DSG_F_RHON: case DSG_F_MUN: case DSG_F_KTUR: case DSG_F_EPS: case DSG_F_MUT:
+    case DSG_F_HXMIN: case DSG_F_HXMAX: case DSG_F_HYMIN: case DSG_F_HYMAX: case DSG_F_HZMIN: case DSG_F_HZMAX:
+      return PH_VOF;
+    default:
+      return PH_PRES;
+  }
+}
+
+int xfer_resources(dsg_ctx *ctx) {
+  if (ctx->xfer_stream) return DSG_OK;
+  DSG_CK(ctx, cudaEventCreateWithFlags(&ctx->xfer_start, cudaEventDisableTiming));
+  for (int q = 0; q < dsg_ctx::kStepPhases; q++) {
+    DSG_CK(ctx, cudaEventCreateWithFlags(&ctx->xfer_in[q], cudaEventDisableTiming));
+    DSG_CK(ctx, cudaEventCreateWithFlags(&ctx->xfer_done[q], cudaEventDisableTiming));
+  }
+  DSG_CK(ctx, cudaStreamCreateWithFlags(&ctx->xfer_stream, cudaStreamNonBlocking));
+  return DSG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dsg_step(dsg_ctx *ctx, int t, dsg_mg_stats *stats) {
+  if (!ctx) return DSG_E_ARG;
+  return step_phases(ctx, t, stats, [](int, bool) { return DSG_OK; });
+}
+
+int dsg_step_host(dsg_ctx *ctx, int t, dsg_mg_stats *stats, int n_in, const int *in_fields,
+                  const double *const *in_host, int n_out, const int *out_fields, double *const *out_host) {
+  if (!ctx) return DSG_E_ARG;
+  if (n_in < 0 || n_out < 0 || (n_in > 0 && (!in_fields || !in_host)) || (n_out > 0 && (!out_fields || !out_host)))
+    return dsg::set_error(ctx, DSG_E_ARG, "dsg_step_host: bad field lists");
+  for (int q = 0; q < n_in; q++)
+    if (in_fields[q] < 0 || in_fields[q] >= DSG_NFIELDS || !in_host[q])
+      return dsg::set_error(ctx, DSG_E_ARG, "dsg_step_host: bad input %d (field %d)", q, in_fields[q]);
+  for (int q = 0; q < n_out; q++)
+    if (out_fields[q] < 0 || out_fields[q] >= DSG_NFIELDS || !out_host[q])
+      return dsg::set_error(ctx, DSG_E_ARG, "dsg_step_host: bad output %d (field %d)", q, out_fields[q]);
+  int rc = xfer_resources(ctx);
+  if (rc) return rc;
+  cudaStream_t cs = ctx->xfer_stream;
+  const size_t bytes = ctx->fine().count() * sizeof(double);
+  // the copies start after the work already queued on the library's stream
+  DSG_CK(ctx, cudaEventRecord(ctx->xfer_start, ctx->stream));
+  DSG_CK(ctx, cudaStreamWaitEvent(cs, ctx->xfer_start, 0));
+  // inputs in the order the phases need them, one event after each phase's group
+  bool need[dsg_ctx::kStepPhases] = {};
+  for (int ph = 0; ph < dsg_ctx::kStepPhases; ph++) {
+    for (int q = 0; q < n_in; q++)
+      if (first_touch(ctx, in_fields[q]) == ph) {
+        DSG_CK(ctx, cudaMemcpyAsync(ctx->f[in_fields[q]], in_host[q], bytes, cudaMemcpyHostToDevice, cs));
+        need[ph] = true;
+      }
+    if (need[ph]) DSG_CK(ctx, cudaEventRecord(ctx->xfer_in[ph], cs));
+  }
+  auto hook = [&](int ph, bool after) -> int {
+    if (!after) {
+      if (need[ph]) DSG_CK(ctx, cudaStreamWaitEvent(ctx->stream, ctx->xfer_in[ph], 0));
+      return DSG_OK;
+    }
+    bool any = false;
+    for (int q = 0; q < n_out; q++) any = any || last_write(out_fields[q]) == ph;
+    if (!any) return DSG_OK;
+    DSG_CK(ctx, cudaEventRecord(ctx->xfer_done[ph], ctx->stream));
+    DSG_CK(ctx, cudaStreamWaitEvent(cs, ctx->xfer_done[ph], 0));
+    for (int q = 0; q < n_out; q++)
+      if (last_write(out_fields[q]) == ph)
+        DSG_CK(ctx, cudaMemcpyAsync(out_host[q], ctx->f[out_fields[q]], bytes, cudaMemcpyDeviceToHost, cs));
+    return DSG_OK;
+  };
+  rc = step_phases(ctx, t, stats, hook);
+  // no copy stays in flight into or out of the caller's buffers, also on errors
+  const cudaError_t e1 = cudaStreamSynchronize(cs);
+  const cudaError_t e2 = cudaStreamSynchronize(ctx->stream);
+  if (rc) return rc;
+  if (e1 != cudaSuccess) return dsg::cuda_fail(ctx, e1, "dsg_step_host copies");
+  if (e2 != cudaSuccess) return dsg::cuda_fail(ctx, e2, "dsg_step_host");
+  return DSG_OK;
 }
 
 int dsg_liquid_volume(dsg_ctx *ctx, double *out) {

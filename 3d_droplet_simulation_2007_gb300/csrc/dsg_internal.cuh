@@ -284,6 +284,13 @@ struct dsg_ctx {
   cudaEvent_t snap_ready = nullptr, snap_done = nullptr;
   bool snap_pending = false;
   int snap_t = -1;
+  // host-buffer step (dsg_step_host): copy stream, per-phase upload and
+  // phase-done events (created on first use)
+  static constexpr int kStepPhases = 4;
+  cudaStream_t xfer_stream = nullptr;
+  cudaEvent_t xfer_in[kStepPhases] = {};
+  cudaEvent_t xfer_done[kStepPhases] = {};
+  cudaEvent_t xfer_start = nullptr;
   dsg::Dims fine() const { return dsg::Dims{nx, ny, nz}; }
   dsg::Dims level(int l) const { return dsg::Dims{lnx[l], lny[l], lnz[l]}; }
 };

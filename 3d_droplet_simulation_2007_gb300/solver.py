@@ -171,6 +171,31 @@ class Solver:
         self.last_stats = st.as_dict()
         return self.last_stats
 
+    def step_host(self, inputs, outputs, t=None):
+        """dsg_step with the state exchanged through host arrays: `inputs` and
+        `outputs` map field names to contiguous float64 arrays of the field
+        size (page-locked for asynchronous copies).  The inputs are copied in
+        and the outputs out on a second stream, overlapped with the step."""
+        if t is None:
+            t = self.t + 1
+        n = self.shape[0] * self.shape[1] * self.shape[2]
+
+        def check(arr):
+            if arr.dtype != np.float64 or arr.size != n or not (arr.flags["F_CONTIGUOUS"] or arr.ndim == 1):
+                raise ValueError("step_host needs contiguous float64 arrays of the field size")
+            return arr.ctypes.data
+
+        ins, outs = list(inputs.items()), list(outputs.items())
+        fi = (C.c_int * max(1, len(ins)))(*[_lib.FIELD_ID[k] for k, _ in ins])
+        pi = (C.c_void_p * max(1, len(ins)))(*[check(a) for _, a in ins])
+        fo = (C.c_int * max(1, len(outs)))(*[_lib.FIELD_ID[k] for k, _ in outs])
+        po = (C.c_void_p * max(1, len(outs)))(*[check(a) for _, a in outs])
+        st = _lib.DsgMgStats()
+        self._ck(self.lib.dsg_step_host(self.ctx, t, C.byref(st), len(ins), fi, pi, len(outs), fo, po))
+        self.t = t
+        self.last_stats = st.as_dict()
+        return self.last_stats
+
     def run(self, steps):
         for _ in range(steps):
             self.step()

@@ -171,6 +171,18 @@ int dsg_solvelpres(dsg_ctx *ctx, int t, dsg_mg_stats *stats);
 int dsg_mglin(dsg_ctx *ctx, dsg_mg_stats *stats);
 /* One body of the main.f:19-73 loop with surfacet=2 (CSF), hswitch=0, laminar. */
 int dsg_step(dsg_ctx *ctx, int t, dsg_mg_stats *stats);
+/* dsg_step with the state exchanged through host arrays, as a host that owns
+   its fields (the reference's COMMON blocks) needs it: the fields
+   in_fields[0..n_in) are copied from in_host[q] and the fields
+   out_fields[0..n_out) to out_host[q], each a full nx*ny*nz FP64 array.  The
+   copies run on a second stream: each input is waited for only by the first
+   phase of the step that touches its field and each output is copied as soon
+   as the last phase that writes it is done, so most of the transfer overlaps
+   the step's kernels.  Returns once the outputs are on the host, also on
+   errors.  Page-locked host arrays (cudaHostRegister or cudaMallocHost) make
+   the copies asynchronous. */
+int dsg_step_host(dsg_ctx *ctx, int t, dsg_mg_stats *stats, int n_in, const int *in_fields,
+                  const double *const *in_host, int n_out, const int *out_fields, double *const *out_host);
 /* SUMFIELD(cc) main.f:4783-4801: liquid volume (FP64, deterministic order) */
 int dsg_liquid_volume(dsg_ctx *ctx, double *out);
 /* h * FMODMAX(div u) on the resident velocity (main.f:3389-3398) */
