@@ -101,6 +101,9 @@ class InputData:
     # sweeps of the FP32 V-cycles on the finest level (0: mg32_npre/mg32_npost)
     mg32_fine_npre: int = 3
     mg32_fine_npost: int = 3
+    # sweeps on the level below the finest (0: mg32_npre/mg32_npost)
+    mg32_mid_npre: int = 0
+    mg32_mid_npost: int = 0
 
     def as_dict(self):
         return asdict(self)

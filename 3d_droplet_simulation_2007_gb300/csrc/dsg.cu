@@ -198,13 +198,18 @@ inline float omega32(const dsg_ctx *ctx) {
 inline int pre32(const dsg_ctx *ctx) { return ctx->cfg.mg32_npre > 0 ? ctx->cfg.mg32_npre : ctx->s.npre; }
 inline int post32(const dsg_ctx *ctx) { return ctx->cfg.mg32_npost > 0 ? ctx->cfg.mg32_npost : ctx->s.npost; }
 
-// Sweeps on level l: the finest level may have its own counts (its sweeps
-// cost 8x a coarse level's).
+// Sweeps on level l: the finest level and the one below it may have their own
+// counts (a sweep there costs 8x and 2-3x one of the smaller levels, which
+// are bound by launch latency).
 inline int pre32(const dsg_ctx *ctx, int l) {
-  return (l == ctx->ng && ctx->cfg.mg32_fine_npre > 0) ? ctx->cfg.mg32_fine_npre : pre32(ctx);
+  if (l == ctx->ng && ctx->cfg.mg32_fine_npre > 0) return ctx->cfg.mg32_fine_npre;
+  if (l == ctx->ng - 1 && ctx->cfg.mg32_mid_npre > 0) return ctx->cfg.mg32_mid_npre;
+  return pre32(ctx);
 }
 inline int post32(const dsg_ctx *ctx, int l) {
-  return (l == ctx->ng && ctx->cfg.mg32_fine_npost > 0) ? ctx->cfg.mg32_fine_npost : post32(ctx);
+  if (l == ctx->ng && ctx->cfg.mg32_fine_npost > 0) return ctx->cfg.mg32_fine_npost;
+  if (l == ctx->ng - 1 && ctx->cfg.mg32_mid_npost > 0) return ctx->cfg.mg32_mid_npost;
+  return post32(ctx);
 }
 
 // Prolongation of the FP32 V-cycles and FMG start: trilinear unless the
@@ -306,11 +311,10 @@ void tail_args(dsg_ctx *ctx, int top, dsg::TailArgs *A) {
   memset(A, 0, sizeof *A);
   for (int l = 1; l <= top; l++) {
     float **L = ctx->lv32[l];
-    A->lv[l] = dsg::TailLevel{L[U32], L[RHS32], L[A32], L[B32], L[C32], L[EI32], ctx->level(l), level_h2(ctx, l)};
+    A->lv[l] = dsg::TailLevel{L[U32],       L[RHS32],          L[A32],     L[B32],         L[C32],
+                              L[EI32],      ctx->level(l),     level_h2(ctx, l), pre32(ctx, l), post32(ctx, l)};
   }
   A->top = top;
-  A->npre = pre32(ctx);
-  A->npost = post32(ctx);
   A->ntop = ctx->s.ntop;
   A->omega = omega32(ctx);
   A->tri = tri32(ctx);

@@ -180,10 +180,11 @@ struct TailLevel {
   const float *a, *b, *c, *ei;
   Dims d;
   float h2;
+  int npre, npost;  // sweeps on this level
 };
 struct TailArgs {
   TailLevel lv[kTailMaxLevels + 1];  // 1..top
-  int top, npre, npost, ntop;
+  int top, ntop;
   float omega;
   int tri;  // trilinear prolongation (else injection)
 };

@@ -442,26 +442,26 @@ __device__ void tail_body(const TailArgs &A) {
     if ((d.nx - 2) * (d.ny - 2) * (d.nz - 2) <= kTailWarpCells) lw = l;
   }
   for (int l = A.top; l > lw && l >= 2; l--) {
-    tail_relax<false>(A.lv[l], A.npre, A.omega);
+    tail_relax<false>(A.lv[l], A.lv[l].npre, A.omega);
     tail_restrict<false>(A.lv[l], A.lv[l - 1]);
   }
   if (lw == 0) {
     tail_relax<false>(A.lv[1], A.ntop, A.omega);
   } else if (threadIdx.x < 32) {
     for (int l = lw; l >= 2; l--) {
-      tail_relax<true>(A.lv[l], A.npre, A.omega);
+      tail_relax<true>(A.lv[l], A.lv[l].npre, A.omega);
       tail_restrict<true>(A.lv[l], A.lv[l - 1]);
     }
     tail_relax<true>(A.lv[1], A.ntop, A.omega);
     for (int l = 2; l <= lw; l++) {
       tail_addint<true>(A.lv[l], A.lv[l - 1], A.tri);
-      tail_relax<true>(A.lv[l], A.npost, A.omega);
+      tail_relax<true>(A.lv[l], A.lv[l].npost, A.omega);
     }
   }
   if (lw > 0) __syncthreads();
   for (int l = (lw > 1 ? lw : 1) + 1; l <= A.top; l++) {
     tail_addint<false>(A.lv[l], A.lv[l - 1], A.tri);
-    tail_relax<false>(A.lv[l], A.npost, A.omega);
+    tail_relax<false>(A.lv[l], A.lv[l].npost, A.omega);
   }
 }
 
