@@ -1309,23 +1309,10 @@ void ora_filterc27(const double *cc, double *cf, int nx, int ny, int nz) {
 
 /* csf, main.f:2363-2481.  Scratch aliasing as in the reference: w11 is the
  * pressure array, w22 the fine residual array, w33 the fine rhs array. */
-void ora_csf(ora_state *st) {
-  const int nx = st->nx, ny = st->ny, nz = st->nz, ng = st->s.ng;
-  const size_t n = (size_t)nx * ny * nz;
-  double *ccc = LV(ng, LCC), *w11 = LV(ng, LU), *w22 = LV(ng, LRES), *w33 = LV(ng, LRHS);
-  double *ccf = zalloc(n);
-  memcpy(ccf, ccc, n * sizeof(double));
-  ora_filterc27(ccf, w22, nx, ny, nz);
-  memcpy(ccf, w22, n * sizeof(double));
-  ora_bc_out(ccf, nx, ny, nz);
-  if (st->s.sigma == 0.0) {
-    memset(st->s11, 0, n * 8); memset(st->s22, 0, n * 8); memset(st->s33, 0, n * 8);
-    memset(st->s12, 0, n * 8); memset(st->s13, 0, n * 8); memset(st->s23, 0, n * 8);
-    free(ccf);
-    return;
-  }
-  const double tau = st->s.tau, h = st->s.h;
-  const double sigh = 0.5 * (tau * tau) * st->s.sigma / (h * h * h);
+/* csf's curvature (main.f:2402-2451): six face-normal magnitudes of the
+ * filtered fraction with transverse 4-point means (+1e-50 inside the root),
+ * kappa = -(d1x-d2x+d1y-d2y+d1z-d2z) at interior cells, then bc_out. */
+void ora_csf_curvature(double *w11, const double *ccf, int nx, int ny, int nz) {
   for (int j = 2; j <= ny - 1; j++)
     for (int i = 2; i <= nx - 1; i++)
       for (int k = 2; k <= nz - 1; k++) {
@@ -1365,6 +1352,26 @@ void ora_csf(ora_state *st) {
         w11[IX(i, j, k)] = -(d1x - d2x + d1y - d2y + d1z - d2z);
       }
   ora_bc_out(w11, nx, ny, nz);
+}
+
+void ora_csf(ora_state *st) {
+  const int nx = st->nx, ny = st->ny, nz = st->nz, ng = st->s.ng;
+  const size_t n = (size_t)nx * ny * nz;
+  double *ccc = LV(ng, LCC), *w11 = LV(ng, LU), *w22 = LV(ng, LRES), *w33 = LV(ng, LRHS);
+  double *ccf = zalloc(n);
+  memcpy(ccf, ccc, n * sizeof(double));
+  ora_filterc27(ccf, w22, nx, ny, nz);
+  memcpy(ccf, w22, n * sizeof(double));
+  ora_bc_out(ccf, nx, ny, nz);
+  if (st->s.sigma == 0.0) {
+    memset(st->s11, 0, n * 8); memset(st->s22, 0, n * 8); memset(st->s33, 0, n * 8);
+    memset(st->s12, 0, n * 8); memset(st->s13, 0, n * 8); memset(st->s23, 0, n * 8);
+    free(ccf);
+    return;
+  }
+  const double tau = st->s.tau, h = st->s.h;
+  const double sigh = 0.5 * (tau * tau) * st->s.sigma / (h * h * h);
+  ora_csf_curvature(w11, ccf, nx, ny, nz);
   for (int k = 2; k <= nz - 1; k++)
     for (int j = 2; j <= ny - 1; j++)
       for (int i = 2; i <= nx - 1; i++) {

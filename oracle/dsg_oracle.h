@@ -126,6 +126,8 @@ void ora_bc_scalar(double *s, int nx, int ny, int nz);
 void ora_bc_resid(double *s, int nx, int ny, int nz);
 void ora_bc_out(double *s, int nx, int ny, int nz);
 void ora_filterc27(const double *cc, double *cf, int nx, int ny, int nz);
+/* csf's curvature of a filtered fraction ccf into w11 (interior, then bc_out). */
+void ora_csf_curvature(double *w11, const double *ccf, int nx, int ny, int nz);
 double ora_al3d(double b1, double b2, double b3, double cc);
 double ora_fl3d(double m1, double m2, double m3, double alpha, double r0, double dr0);
 /* One split sweep (swp, main.f:848-1000) incl. bc_flux and bc_c; `vof1..3`

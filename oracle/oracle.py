@@ -102,6 +102,7 @@ def load():
     for fn in ("ora_bc_scalar", "ora_bc_resid", "ora_bc_out"):
         getattr(lib, fn).argtypes = [_DP, i, i, i]
     lib.ora_filterc27.argtypes = [_DP, _DP, i, i, i]
+    lib.ora_csf_curvature.argtypes = [_DP, _DP, i, i, i]
     lib.ora_al3d.restype = d
     lib.ora_al3d.argtypes = [d, d, d, d]
     lib.ora_fl3d.restype = d
@@ -313,6 +314,15 @@ def filterc27(cc, out0=None):
     CC = Arr(cc)
     out = Arr(out0 if out0 is not None else np.zeros_like(cc))
     lib.ora_filterc27(CC.p, out.p, *cc.shape)
+    return out.array()
+
+
+def csf_curvature(ccf, out0=None):
+    """csf's curvature of a filtered fraction (dsg_oracle.c ora_csf_curvature)."""
+    lib = load()
+    F = Arr(ccf)
+    out = Arr(out0 if out0 is not None else np.zeros_like(ccf))
+    lib.ora_csf_curvature(out.p, F.p, *ccf.shape)
     return out.array()
 
 
