@@ -857,13 +857,14 @@ void dsg_destroy(dsg_ctx *ctx) {
   if (!ctx) return;
   if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
   dsg::snapshot_release(ctx);
-  if (ctx->xfer_stream) {
-    cudaStreamSynchronize(ctx->xfer_stream);
-    cudaStreamDestroy(ctx->xfer_stream);
-  }
-  for (int q = 0; q < dsg_ctx::kStepPhases; q++) {
-    if (ctx->xfer_in[q]) cudaEventDestroy(ctx->xfer_in[q]);
-    if (ctx->xfer_done[q]) cudaEventDestroy(ctx->xfer_done[q]);
+  for (cudaStream_t x : {ctx->xfer_in, ctx->xfer_out})
+    if (x) {
+      cudaStreamSynchronize(x);
+      cudaStreamDestroy(x);
+    }
+  for (int q = 0; q < dsg_ctx::kSyncPoints; q++) {
+    if (ctx->xfer_in_ev[q]) cudaEventDestroy(ctx->xfer_in_ev[q]);
+    if (ctx->xfer_out_ev[q]) cudaEventDestroy(ctx->xfer_out_ev[q]);
   }
   if (ctx->xfer_start) cudaEventDestroy(ctx->xfer_start);
   for (cudaEvent_t e : ctx->prof_ev) cudaEventDestroy(e);
@@ -978,6 +979,29 @@ int dsg::restart_state(dsg_ctx *ctx) {
   return DSG_OK;
 }
 
+namespace {
+
+// Sync points of a time step, in order: before each of the three VOF sweeps,
+// after the VOF phase (VOFmethod, CalcH3d, kepsmodel), after checktime, after
+// the surface-tension phase, after the multigrid solve inside solvelpres, and
+// at the end of the step.  A host-buffer step hooks its copies in there.
+enum { SP_SWEEP1 = 0, SP_SWEEP2, SP_SWEEP3, SP_VOF, SP_CFL, SP_CSF, SP_MG, SP_END };
+static_assert(SP_END + 1 == dsg_ctx::kSyncPoints, "sync points");
+
+inline int sync_point(dsg_ctx *ctx, int point) {
+  return ctx->sync_hook ? ctx->sync_hook(ctx, point, ctx->sync_arg) : DSG_OK;
+}
+
+// Velocity components of the three sweeps for sweep counter tswap (VOFmethod,
+// main.f:795-824: the order rotates with tswap).
+void sweep_order(int tswap, int order[3]) {
+  if (tswap % 3 == 0) { order[0] = 3; order[1] = 1; order[2] = 2; }
+  else if (tswap % 2 == 0) { order[0] = 2; order[1] = 3; order[2] = 1; }
+  else { order[0] = 1; order[1] = 2; order[2] = 3; }
+}
+
+}  // namespace
+
 extern "C" {
 
 int dsg_vofmethod(dsg_ctx *ctx) {
@@ -989,12 +1013,13 @@ int dsg_vofmethod(dsg_ctx *ctx) {
   s.tswap = s.tswap + 1;
   if (s.tswap > 3) s.tswap = 1;
   int order[3];
-  if (s.tswap % 3 == 0) { order[0] = 3; order[1] = 1; order[2] = 2; }
-  else if (s.tswap % 2 == 0) { order[0] = 2; order[1] = 3; order[2] = 1; }
-  else { order[0] = 1; order[1] = 2; order[2] = 3; }
-  for (int q = 0; q < 3; q++)
+  sweep_order(s.tswap, order);
+  for (int q = 0; q < 3; q++) {
+    int rc = sync_point(ctx, SP_SWEEP1 + q);
+    if (rc) return rc;
     DSG_CK(ctx, dsg::swp(vel[order[q]], cc, s1, s2, s3, order[q], d, s.tauh, reinterpret_cast<unsigned *>(ctx->ccf),
                          ctx->iface_count, ctx->stream));
+  }
   DSG_CK(ctx, dsg::bc_c(cc, d, ctx->stream));
   // turbulent diffusion of the volume fraction (main.f:820)
   if (ctx->cfg.iturb != 0)
@@ -1123,6 +1148,7 @@ int dsg_solvelpres(dsg_ctx *ctx, int t, dsg_mg_stats *stats) {
   int rc = mglin(ctx, &ms);
   if (rc && rc != DSG_E_NOT_CONVERGED) return rc;
   const int mg_rc = rc;
+  if ((rc = sync_point(ctx, SP_MG))) return rc;
   DSG_CK(ctx, phase_mark(ctx, 5));
   if (ctx->net)
     DSG_CK(ctx, cudaMemcpyAsync(ctx->f[DSG_F_PPREV2], ctx->f[DSG_F_PPREV], d.count() * sizeof(double),
@@ -1160,80 +1186,110 @@ int dsg_solvelpres(dsg_ctx *ctx, int t, dsg_mg_stats *stats) {
 
 namespace {
 
-// Phases of a time step in the order of the main.f:19-73 loop body: VOF
-// (VOFmethod, CalcH3d, kepsmodel), CFL (checktime), surface tension (csf /
-// sgip / sgip2) and pressure (solvelpres).
-enum { PH_VOF = 0, PH_CFL = 1, PH_CSF = 2, PH_PRES = 3 };
-
-// One time step; hook(phase, after) runs before (after = false) and after
-// (after = true) each phase and may add stream dependencies.  A pressure
+// One time step in the order of the main.f:19-73 loop body: VOF (VOFmethod,
+// CalcH3d, kepsmodel), CFL (checktime), surface tension (csf / sgip / sgip2)
+// and pressure (solvelpres), with the sync points between them.  A pressure
 // solve that stops at its cycle cap still completes the step and its
-// DSG_E_NOT_CONVERGED is returned after the last hook.
-template <class Hook>
-int step_phases(dsg_ctx *ctx, int t, dsg_mg_stats *stats, Hook &&hook) {
-  int rc = hook(PH_VOF, false);
-  if (rc) return rc;
+// DSG_E_NOT_CONVERGED is returned after the last sync point.
+int step_phases(dsg_ctx *ctx, int t, dsg_mg_stats *stats) {
   DSG_CK(ctx, phase_mark(ctx, 0));
-  rc = dsg_vofmethod(ctx);
+  int rc = dsg_vofmethod(ctx);
   if (rc) return rc;
   if (ctx->cfg.hswitch == 1) {
     rc = dsg_calch3d(ctx);
     if (rc) return rc;
   }
   rc = dsg_kepsmodel(ctx);
-  if (rc) return rc;
-  if ((rc = hook(PH_VOF, true)) || (rc = hook(PH_CFL, false))) return rc;
+  if (rc || (rc = sync_point(ctx, SP_VOF))) return rc;
   DSG_CK(ctx, phase_mark(ctx, 1));
   rc = dsg_checktime(ctx);
-  if (rc) return rc;
-  if ((rc = hook(PH_CFL, true)) || (rc = hook(PH_CSF, false))) return rc;
+  if (rc || (rc = sync_point(ctx, SP_CFL))) return rc;
   DSG_CK(ctx, phase_mark(ctx, 2));
   rc = dsg_csf(ctx);
-  if (rc) return rc;
-  if ((rc = hook(PH_CSF, true)) || (rc = hook(PH_PRES, false))) return rc;
+  if (rc || (rc = sync_point(ctx, SP_CSF))) return rc;
   rc = dsg_solvelpres(ctx, t, stats);
   if (rc && rc != DSG_E_NOT_CONVERGED) return rc;
   DSG_CK(ctx, phase_mark(ctx, -1));
-  const int rh = hook(PH_PRES, true);
+  const int rh = sync_point(ctx, SP_END);
   return rh ? rh : rc;
 }
 
-// First phase that reads or writes field f: a field copied in from the host
-// must have arrived before that phase starts.  (The stress components S12,
-// S13, S23 are first read by solvelpres's stress update; with sigma = 0 the
-// surface-tension phase already zeroes all six.)
+// Sync point before which an input of field f must have arrived from the
+// host: before the first work that reads or writes it.  u, v, w are read first
+// by their own VOF sweep (order from the sweep counter the step will use);
+// the stress components S12, S13, S23 by solvelpres's stress update (with
+// sigma = 0 the surface-tension phase already zeroes all six); a, b, c and
+// the previous pressures only in the pressure phase.
 int first_touch(const dsg_ctx *ctx, int f) {
+  int order[3];
+  sweep_order(ctx->s.tswap + 1 > 3 ? 1 : ctx->s.tswap + 1, order);
   switch (f) {
+    case DSG_F_U: case DSG_F_V: case DSG_F_W:
+      for (int q = 0; q < 3; q++)
+        if (order[q] == f - DSG_F_U + 1) return SP_SWEEP1 + q;
+      return SP_SWEEP1;
     case DSG_F_S11: case DSG_F_S22: case DSG_F_S33:
-      return PH_CSF;
+      return SP_CFL;
     case DSG_F_S12: case DSG_F_S13: case DSG_F_S23:
-      return ctx->s.sigma == 0.0 ? PH_CSF : PH_PRES;
+      return ctx->s.sigma == 0.0 ? SP_CFL : SP_CSF;
     case DSG_F_A: case DSG_F_B: case DSG_F_C: case DSG_F_PPREV: case DSG_F_PPREV2:
-      return PH_PRES;
+      return SP_CSF;
     default:
-      return PH_VOF;
+      return SP_SWEEP1;
   }
 }
 
-// Last phase that writes field f: it can be copied out once that phase is done.
+// Sync point after which field f no longer changes in the step: the VOF
+// fields after the VOF phase, the pressure after the multigrid solve (the
+// projection only reads it), everything else at the end.
 int last_write(int f) {
   switch (f) {
     case DSG_F_CC: case DSG_F_RHON: case DSG_F_MUN: case DSG_F_KTUR: case DSG_F_EPS: case DSG_F_MUT:
     case DSG_F_HXMIN: case DSG_F_HXMAX: case DSG_F_HYMIN: case DSG_F_HYMAX: case DSG_F_HZMIN: case DSG_F_HZMAX:
-      return PH_VOF;
+      return SP_VOF;
+    case DSG_F_P:
+      return SP_MG;
     default:
-      return PH_PRES;
+      return SP_END;
   }
 }
 
 int xfer_resources(dsg_ctx *ctx) {
-  if (ctx->xfer_stream) return DSG_OK;
+  if (ctx->xfer_in) return DSG_OK;
   DSG_CK(ctx, cudaEventCreateWithFlags(&ctx->xfer_start, cudaEventDisableTiming));
-  for (int q = 0; q < dsg_ctx::kStepPhases; q++) {
-    DSG_CK(ctx, cudaEventCreateWithFlags(&ctx->xfer_in[q], cudaEventDisableTiming));
-    DSG_CK(ctx, cudaEventCreateWithFlags(&ctx->xfer_done[q], cudaEventDisableTiming));
+  for (int q = 0; q < dsg_ctx::kSyncPoints; q++) {
+    DSG_CK(ctx, cudaEventCreateWithFlags(&ctx->xfer_in_ev[q], cudaEventDisableTiming));
+    DSG_CK(ctx, cudaEventCreateWithFlags(&ctx->xfer_out_ev[q], cudaEventDisableTiming));
   }
-  DSG_CK(ctx, cudaStreamCreateWithFlags(&ctx->xfer_stream, cudaStreamNonBlocking));
+  DSG_CK(ctx, cudaStreamCreateWithFlags(&ctx->xfer_out, cudaStreamNonBlocking));
+  DSG_CK(ctx, cudaStreamCreateWithFlags(&ctx->xfer_in, cudaStreamNonBlocking));
+  return DSG_OK;
+}
+
+// The copies of one host-buffer step.
+struct HostXfer {
+  int n_in, n_out;
+  const int *in_fields, *out_fields;
+  double *const *out_host;
+  bool need[dsg_ctx::kSyncPoints];
+};
+
+// At a sync point: the library's stream waits for the inputs the following
+// work needs, and the outputs final at this point are copied out on the
+// download stream.
+int xfer_hook(dsg_ctx *ctx, int point, void *arg) {
+  const HostXfer &x = *static_cast<const HostXfer *>(arg);
+  if (x.need[point]) DSG_CK(ctx, cudaStreamWaitEvent(ctx->stream, ctx->xfer_in_ev[point], 0));
+  bool any = false;
+  for (int q = 0; q < x.n_out; q++) any = any || last_write(x.out_fields[q]) == point;
+  if (!any) return DSG_OK;
+  const size_t bytes = ctx->fine().count() * sizeof(double);
+  DSG_CK(ctx, cudaEventRecord(ctx->xfer_out_ev[point], ctx->stream));
+  DSG_CK(ctx, cudaStreamWaitEvent(ctx->xfer_out, ctx->xfer_out_ev[point], 0));
+  for (int q = 0; q < x.n_out; q++)
+    if (last_write(x.out_fields[q]) == point)
+      DSG_CK(ctx, cudaMemcpyAsync(x.out_host[q], ctx->f[x.out_fields[q]], bytes, cudaMemcpyDeviceToHost,
+                                  ctx->xfer_out));
   return DSG_OK;
 }
 
@@ -1243,7 +1299,7 @@ extern "C" {
 
 int dsg_step(dsg_ctx *ctx, int t, dsg_mg_stats *stats) {
   if (!ctx) return DSG_E_ARG;
-  return step_phases(ctx, t, stats, [](int, bool) { return DSG_OK; });
+  return step_phases(ctx, t, stats);
 }
 
 int dsg_step_host(dsg_ctx *ctx, int t, dsg_mg_stats *stats, int n_in, const int *in_fields,
@@ -1259,43 +1315,34 @@ int dsg_step_host(dsg_ctx *ctx, int t, dsg_mg_stats *stats, int n_in, const int 
       return dsg::set_error(ctx, DSG_E_ARG, "dsg_step_host: bad output %d (field %d)", q, out_fields[q]);
   int rc = xfer_resources(ctx);
   if (rc) return rc;
-  cudaStream_t cs = ctx->xfer_stream;
   const size_t bytes = ctx->fine().count() * sizeof(double);
-  // the copies start after the work already queued on the library's stream
+  HostXfer x{n_in, n_out, in_fields, out_fields, out_host, {}};
+  // the uploads start after the work already queued on the library's stream,
+  // in the order the step needs them, one event after each sync point's group
   DSG_CK(ctx, cudaEventRecord(ctx->xfer_start, ctx->stream));
-  DSG_CK(ctx, cudaStreamWaitEvent(cs, ctx->xfer_start, 0));
-  // inputs in the order the phases need them, one event after each phase's group
-  bool need[dsg_ctx::kStepPhases] = {};
-  for (int ph = 0; ph < dsg_ctx::kStepPhases; ph++) {
+  DSG_CK(ctx, cudaStreamWaitEvent(ctx->xfer_in, ctx->xfer_start, 0));
+  DSG_CK(ctx, cudaStreamWaitEvent(ctx->xfer_out, ctx->xfer_start, 0));
+  for (int p = 0; p < dsg_ctx::kSyncPoints; p++) {
     for (int q = 0; q < n_in; q++)
-      if (first_touch(ctx, in_fields[q]) == ph) {
-        DSG_CK(ctx, cudaMemcpyAsync(ctx->f[in_fields[q]], in_host[q], bytes, cudaMemcpyHostToDevice, cs));
-        need[ph] = true;
+      if (first_touch(ctx, in_fields[q]) == p) {
+        DSG_CK(ctx, cudaMemcpyAsync(ctx->f[in_fields[q]], in_host[q], bytes, cudaMemcpyHostToDevice, ctx->xfer_in));
+        x.need[p] = true;
       }
-    if (need[ph]) DSG_CK(ctx, cudaEventRecord(ctx->xfer_in[ph], cs));
+    if (x.need[p]) DSG_CK(ctx, cudaEventRecord(ctx->xfer_in_ev[p], ctx->xfer_in));
   }
-  auto hook = [&](int ph, bool after) -> int {
-    if (!after) {
-      if (need[ph]) DSG_CK(ctx, cudaStreamWaitEvent(ctx->stream, ctx->xfer_in[ph], 0));
-      return DSG_OK;
-    }
-    bool any = false;
-    for (int q = 0; q < n_out; q++) any = any || last_write(out_fields[q]) == ph;
-    if (!any) return DSG_OK;
-    DSG_CK(ctx, cudaEventRecord(ctx->xfer_done[ph], ctx->stream));
-    DSG_CK(ctx, cudaStreamWaitEvent(cs, ctx->xfer_done[ph], 0));
-    for (int q = 0; q < n_out; q++)
-      if (last_write(out_fields[q]) == ph)
-        DSG_CK(ctx, cudaMemcpyAsync(out_host[q], ctx->f[out_fields[q]], bytes, cudaMemcpyDeviceToHost, cs));
-    return DSG_OK;
-  };
-  rc = step_phases(ctx, t, stats, hook);
+  ctx->sync_hook = xfer_hook;
+  ctx->sync_arg = &x;
+  rc = step_phases(ctx, t, stats);
+  ctx->sync_hook = nullptr;
+  ctx->sync_arg = nullptr;
   // no copy stays in flight into or out of the caller's buffers, also on errors
-  const cudaError_t e1 = cudaStreamSynchronize(cs);
-  const cudaError_t e2 = cudaStreamSynchronize(ctx->stream);
+  const cudaError_t e1 = cudaStreamSynchronize(ctx->xfer_in);
+  const cudaError_t e2 = cudaStreamSynchronize(ctx->xfer_out);
+  const cudaError_t e3 = cudaStreamSynchronize(ctx->stream);
   if (rc) return rc;
-  if (e1 != cudaSuccess) return dsg::cuda_fail(ctx, e1, "dsg_step_host copies");
-  if (e2 != cudaSuccess) return dsg::cuda_fail(ctx, e2, "dsg_step_host");
+  if (e1 != cudaSuccess) return dsg::cuda_fail(ctx, e1, "dsg_step_host uploads");
+  if (e2 != cudaSuccess) return dsg::cuda_fail(ctx, e2, "dsg_step_host downloads");
+  if (e3 != cudaSuccess) return dsg::cuda_fail(ctx, e3, "dsg_step_host");
   return DSG_OK;
 }
 

@@ -285,13 +285,16 @@ struct dsg_ctx {
   cudaEvent_t snap_ready = nullptr, snap_done = nullptr;
   bool snap_pending = false;
   int snap_t = -1;
-  // host-buffer step (dsg_step_host): copy stream, per-phase upload and
-  // phase-done events (created on first use)
-  static constexpr int kStepPhases = 4;
-  cudaStream_t xfer_stream = nullptr;
-  cudaEvent_t xfer_in[kStepPhases] = {};
-  cudaEvent_t xfer_done[kStepPhases] = {};
+  // host-buffer step (dsg_step_host): upload and download streams, one
+  // event per sync point for each (created on first use), and the hook the
+  // step calls at its sync points while a host-buffer step runs
+  static constexpr int kSyncPoints = 8;
+  cudaStream_t xfer_in = nullptr, xfer_out = nullptr;
+  cudaEvent_t xfer_in_ev[kSyncPoints] = {};
+  cudaEvent_t xfer_out_ev[kSyncPoints] = {};
   cudaEvent_t xfer_start = nullptr;
+  int (*sync_hook)(dsg_ctx *ctx, int point, void *arg) = nullptr;
+  void *sync_arg = nullptr;
   dsg::Dims fine() const { return dsg::Dims{nx, ny, nz}; }
   dsg::Dims level(int l) const { return dsg::Dims{lnx[l], lny[l], lnz[l]}; }
 };
