@@ -86,3 +86,21 @@ def test_inputdata_positional_order():
     assert (inp.nx, inp.ny, inp.nz) == (66, 34, 34)
     assert inp.rho2_si == 500.0 and inp.sigma_si == 0.0728 and inp.surfacet == 5
     assert inp.y0_si == -0.00017365
+
+
+def test_fortran_binding_matches_config():
+    """The ISO_C_BINDING type in the integration notes lists dsg_config's
+    fields in the C order with matching kinds, so a Fortran host that copies
+    it passes its values where the library reads them."""
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    block = re.search(r"type, bind\(C\) :: dsg_config\n(.*?)\n\s*end type", text, re.S).group(1)
+    fortran = []
+    for line in block.splitlines():
+        kind, names = line.split("::")
+        k = re.search(r"\((c_\w+)\)", kind).group(1)
+        fortran += [(n.strip(), k) for n in names.split(",")]
+    dsg = pkg()
+    import ctypes as C
+    kinds = {C.c_int: "c_int", C.c_double: "c_double", C.c_uint64: "c_int64_t"}
+    want = [(n, kinds[t]) for n, t in dsg._lib.DsgConfig._fields_]
+    assert fortran == want
