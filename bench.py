@@ -59,7 +59,7 @@ def parse():
                     help="pre,post sweeps of the FP32 V-cycles on the level below the finest")
     ap.add_argument("--tail-nodes", type=int, default=0,
                     help="largest FP32 level (nodes) of the single-block coarse tail (0: default, -1: off)")
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=6)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 reference point")
