@@ -18,6 +18,8 @@ import argparse
 import importlib
 import json
 import os
+import platform
+import re
 import subprocess
 import sys
 import tempfile
@@ -173,6 +175,25 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(rows)}
 
 
+def host_cpu():
+    """CPU model and logical core count of this host."""
+    model = None
+    try:
+        with open("/proc/cpuinfo") as f:
+            info = f.read()
+        m = re.search(r"^model name\s*:\s*(.+)$", info, re.M)
+        if m:
+            model = m.group(1).strip()
+        else:
+            imp = re.search(r"^CPU implementer\s*:\s*(\S+)$", info, re.M)
+            part = re.search(r"^CPU part\s*:\s*(\S+)$", info, re.M)
+            if imp and part:
+                model = "arm implementer %s part %s" % (imp.group(1), part.group(1))
+    except OSError:
+        pass
+    return {"model": model or platform.machine(), "nproc": os.cpu_count()}
+
+
 def cpu_baseline(dsg, n, tol, steps=1):
     """Single-threaded oracle (plain FP64 MG to tol) on a bounded sample."""
     from oracle import Oracle
@@ -182,7 +203,7 @@ def cpu_baseline(dsg, n, tol, steps=1):
     for t in range(1, steps + 1):
         ora.step(t)
     dt = time.perf_counter() - t0
-    return {"value": steps / dt, "unit": UNIT, "cores": 1, "kind": "port",
+    return {"value": steps / dt, "unit": UNIT, "cores": 1, "kind": "port", "host": host_cpu(),
             "sample": "%d time step(s) of the %d^3 workload from its initial condition, C oracle "
                       "(plain FP64 FMG + V-cycles to %.0e), 1 thread, %.1f s" % (steps, n, tol, dt)}
 
