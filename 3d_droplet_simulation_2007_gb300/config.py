@@ -104,6 +104,9 @@ class InputData:
     # sweeps on the level below the finest (0: mg32_npre/mg32_npost)
     mg32_mid_npre: int = 0
     mg32_mid_npost: int = 0
+    # sweeps on the levels of at most 18^3 nodes (0: mg32_npre/mg32_npost)
+    mg32_small_npre: int = 0
+    mg32_small_npost: int = 0
 
     def as_dict(self):
         return asdict(self)

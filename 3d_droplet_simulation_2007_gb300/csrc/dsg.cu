@@ -198,17 +198,28 @@ inline float omega32(const dsg_ctx *ctx) {
 inline int pre32(const dsg_ctx *ctx) { return ctx->cfg.mg32_npre > 0 ? ctx->cfg.mg32_npre : ctx->s.npre; }
 inline int post32(const dsg_ctx *ctx) { return ctx->cfg.mg32_npost > 0 ? ctx->cfg.mg32_npost : ctx->s.npost; }
 
-// Sweeps on level l: the finest level and the one below it may have their own
-// counts (a sweep there costs 8x and 2-3x one of the smaller levels, which
-// are bound by launch latency).
+// Levels of at most this many nodes may have their own sweep counts
+// (mg32_small_npre/npost): the levels the coarse tail runs by default.
+constexpr long long kSmallLevelNodes = 18LL * 18 * 18;
+
+inline bool small_level(const dsg_ctx *ctx, int l) {
+  return (long long)ctx->lnx[l] * ctx->lny[l] * ctx->lnz[l] <= kSmallLevelNodes;
+}
+
+// Sweeps on level l: the finest level, the one below it and the small levels
+// may have their own counts (a sweep on the finest level costs 8x and on the
+// next 2-3x one of the smaller levels, which are bound by launch latency or,
+// inside the coarse tail, by one SM's issue rate).
 inline int pre32(const dsg_ctx *ctx, int l) {
   if (l == ctx->ng && ctx->cfg.mg32_fine_npre > 0) return ctx->cfg.mg32_fine_npre;
   if (l == ctx->ng - 1 && ctx->cfg.mg32_mid_npre > 0) return ctx->cfg.mg32_mid_npre;
+  if (l < ctx->ng && small_level(ctx, l) && ctx->cfg.mg32_small_npre > 0) return ctx->cfg.mg32_small_npre;
   return pre32(ctx);
 }
 inline int post32(const dsg_ctx *ctx, int l) {
   if (l == ctx->ng && ctx->cfg.mg32_fine_npost > 0) return ctx->cfg.mg32_fine_npost;
   if (l == ctx->ng - 1 && ctx->cfg.mg32_mid_npost > 0) return ctx->cfg.mg32_mid_npost;
+  if (l < ctx->ng && small_level(ctx, l) && ctx->cfg.mg32_small_npost > 0) return ctx->cfg.mg32_small_npost;
   return post32(ctx);
 }
 

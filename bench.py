@@ -57,6 +57,8 @@ def parse():
                     help="V-cycles per level of the FP32 FMG start (default: the library configuration's)")
     ap.add_argument("--fine-sweeps32", type=str, default=None,
                     help="pre,post sweeps of the FP32 V-cycles on the finest level (default: as on the others)")
+    ap.add_argument("--small-sweeps32", type=str, default=None,
+                    help="pre,post sweeps of the FP32 V-cycles on the levels of at most 18^3 nodes")
     ap.add_argument("--mid-sweeps32", type=str, default=None,
                     help="pre,post sweeps of the FP32 V-cycles on the level below the finest")
     ap.add_argument("--tail-nodes", type=int, default=0,
@@ -80,7 +82,7 @@ def dist_env():
 
 
 def workload(dsg, n, mode, tol, inner=0, graphs=True, tail_nodes=0, omega32=None, start=None, sweeps32=None,
-             prolong32=None, fmg32=None, fine_sweeps32=None, mid_sweeps32=None):
+             prolong32=None, fmg32=None, fine_sweeps32=None, mid_sweeps32=None, small_sweeps32=None):
     cfg = dsg.config
     inp = cfg.droplet(n, steps=1000, impact_speed=3.0, noise_si=1e-4, mode=mode, tol=tol,
                       npre=4, npost=4, ntop=4).replace(inner_vcycles=inner, use_graphs=1 if graphs else 0,
@@ -89,6 +91,9 @@ def workload(dsg, n, mode, tol, inner=0, graphs=True, tail_nodes=0, omega32=None
     inp = inp if start is None else inp.replace(warm_start=start)
     inp = inp if prolong32 is None else inp.replace(mg32_prolong=prolong32)
     inp = inp if fmg32 is None else inp.replace(mg32_fmg_cycles=fmg32)
+    if small_sweeps32:
+        a, b = (int(x) for x in small_sweeps32.split(","))
+        inp = inp.replace(mg32_small_npre=a, mg32_small_npost=b)
     if mid_sweeps32:
         a, b = (int(x) for x in mid_sweeps32.split(","))
         inp = inp.replace(mg32_mid_npre=a, mg32_mid_npost=b)
@@ -271,7 +276,7 @@ def run_gb300(args):
     mode = mode_of(dsg, args.mode)
     inp = workload(dsg, args.n, mode, args.tol, args.inner, not args.no_graphs, args.tail_nodes, args.omega32,
                    args.start, args.sweeps32, args.prolong32, args.fmg32, args.fine_sweeps32,
-                   args.mid_sweeps32)
+                   args.mid_sweeps32, args.small_sweeps32)
     solver = dsg.Solver(inp)
     solver.set_stream(torch.cuda.current_stream().cuda_stream)
     for t in range(1, args.warmup + 1):

@@ -104,6 +104,9 @@ typedef struct dsg_config {
   int mg32_mid_npre;   /* pre-/post-sweeps of the FP32 V-cycles on the level below the finest (<= 0:
                           as on the smaller levels) */
   int mg32_mid_npost;
+  int mg32_small_npre; /* pre-/post-sweeps of the FP32 V-cycles on the levels of at most 18^3 nodes below
+                          the finest (<= 0: as on the other levels) */
+  int mg32_small_npost;
 } dsg_config;
 
 /* Non-dimensional scalars and adaptive counters (COMMON /PHYSICS/, /DIFF/,

@@ -59,17 +59,21 @@ def test_mixed_free_run_volume(gpu_lib):
     assert relerr(gpu.field("p"), ora.field("p")) < 1e-5
 
 
-@pytest.mark.parametrize("n,tail,prolong,mid", [(32, 0, 0, 0), (48, 0, 0, 0), (64, 0, 0, 0), (64, 10 ** 6, 0, 0),
-                                               (64, 10 ** 6, 1, 0), (64, 10 ** 6, 0, 4), (32, 10 ** 6, 0, 3)])
-def test_coarse_tail_is_bit_identical(gpu_lib, n, tail, prolong, mid):
+@pytest.mark.parametrize("n,tail,prolong,mid,small", [(32, 0, 0, 0, 0), (48, 0, 0, 0, 0), (64, 0, 0, 0, 0),
+                                                     (64, 10 ** 6, 0, 0, 0), (64, 10 ** 6, 1, 0, 0),
+                                                     (64, 10 ** 6, 0, 4, 0), (32, 10 ** 6, 0, 3, 0),
+                                                     (64, 0, 0, 0, 2), (64, 10 ** 6, 0, 0, 3)])
+def test_coarse_tail_is_bit_identical(gpu_lib, n, tail, prolong, mid, small):
     """The single-block coarse tail computes the same bits as one launch per
     pass, with fewer launches.  tail=10**6 runs every level below the finest
     in the tail kernel.  prolong: 0 trilinear, 1 injection; mid: own sweep
-    counts (mid, mid+2) on the level below the finest."""
+    counts (mid, mid+2) on the level below the finest; small: (small,
+    small+1) on the levels of at most 18^3 nodes."""
     dsg = gpu_lib
     lib = dsg.load()
     base = dsg.config.droplet(n, mode=dsg.config.MODE_TOL_MIXED, tol=1e-9, impact_speed=2.0).replace(
-        mg32_prolong=prolong, mg32_mid_npre=mid, mg32_mid_npost=mid + 2 if mid else 0)
+        mg32_prolong=prolong, mg32_mid_npre=mid, mg32_mid_npost=mid + 2 if mid else 0,
+        mg32_small_npre=small, mg32_small_npost=small + 1 if small else 0)
     runs = {}
     for key, tn in (("pass", -1), ("tail", tail)):
         with dsg.Solver(base.replace(tail_nodes=tn)) as s:
