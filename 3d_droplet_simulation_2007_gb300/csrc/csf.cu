@@ -16,7 +16,7 @@ __global__ void k_curvature(double *__restrict__ kap, const double *__restrict__
   if (i > d.nx - 1 || j > d.ny - 1) return;
   const size_t q = d.ix(i, j, k);
   const long sy = (long)d.sy(), sz = (long)d.sz();
-#define F(di, dj, dk) f[q + (long)(di) + (long)(dj) * sy + (long)(dk) * sz]
+#define F(di, dj, dk) f[(long)q + (long)(di) + (long)(dj) * sy + (long)(dk) * sz]
   // Uniform 19-point neighbourhood (bulk liquid or gas): every difference is
   // +0, every d is 0/sqrt(1e-50) = +0 and kappa = -(+0) = -0 exactly.
   const double f0 = F(0, 0, 0);

@@ -68,7 +68,7 @@ void fort_e15_7(char *out, double x) {
     snprintf(mant, sizeof mant, "%s0.%sE%c%02d", neg ? "-" : "", digits, ex < 0 ? '-' : '+', ax);
   else
     snprintf(mant, sizeof mant, "%s0.%s%c%03d", neg ? "-" : "", digits, ex < 0 ? '-' : '+', ax);
-  snprintf(out, 16, "%15s", mant);
+  snprintf(out, 16, "%15.15s", mant);  // E15.7 fields hold at most 14 characters
 }
 
 void put_row(FILE *f, const double *v, int n) {

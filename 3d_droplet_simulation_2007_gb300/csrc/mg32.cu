@@ -64,10 +64,8 @@ struct Split {
   __host__ __device__ __forceinline__ size_t at(int m, int j, int k) const {
     return (size_t)m + (size_t)hx * ((size_t)(j - 2) + (size_t)ny2 * (size_t)(k - 2));
   }
-  __host__ __device__ __forceinline__ size_t count() const { return (size_t)hx * ny2 * nz2; }
 };
 
-__device__ __forceinline__ Split split_of(Dims d) { return Split{(d.nx - 2) >> 1, d.ny - 2, d.nz - 2}; }
 
 __device__ __forceinline__ unsigned at32(Split sp, int m, int j, int k) {
   return (unsigned)m + (unsigned)sp.hx * ((unsigned)(j - 2) + (unsigned)sp.ny2 * (unsigned)(k - 2));

@@ -284,7 +284,7 @@ __global__ void k_filterc27(const double *__restrict__ cc, double *__restrict__ 
   const double w0 = (double)0.2729f, w1 = (double)0.08185f, w2 = (double)0.0178f, w3 = (double)0.0028f;
   const size_t q = d.ix(i, j, k);
   const long sy = (long)d.sy(), sz = (long)d.sz();
-#define C(di, dj, dk) cc[q + (long)(di) + (long)(dj) * sy + (long)(dk) * sz]
+#define C(di, dj, dk) cc[(long)q + (long)(di) + (long)(dj) * sy + (long)(dk) * sz]
   // Uniform 27-point neighbourhood of 0 or 1: the partial sums are exact
   // multiples of the value, so the weighted sum equals the precomputed one.
   const double c0 = C(0, 0, 0);

@@ -65,9 +65,9 @@ __global__ void k_convective(double *__restrict__ u, double *__restrict__ v, dou
   if (i > d.nx - 1 || j > d.ny - 1) return;
   const size_t q = d.ix(i, j, k);
   const long sy = (long)d.sy(), sz = (long)d.sz();
-#define W1(di, dj, dk) w1[q + (long)(di) + (long)(dj) * sy + (long)(dk) * sz]
-#define W2(di, dj, dk) w2[q + (long)(di) + (long)(dj) * sy + (long)(dk) * sz]
-#define W3(di, dj, dk) w3[q + (long)(di) + (long)(dj) * sy + (long)(dk) * sz]
+#define W1(di, dj, dk) w1[(long)q + (long)(di) + (long)(dj) * sy + (long)(dk) * sz]
+#define W2(di, dj, dk) w2[(long)q + (long)(di) + (long)(dj) * sy + (long)(dk) * sz]
+#define W3(di, dj, dk) w3[(long)q + (long)(di) + (long)(dj) * sy + (long)(dk) * sz]
   double p, m, x;
   p = W1(0, 0, 0) + W1(-1, 0, 0);
   m = W1(1, 0, 0) + W1(0, 0, 0);

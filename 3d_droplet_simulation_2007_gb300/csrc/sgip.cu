@@ -18,7 +18,7 @@ __device__ __forceinline__ double cube(double x) { return x * x * x; }
 // pentagon and hexagon), assigned to the axes and clipped to [0, 1].
 // Returns 0, 1 ("NO MATCH CASES FOUND") or 2 ("PROBLEM finding MIN and MAX").
 __device__ int h3d_cell(const double *__restrict__ c, size_t q, long sy, long sz, double h[6]) {
-#define C(di, dj, dk) c[q + (long)(di) + (long)(dj) * sy + (long)(dk) * sz]
+#define C(di, dj, dk) c[(long)q + (long)(di) + (long)(dj) * sy + (long)(dk) * sz]
   double mm1, mm2;
   mm1 = C(-1, -1, -1) + C(-1, -1, 1) + C(-1, 1, -1) + C(-1, 1, 1) +
         2.0 * (C(-1, -1, 0) + C(-1, 1, 0) + C(-1, 0, -1) + C(-1, 0, 1)) + 4.0 * C(-1, 0, 0);
@@ -229,7 +229,7 @@ __global__ void k_sgip_curvature(double *__restrict__ kap, const double *__restr
   if (i > d.nx - 1 || j > d.ny - 1) return;
   const size_t q = d.ix(i, j, k);
   const long sy = (long)d.sy(), sz = (long)d.sz();
-#define F(di, dj, dk) f[q + (long)(di) + (long)(dj) * sy + (long)(dk) * sz]
+#define F(di, dj, dk) f[(long)q + (long)(di) + (long)(dj) * sy + (long)(dk) * sz]
   // uniform 19-point neighbourhood: every difference +0, kappa = -0 exactly
   const double f0 = F(0, 0, 0);
 #define EQ(di, dj, dk) same_bits(F(di, dj, dk), f0)

@@ -111,7 +111,7 @@ __device__ void iface_flux(size_t q, const double *__restrict__ us, const double
   const double a2 = us[q + sd] * tauh;
   const double c0 = cc[q];
   double f1 = 0.0, f2 = 0.0, f3 = 0.0;
-#define C(di, dj, dk) cc[q + (long)(di) + (long)(dj) * sy + (long)(dk) * sz]
+#define C(di, dj, dk) cc[(long)q + (long)(di) + (long)(dj) * sy + (long)(dk) * sz]
   double mm1, mm2, mx, my, mz;
   mm1 = C(-1, -1, -1) + C(-1, -1, 1) + C(-1, 1, -1) + C(-1, 1, 1) +
         2.0 * (C(-1, -1, 0) + C(-1, 1, 0) + C(-1, 0, -1) + C(-1, 0, 1)) + 4.0 * C(-1, 0, 0);
