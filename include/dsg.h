@@ -184,9 +184,10 @@ int dsg_step(dsg_ctx *ctx, int t, dsg_mg_stats *stats);
    copies run on a second stream: each input is waited for only by the first
    phase of the step that touches its field and each output is copied as soon
    as the last phase that writes it is done, so most of the transfer overlaps
-   the step's kernels.  Returns once the outputs are on the host, also on
-   errors.  Page-locked host arrays (cudaHostRegister or cudaMallocHost) make
-   the copies asynchronous. */
+   the step's kernels.  Returns once the outputs are on the host.  On an error
+   it returns once no copy is in flight any more; outputs whose phase was not
+   reached are left unwritten.  Page-locked host arrays (cudaHostRegister or
+   cudaMallocHost) make the copies asynchronous. */
 int dsg_step_host(dsg_ctx *ctx, int t, dsg_mg_stats *stats, int n_in, const int *in_fields,
                   const double *const *in_host, int n_out, const int *out_fields, double *const *out_host);
 /* SUMFIELD(cc) main.f:4783-4801: liquid volume (FP64, deterministic order) */
