@@ -49,7 +49,7 @@ class DsgConfig(C.Structure):
         ("warm_start", C.c_int), ("mg32_omega", C.c_double), ("mg32_npre", C.c_int), ("mg32_npost", C.c_int),
         ("mg32_prolong", C.c_int), ("mg32_fmg_cycles", C.c_int), ("mg32_fine_npre", C.c_int),
         ("mg32_fine_npost", C.c_int), ("mg32_mid_npre", C.c_int), ("mg32_mid_npost", C.c_int),
-        ("mg32_small_npre", C.c_int), ("mg32_small_npost", C.c_int),
+        ("mg32_small_npre", C.c_int), ("mg32_small_npost", C.c_int), ("fp64_exact", C.c_int),
     ]
 
 

@@ -107,6 +107,9 @@ class InputData:
     # sweeps on the levels of at most 18^3 nodes (0: mg32_npre/mg32_npost)
     mg32_small_npre: int = 0
     mg32_small_npost: int = 0
+    # tolerance mode: 0 = FP64 multigrid in fused multiply-add form (within
+    # ulps of the oracle), 1 = the reference's exact operation order
+    fp64_exact: int = 0
 
     def as_dict(self):
         return asdict(self)

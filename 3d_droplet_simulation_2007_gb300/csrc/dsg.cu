@@ -118,6 +118,14 @@ cudaError_t phase_mark(dsg_ctx *ctx, int id) {
   return cudaEventRecord(ctx->phase_ev[ctx->phase_used++], ctx->stream);
 }
 
+// The FP64 multigrid of the tolerance mode runs its sweeps, residuals and
+// norm in fused multiply-add form unless the configuration asks for the
+// reference's exact operation order; the reference's fixed-cycle mode always
+// keeps that order.
+inline bool fp64_fma(const dsg_ctx *ctx) {
+  return ctx->cfg.mode == DSG_MODE_TOL_FP64 && ctx->cfg.fp64_exact == 0;
+}
+
 // relax_n on level jj; the finest level is timed with an event pair when the
 // live profile is on.
 cudaError_t relax_level(dsg_ctx *ctx, int n, int jj, double ls) {
@@ -136,7 +144,8 @@ cudaError_t relax_level(dsg_ctx *ctx, int n, int jj, double ls) {
     cudaError_t r = cudaEventRecord(ctx->prof_ev[ctx->prof_used], ctx->stream);
     if (r != cudaSuccess) return r;
   }
-  cudaError_t e = dsg::relax_n(n, L[1], ls, L[3], L[4], L[5], L[6], L[7], d, ctx->cfg.omega, ctx->stream);
+  cudaError_t e =
+      dsg::relax_n(n, L[1], ls, L[3], L[4], L[5], L[6], L[7], d, ctx->cfg.omega, ctx->stream, fp64_fma(ctx));
   if (timed) {
     cudaError_t r = cudaEventRecord(ctx->prof_ev[ctx->prof_used + 1], ctx->stream);
     if (r != cudaSuccess) return r;
@@ -156,7 +165,7 @@ int vcycle(dsg_ctx *ctx, int j) {
     double **L = ctx->lv[jj];
     const Dims d = ctx->level(jj);
     DSG_CK(ctx, relax_level(ctx, ctx->s.npre, jj, ls));
-    DSG_CK(ctx, dsg::resid(ls, L[2], L[1], L[3], L[4], L[5], L[6], d, st));
+    DSG_CK(ctx, dsg::resid(ls, L[2], L[1], L[3], L[4], L[5], L[6], d, st, fp64_fma(ctx)));
     const Dims dc = ctx->level(jj - 1);
     DSG_CK(ctx, dsg::rstrct(ctx->lv[jj - 1][3], L[2], dc, st));
     DSG_CK(ctx, dsg::fill_zero(ctx->lv[jj - 1][1], dc.count(), st));
@@ -174,7 +183,7 @@ int vcycle(dsg_ctx *ctx, int j) {
 int relres_host(dsg_ctx *ctx, double *out) {
   double **L = ctx->lv[ctx->ng];
   DSG_CK(ctx, dsg::relres_sums(ctx->red_out, ctx->red_partials, ctx->s.lengthsize, L[1], L[3], L[4], L[5],
-                               L[6], ctx->fine(), ctx->stream));
+                               L[6], ctx->fine(), ctx->stream, fp64_fma(ctx)));
   int rc = read_device(ctx, 2);
   if (rc) return rc;
   const double rr = ctx->red_host[0], bb = ctx->red_host[1];
@@ -695,7 +704,7 @@ int mglin(dsg_ctx *ctx, dsg_mg_stats *stats) {
   DSG_CK(ctx, dsg::fill_zero(L1[1], ctx->level(1).count(), st));
   // First coarse solve with lengthscale in place of lengthsize (main.f:3686-3689).
   DSG_CK(ctx, dsg::relax_n(ctx->s.ntop, L1[1], ctx->s.lengthscale, L1[3], L1[4], L1[5], L1[6], L1[7],
-                           ctx->level(1), om, st));
+                           ctx->level(1), om, st, fp64_fma(ctx)));
   for (int j = 2; j <= ng; j++) {
     DSG_CK(ctx, dsg::interp(ctx->lv[j][1], ctx->lv[j - 1][1], ctx->level(j), st));
     for (int c = 0; c < ctx->cfg.cycles; c++) {
@@ -1228,9 +1237,10 @@ int step_phases(dsg_ctx *ctx, int t, dsg_mg_stats *stats) {
 // Sync point before which an input of field f must have arrived from the
 // host: before the first work that reads or writes it.  u, v, w are read first
 // by their own VOF sweep (order from the sweep counter the step will use);
-// the stress components S12, S13, S23 by solvelpres's stress update (with
-// sigma = 0 the surface-tension phase already zeroes all six); a, b, c and
-// the previous pressures only in the pressure phase.
+// all six stress components are written by the surface-tension phase (csf's
+// bc_tensor zeroes ghost faces of S12, S13, S23; with sigma = 0 all six are
+// zeroed), so they arrive before it; a, b, c and the previous pressures are
+// first touched in the pressure phase.
 int first_touch(const dsg_ctx *ctx, int f) {
   int order[3];
   sweep_order(ctx->s.tswap + 1 > 3 ? 1 : ctx->s.tswap + 1, order);
@@ -1240,9 +1250,8 @@ int first_touch(const dsg_ctx *ctx, int f) {
         if (order[q] == f - DSG_F_U + 1) return SP_SWEEP1 + q;
       return SP_SWEEP1;
     case DSG_F_S11: case DSG_F_S22: case DSG_F_S33:
-      return SP_CFL;
     case DSG_F_S12: case DSG_F_S13: case DSG_F_S23:
-      return ctx->s.sigma == 0.0 ? SP_CFL : SP_CSF;
+      return SP_CFL;
     case DSG_F_A: case DSG_F_B: case DSG_F_C: case DSG_F_PPREV: case DSG_F_PPREV2:
       return SP_CSF;
     default:

@@ -93,11 +93,14 @@ cudaError_t bc_resid(double *s, Dims d, cudaStream_t st);
 cudaError_t bc_out(double *s, Dims d, cudaStream_t st);
 cudaError_t relax(double *u, double lengthsize, const double *rhs, const double *a, const double *b,
                   const double *c, const double *ei, Dims d, double omega, cudaStream_t st);
+// fma = true: the fused multiply-add form of the FP64 sweep and residual
+// (fewer FP64 operations, results within ulps of the reference order);
+// fma = false: the reference's operation order, bit-identical to the oracle.
 cudaError_t relax_n(int n, double *u, double lengthsize, const double *rhs, const double *a,
                     const double *b, const double *c, const double *ei, Dims d, double omega,
-                    cudaStream_t st);
+                    cudaStream_t st, bool fma = false);
 cudaError_t resid(double lengthsize, double *res, const double *u, const double *rhs, const double *a,
-                  const double *b, const double *c, Dims d, cudaStream_t st);
+                  const double *b, const double *c, Dims d, cudaStream_t st, bool fma = false);
 cudaError_t rstrct(double *uc, const double *uf, Dims dc, cudaStream_t st);
 cudaError_t interp(double *uf, const double *uc, Dims df, cudaStream_t st);
 cudaError_t addint(double *uf, const double *uc, double *res, Dims df, cudaStream_t st);
@@ -109,7 +112,7 @@ cudaError_t filterc27(const double *cc, double *cf, Dims d, cudaStream_t st);
 // relres partial sums: out[0] = sum r^2, out[1] = sum rhs^2 (device, 2 doubles)
 cudaError_t relres_sums(double *out, double *partials, double lengthsize, const double *u,
                         const double *rhs, const double *a, const double *b, const double *c, Dims d,
-                        cudaStream_t st);
+                        cudaStream_t st, bool fma = false);
 // out[0] = interior sum of f (SUMFIELD order-independent tree sum)
 cudaError_t sumfield(double *out, double *partials, const double *f, Dims d, cudaStream_t st);
 // out[0] = max |f| over the interior

@@ -86,6 +86,12 @@ __global__ void k_bc_out_z(double *__restrict__ s, Dims d) {
 // ---- relax: one colour pass (main.f:3973-3992) ----------------------------
 // colour 0 updates i+j+k even (first pass), colour 1 odd.  Thread (t, j, k)
 // updates i = i0 + 2t.  Ghost neighbours are virtual (see file header).
+// FMA = false: the reference's operation order, no contraction (17 FP64
+// operations per cell, bit-identical to the oracle).  FMA = true: the same
+// sum as a fused multiply-add chain and the update written as
+// u + omega*(temp - u) (10 FP64 operations); GB300's FP64 pipe, not HBM,
+// bounds this kernel, so the operation count sets its speed.
+template <bool FMA>
 __global__ void k_relax_colour(double *__restrict__ u, const double *__restrict__ rhs,
                                const double *__restrict__ a, const double *__restrict__ b,
                                const double *__restrict__ c, const double *__restrict__ ei, Dims d,
@@ -104,13 +110,47 @@ __global__ void k_relax_colour(double *__restrict__ u, const double *__restrict_
   const double uym = (j - 1 == 1) ? uc : u[q - sy];
   const double uzp = (k + 1 == d.nz) ? uc : u[q + sz];
   const double uzm = (k - 1 == 1) ? uc : u[q - sz];
+  if (FMA) {
+    double t = a[q] * uxp;
+    t = __fma_rn(a[q - 1], uxm, t);
+    t = __fma_rn(b[q], uyp, t);
+    t = __fma_rn(b[q - sy], uym, t);
+    t = __fma_rn(c[q], uzp, t);
+    t = __fma_rn(c[q - sz], uzm, t);
+    t = __fma_rn(-h2, rhs[q], t) * ei[q];
+    u[q] = __fma_rn(omega, t - uc, uc);
+    return;
+  }
   const double temp = (a[q] * uxp + a[q - 1] * uxm + b[q] * uyp + b[q - sy] * uym + c[q] * uzp +
                        c[q - sz] * uzm - h2 * rhs[q]) *
                       ei[q];
   u[q] = omega * temp + (1.0 - omega) * uc;
 }
 
+// Residual of one interior cell, rhs - (1/h^2) sum a_nb (u_nb - u) (main.f:3912-3925),
+// in the reference's order or as a fused multiply-add chain.
+template <bool FMA>
+__device__ __forceinline__ double cell_resid(const double *__restrict__ u, const double *__restrict__ rhs,
+                                             const double *__restrict__ a, const double *__restrict__ b,
+                                             const double *__restrict__ c, size_t q, size_t sy, size_t sz,
+                                             double h2i) {
+  const double uc = u[q];
+  if (FMA) {
+    double t = a[q] * (u[q + 1] - uc);
+    t = __fma_rn(a[q - 1], u[q - 1] - uc, t);
+    t = __fma_rn(b[q], u[q + sy] - uc, t);
+    t = __fma_rn(b[q - sy], u[q - sy] - uc, t);
+    t = __fma_rn(c[q], u[q + sz] - uc, t);
+    t = __fma_rn(c[q - sz], u[q - sz] - uc, t);
+    return __fma_rn(-h2i, t, rhs[q]);
+  }
+  return -h2i * (a[q] * (u[q + 1] - uc) + a[q - 1] * (u[q - 1] - uc) + b[q] * (u[q + sy] - uc) +
+                 b[q - sy] * (u[q - sy] - uc) + c[q] * (u[q + sz] - uc) + c[q - sz] * (u[q - sz] - uc)) +
+         rhs[q];
+}
+
 // ---- resid (main.f:3912-3925), reads the ghosts from memory ----------------
+template <bool FMA>
 __global__ void k_resid(double *__restrict__ res, const double *__restrict__ u,
                         const double *__restrict__ rhs, const double *__restrict__ a,
                         const double *__restrict__ b, const double *__restrict__ c, Dims d,
@@ -120,11 +160,7 @@ __global__ void k_resid(double *__restrict__ res, const double *__restrict__ u,
   const int k = blockIdx.z + 2;
   if (i > d.nx - 1 || j > d.ny - 1) return;
   const size_t q = d.ix(i, j, k);
-  const size_t sy = d.sy(), sz = d.sz();
-  const double uc = u[q];
-  res[q] = -h2i * (a[q] * (u[q + 1] - uc) + a[q - 1] * (u[q - 1] - uc) + b[q] * (u[q + sy] - uc) +
-                   b[q - sy] * (u[q - sy] - uc) + c[q] * (u[q + sz] - uc) + c[q - sz] * (u[q - sz] - uc)) +
-           rhs[q];
+  res[q] = cell_resid<FMA>(u, rhs, a, b, c, q, d.sy(), d.sz(), h2i);
 }
 
 // ---- rstrct fused with the coarse bc_scalar (main.f:3765-3791) ------------
@@ -409,6 +445,7 @@ __device__ __forceinline__ long long abs_bits(double x) {
   return __double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFLL;
 }
 
+template <bool FMA>
 __global__ void k_relres_partial(double *__restrict__ partials, const double *__restrict__ u,
                                  const double *__restrict__ rhs, const double *__restrict__ a,
                                  const double *__restrict__ b, const double *__restrict__ c, Dims d,
@@ -419,13 +456,14 @@ __global__ void k_relres_partial(double *__restrict__ partials, const double *__
   for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
     int i, j, k;
     const size_t q = interior_cell(t, d, i, j, k);
-    const double uc = u[q];
-    const double r = -h2i * (a[q] * (u[q + 1] - uc) + a[q - 1] * (u[q - 1] - uc) + b[q] * (u[q + sy] - uc) +
-                             b[q - sy] * (u[q - sy] - uc) + c[q] * (u[q + sz] - uc) +
-                             c[q - sz] * (u[q - sz] - uc)) +
-                     rhs[q];
-    v[0] += r * r;
-    v[1] += rhs[q] * rhs[q];
+    const double r = cell_resid<FMA>(u, rhs, a, b, c, q, sy, sz, h2i);
+    if (FMA) {
+      v[0] = __fma_rn(r, r, v[0]);
+      v[1] = __fma_rn(rhs[q], rhs[q], v[1]);
+    } else {
+      v[0] += r * r;
+      v[1] += rhs[q] * rhs[q];
+    }
   }
   block_sum_store<2>(v, partials);
 }
@@ -509,12 +547,16 @@ cudaError_t bc_out(double *s, Dims d, cudaStream_t st) {
 }
 
 static void relax_passes(double *u, double h2, const double *rhs, const double *a, const double *b,
-                         const double *c, const double *ei, Dims d, double omega, cudaStream_t st) {
+                         const double *c, const double *ei, Dims d, double omega, bool fma, cudaStream_t st) {
   const int half = (d.nx - 2 + 1) / 2;
   const dim3 grid((unsigned)((half + kBlk.x - 1) / kBlk.x), (unsigned)((d.ny - 2 + kBlk.y - 1) / kBlk.y),
                   (unsigned)(d.nz - 2));
-  DSG_COUNT k_relax_colour<<<grid, kBlk, 0, st>>>(u, rhs, a, b, c, ei, d, h2, omega, 0);
-  DSG_COUNT k_relax_colour<<<grid, kBlk, 0, st>>>(u, rhs, a, b, c, ei, d, h2, omega, 1);
+  for (int colour = 0; colour < 2; colour++) {
+    if (fma)
+      DSG_COUNT k_relax_colour<true><<<grid, kBlk, 0, st>>>(u, rhs, a, b, c, ei, d, h2, omega, colour);
+    else
+      DSG_COUNT k_relax_colour<false><<<grid, kBlk, 0, st>>>(u, rhs, a, b, c, ei, d, h2, omega, colour);
+  }
 }
 
 cudaError_t relax(double *u, double lengthsize, const double *rhs, const double *a, const double *b,
@@ -524,19 +566,22 @@ cudaError_t relax(double *u, double lengthsize, const double *rhs, const double 
 
 cudaError_t relax_n(int n, double *u, double lengthsize, const double *rhs, const double *a,
                     const double *b, const double *c, const double *ei, Dims d, double omega,
-                    cudaStream_t st) {
+                    cudaStream_t st, bool fma) {
   if (n <= 0) return cudaSuccess;
   const double h1 = lengthsize / (d.nx - 2);
   const double h2 = h1 * h1;
-  for (int q = 0; q < n; q++) relax_passes(u, h2, rhs, a, b, c, ei, d, omega, st);
+  for (int q = 0; q < n; q++) relax_passes(u, h2, rhs, a, b, c, ei, d, omega, fma, st);
   return bc_scalar(u, d, st);
 }
 
 cudaError_t resid(double lengthsize, double *res, const double *u, const double *rhs, const double *a,
-                  const double *b, const double *c, Dims d, cudaStream_t st) {
+                  const double *b, const double *c, Dims d, cudaStream_t st, bool fma) {
   const double h1 = lengthsize / (d.nx - 2);
   const double h2i = 1.0 / (h1 * h1);
-  DSG_COUNT k_resid<<<interior_grid(d, kBlk), kBlk, 0, st>>>(res, u, rhs, a, b, c, d, h2i);
+  if (fma)
+    DSG_COUNT k_resid<true><<<interior_grid(d, kBlk), kBlk, 0, st>>>(res, u, rhs, a, b, c, d, h2i);
+  else
+    DSG_COUNT k_resid<false><<<interior_grid(d, kBlk), kBlk, 0, st>>>(res, u, rhs, a, b, c, d, h2i);
   return bc_resid(res, d, st);
 }
 
@@ -585,10 +630,13 @@ cudaError_t filterc27(const double *cc, double *cf, Dims d, cudaStream_t st) {
 
 cudaError_t relres_sums(double *out, double *partials, double lengthsize, const double *u,
                         const double *rhs, const double *a, const double *b, const double *c, Dims d,
-                        cudaStream_t st) {
+                        cudaStream_t st, bool fma) {
   const double h1 = lengthsize / (d.nx - 2);
   const double h2i = 1.0 / (h1 * h1);
-  DSG_COUNT k_relres_partial<<<kRedBlocks, kRedThreads, 0, st>>>(partials, u, rhs, a, b, c, d, h2i);
+  if (fma)
+    DSG_COUNT k_relres_partial<true><<<kRedBlocks, kRedThreads, 0, st>>>(partials, u, rhs, a, b, c, d, h2i);
+  else
+    DSG_COUNT k_relres_partial<false><<<kRedBlocks, kRedThreads, 0, st>>>(partials, u, rhs, a, b, c, d, h2i);
   DSG_COUNT k_fold<2, false><<<1, kRedThreads, 0, st>>>(partials, out);
   return cudaGetLastError();
 }

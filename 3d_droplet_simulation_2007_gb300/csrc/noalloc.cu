@@ -23,6 +23,8 @@
 //  * the first call on each device looks up the array's device address with
 //    cudaGetSymbolAddress (with that device current) and caches it; make that
 //    first call before any stream capture is started.
+#include <atomic>
+
 #include "dsg_internal.cuh"
 
 namespace {
@@ -36,7 +38,10 @@ constexpr size_t kNoAllocDoubles = (size_t)66 * 66 * 66 + 7 * ((size_t)34 * 34 *
 static __device__ __align__(256) double g_noalloc_scratch[kNoAllocDoubles];
 
 constexpr int kMaxDevices = 64;
-double *g_scratch_addr[kMaxDevices] = {nullptr};
+// Per-device cache of the array's address.  Host threads that make their first
+// call on a device at the same time may both look it up; they store the same
+// value, and the atomics make that well defined.
+std::atomic<double *> g_scratch_addr[kMaxDevices];
 
 // Device address of the scratch array on the current device (looked up once
 // per device; host code cannot use the symbol itself as a device pointer).
@@ -45,14 +50,16 @@ int scratch_address(double **out) {
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return dsg::set_error(nullptr, DSG_E_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
   if (dev < 0 || dev >= kMaxDevices) return dsg::set_error(nullptr, DSG_E_ARG, "device %d out of range", dev);
-  if (!g_scratch_addr[dev]) {
+  double *addr = g_scratch_addr[dev].load(std::memory_order_acquire);
+  if (!addr) {
     void *p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p)
       return dsg::set_error(nullptr, DSG_E_CUDA, "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
-    g_scratch_addr[dev] = (double *)p;
+    addr = (double *)p;
+    g_scratch_addr[dev].store(addr, std::memory_order_release);
   }
-  *out = g_scratch_addr[dev];
+  *out = addr;
   return DSG_OK;
 }
 
@@ -107,6 +114,10 @@ extern "C" int dsg_mglin_noalloc(double *p, const double *rhs, const double *a, 
   }
   if (nn < 4 || (1 << ng) + 2 != nn)
     return dsg::set_error(nullptr, DSG_E_ARG, "dsg_mglin_noalloc: min(nx,ny,nz)=%d is not 2**ng+2", nn);
+  // every side must halve evenly down to the coarsest level, as in dsg_create
+  if (dsg::level_count(nx, ny, nz) != ng)
+    return dsg::set_error(nullptr, DSG_E_ARG,
+                          "dsg_mglin_noalloc: grid %dx%dx%d does not coarsen evenly over %d levels", nx, ny, nz, ng);
   double *scratch = nullptr;
   int rc = scratch_address(&scratch);
   if (rc) return rc;

@@ -2,17 +2,24 @@
 """Benchmark: time-steps/s of the droplet projection hot path at 256^3.
 
 Workload: the splash-on-wall case, 256^3 interior cells (258^3 nodes), 3 m/s
-impact, 4 pre/4 post red-black sweeps, laminar (k-epsilon is not part of this
-build), pressure solved to 1e-8 relative residual.  A "step" is one body of the
-main.f time loop (VOF advection, CFL check, CSF force, momentum + pressure
-projection) with every field resident in HBM.
+impact, pressure solved to 1e-8 relative residual, laminar: the reference's
+explicit k-epsilon update (main.f:1888-2026) overflows on this drop by its third
+step, so the k-epsilon variant of the case has no finite state to time.  A
+"step" is one body of the main.f time loop (VOF advection, CFL check, CSF force,
+momentum + pressure projection) with every field resident in HBM.  The
+headline solve is FP64 defect correction around FP32 V-cycles (FP32 full
+multigrid start, V(3,3) on the finest level and V(8,8) below, omega 1.5,
+trilinear prolongation); the plain FP64 multigrid (the reference's FMG with
+V(4,4), then FP64 V-cycles to the same tolerance) is timed beside it.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
 Prints one JSON line.  With N>1 (torchrun) every rank advances its own
 independent droplet replica (weak scaling, no collective on the data path).
 ``--impl reference`` times the CPU reference restatement (the oracle: plain
-FP64 multigrid to the same tolerance, single thread) on the same workload.
+FP64 multigrid to the same tolerance, single thread, as the reference is
+serial) on the same workload and step window: W untimed warm-up steps from the
+initial condition, then steps W+1 ... W+k.
 """
 import argparse
 import importlib
@@ -104,6 +111,34 @@ def workload(dsg, n, mode, tol, inner=0, graphs=True, tail_nodes=0, omega32=None
         a, b = (int(x) for x in sweeps32.split(","))
         inp = inp.replace(mg32_npre=a, mg32_npost=b)
     return inp
+
+
+def schedule(inp, mode, dsg):
+    """The pressure solve the line measured, in words."""
+    m = dsg.config.MODE_NAMES
+    if mode in (m["tol_mixed"], m["learned"]):
+        fine = (inp.mg32_fine_npre or inp.mg32_npre, inp.mg32_fine_npost or inp.mg32_npost)
+        start = "learned network (guarded by the FP32 FMG start)" if mode == m["learned"] else \
+            {0: "FP32 full multigrid", 1: "previous-step pressure", 2: "zero"}[inp.warm_start]
+        return ("FP64 defect correction (FP64 residual, correction and projection) around FP32 V-cycles: "
+                "%s start, V(%d,%d) on the finest level and V(%d,%d) below, omega %.2f, %s prolongation, "
+                "red-black Gauss-Seidel, to %.0e relative residual"
+                % (start, fine[0], fine[1], inp.mg32_npre, inp.mg32_npost, inp.mg32_omega,
+                   "trilinear" if inp.mg32_prolong == 0 else "piecewise-constant", inp.tol))
+    if mode == m["ref_exact"]:
+        return "the reference's FP64 FMG (fixed cycles, V(%d,%d), omega %.2f), no residual test" % (
+            inp.npre, inp.npost, inp.omega)
+    return ("plain FP64: the reference's FMG, V(%d,%d), omega %.2f, then FP64 V-cycles to %.0e relative residual"
+            % (inp.npre, inp.npost, inp.omega, inp.tol))
+
+
+def dtype_of(mode, dsg):
+    m = dsg.config.MODE_NAMES
+    return "f32+f64" if mode in (m["tol_mixed"], m["learned"]) else "f64"
+
+
+LAMINAR = ("laminar: with k-epsilon on, the reference's explicit k-epsilon update (main.f:1888-2026) "
+           "overflows on the drop by its third step, so that variant has no finite state to time")
 
 
 def measured_peaks():
@@ -199,36 +234,98 @@ def host_cpu():
     return {"model": model or platform.machine(), "nproc": os.cpu_count()}
 
 
-def cpu_baseline(dsg, n, tol, steps=1):
-    """Single-threaded oracle (plain FP64 MG to tol) on a bounded sample."""
+STATE = ["cc", "p", "res", "rhs", "a", "b", "c", "ei", "u", "v", "w",
+         "s11", "s22", "s33", "s12", "s13", "s23", "rhon", "mun"]
+STATE_SCALARS = ("tau", "tauh", "time", "tauh2", "tswap", "npre", "npost", "ntop")
+
+
+def oracle_from_solver(dsg, solver, tol):
+    """A plain FP64 oracle (tol mode) holding the solver's current state."""
     from oracle import Oracle
-    inp = workload(dsg, n, dsg.config.MODE_TOL_FP64, tol)
-    ora = Oracle(inp.as_dict())
-    t0 = time.perf_counter()
-    for t in range(1, steps + 1):
-        ora.step(t)
-    dt = time.perf_counter() - t0
-    return {"value": steps / dt, "unit": UNIT, "cores": 1, "kind": "port", "host": host_cpu(),
-            "sample": "%d time step(s) of the %d^3 workload from its initial condition, C oracle "
-                      "(plain FP64 FMG + V-cycles to %.0e), 1 thread, %.1f s" % (steps, n, tol, dt)}
+    ora = Oracle(solver.inp.replace(mode=dsg.config.MODE_TOL_FP64, tol=tol).as_dict())
+    for f in STATE:
+        solver.download_into(f, ora.field(f).reshape(-1, order="F"))
+    so, sg = ora.scalars(), solver.scalars()
+    for k in STATE_SCALARS:
+        setattr(so, k, getattr(sg, k))
+    ora.set_scalars(so)
+    return ora
+
+
+def field_errors(get, ora):
+    """max|x - oracle| / max|oracle| per field, and the liquid volume's
+    relative difference."""
+    import numpy as np
+    out = {}
+    for f in ("p", "u", "v", "w", "cc"):
+        o = ora.field(f)
+        g = get(f)
+        scale = float(np.max(np.abs(o)))
+        out[f] = float(np.max(np.abs(g - o))) / (scale if scale > 0 else 1.0)
+    return out
 
 
 def run_reference(args):
+    """The reference arm: the oracle (plain FP64 multigrid to tol, one
+    thread) on the same workload and step window as the GPU arm."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
     dsg = importlib.import_module(PKG)
-    steps = max(1, min(args.steps, 3))
-    cb = cpu_baseline(dsg, args.n, args.tol, steps=steps)
-    line = {"metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
-            "warmup": 0, "ms_per_step": 1e3 / cb["value"], "higher_is_better": True, "scaling": "weak",
+    from oracle import Oracle
+    inp = workload(dsg, args.n, dsg.config.MODE_TOL_FP64, args.tol)
+    ora = Oracle(inp.as_dict())
+    w0 = time.perf_counter()
+    for t in range(1, args.warmup + 1):
+        ora.step(t)
+    warm_s = time.perf_counter() - w0
+    # at most 3 timed steps (about 15 s each on one core at 256^3)
+    k = max(1, min(args.steps, 3))
+    t0 = time.perf_counter()
+    for t in range(args.warmup + 1, args.warmup + k + 1):
+        ora.step(t)
+    dt = time.perf_counter() - t0
+    value = k / dt
+    cb = {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "host": host_cpu(),
+          "sample": "time steps %d-%d of the %d^3 workload (after %d untimed warm-up steps, %.0f s), C oracle "
+                    "(plain FP64 FMG + V-cycles to %.0e), 1 thread (the reference is serial), %.1f s"
+                    % (args.warmup + 1, args.warmup + k, args.n, args.warmup, warm_s, args.tol, dt)}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": k,
+            "steps_requested": args.steps, "warmup": args.warmup, "window": [args.warmup + 1, args.warmup + k],
+            "ms_per_step": 1e3 / value, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "splash-on-wall droplet %d^3, 3 m/s, laminar, plain FP64 MG to %.0e"
-                                   % (args.n, args.tol)},
+            "config": {"workload": "splash-on-wall droplet %d^3 cells (%d^3 nodes), 3 m/s, %s"
+                                   % (args.n, args.n + 2, LAMINAR),
+                       "solver": schedule(inp, dsg.config.MODE_TOL_FP64, dsg)},
             "impl": "reference", "cpu_baseline": cb,
-            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
+
+
+def relax_roofline(prof, step_ms, n):
+    """Roofline entry of the finest-level relax from the live CUDA-event
+    profile: algorithmic bytes per call / mean call time against the measured
+    HBM copy bandwidth."""
+    peak, peak_kind = measured_peaks()
+    achieved = None
+    if prof["relax_calls"]:
+        per_call_ms = prof["relax_ms"] / prof["relax_calls"]
+        per_call_bytes = prof["relax_bytes"] / prof["relax_calls"]
+        achieved = per_call_bytes / (per_call_ms / 1e3) / 1e9
+    split = prof.get("relax_bits") == 32
+    kname = "k_relax32_split" if split else "k_relax_colour"
+    return {"bound": "hbm",
+            "kernel": ("%s: finest-level relax, colour-split FP32 red-black sweep, 2 launches per relax "
+                       "(other colour, own colour r+w, own rhs, cc: 24 B/cell)" % kname if split
+                       else "%s: finest-level relax, 2 red-black FP64 colour passes (u r+w, a, b, c, rhs: "
+                            "48 B/cell)" % kname),
+            "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": (achieved / peak) if achieved else None, "traffic": committed_traffic(kname, n),
+            "peak_kind": peak_kind,
+            "bytes_per_launch": (prof["relax_bytes"] / prof["relax_calls"]) if prof["relax_calls"] else None,
+            "relax_calls": prof["relax_calls"],
+            "share_of_step": (prof["relax_ms"] / step_ms) if step_ms else None}
 
 
 def mode_of(dsg, name):
@@ -307,8 +404,13 @@ def run_gb300(args):
         ps.set_stream(torch.cuda.current_stream().cuda_stream)
         for t in range(1, args.warmup + 1):
             ps.step(t)
+        ps.profile_enable(True)
         pms, pst = time_steps(torch, ps, args.steps, args.warmup + 1)
-        plain = {"value": args.steps / (pms / 1e3), "vcycles": [s["vcycles"] for s in pst]}
+        pprof = ps.profile_read()
+        ps.profile_enable(False)
+        plain = {"value": args.steps / (pms / 1e3), "ms_per_step": pms / args.steps,
+                 "vcycles": [s["vcycles"] for s in pst], "solver": schedule(p_inp, p_inp.mode, dsg),
+                 "roofline": relax_roofline(pprof, pms, args.n)}
         ps.close()
 
     # the learned warm start (committed weights), same workload, as a measured
@@ -331,6 +433,47 @@ def run_gb300(args):
             ls.close()
             net.close()
 
+    # error against the FP64 oracle from one shared state: the state after
+    # the timed steps goes into the oracle (plain FP64 to the same tolerance)
+    # and into a plain FP64 GPU solver; one more step of each, and of the
+    # headline solver, is compared field by field.  The oracle step is also
+    # the CPU baseline: one step of the same workload in the same window.
+    t_next = args.warmup + args.steps + 1
+    cb, err = None, None
+    if ws == 1 and rank == 0 and not args.no_cpu_baseline:
+        ora = oracle_from_solver(dsg, solver, args.tol)
+        p2 = None
+        if mode != dsg.config.MODE_TOL_FP64:
+            p2 = dsg.Solver(inp.replace(mode=dsg.config.MODE_TOL_FP64), init=False)
+            p2.set_stream(torch.cuda.current_stream().cuda_stream)
+            for f in STATE:
+                p2.upload(f, ora.field(f))
+            p2.set_scalars(solver.scalars())
+        c0 = time.perf_counter()
+        ora.step(t_next)
+        cdt = time.perf_counter() - c0
+        cb = {"value": 1.0 / cdt, "unit": UNIT, "cores": 1, "kind": "port", "host": host_cpu(),
+              "sample": "time step %d of the %d^3 workload from the GPU state after the timed steps, C oracle "
+                        "(plain FP64 FMG + V-cycles to %.0e), 1 thread (the reference is serial), %.1f s"
+                        % (t_next, args.n, args.tol, cdt)}
+        st_h = solver.step(t_next)
+        vo = ora.liquid_volume()
+        err = {"step": t_next, "state": "GPU state after the timed steps, loaded into both",
+               "norm": "max|x - oracle| / max|oracle| over the whole field",
+               "oracle": "C oracle, plain FP64 multigrid to %.0e" % args.tol,
+               "oracle_relres": ora.scalars().last_relres,
+               "headline": field_errors(solver.field, ora)}
+        err["headline"]["volume"] = abs(solver.liquid_volume() - vo) / abs(vo)
+        err["headline"]["relres"] = st_h["relres"]
+        if p2 is not None:
+            st_p = p2.step(t_next)
+            err["plain_fp64"] = field_errors(p2.field, ora)
+            err["plain_fp64"]["volume"] = abs(p2.liquid_volume() - vo) / abs(vo)
+            err["plain_fp64"]["relres"] = st_p["relres"]
+            p2.close()
+        ora.close()
+        t_next += 1
+
     # end to end through the public API: pinned host state in, results out,
     # every step through dsg_step_host (the copies overlap the step's phases)
     e2e = None
@@ -346,7 +489,7 @@ def run_gb300(args):
         k2 = max(1, args.e2e_steps)
         torch.cuda.synchronize()
         t_start = time.perf_counter()
-        t = args.warmup + args.steps
+        t = t_next - 1
         for _ in range(k2):
             t += 1
             solver.step_host({nm: host[nm] for nm in ins}, {nm: host[nm] for nm in outs}, t)
@@ -357,40 +500,21 @@ def run_gb300(args):
     solver.close()
 
     if rank == 0:
-        peak, peak_kind = measured_peaks()
-        achieved = None
-        if prof["relax_calls"]:
-            per_call_ms = prof["relax_ms"] / prof["relax_calls"]
-            per_call_bytes = prof["relax_bytes"] / prof["relax_calls"]
-            achieved = per_call_bytes / (per_call_ms / 1e3) / 1e9
-        split = prof.get("relax_bits") == 32
-        kname = "k_relax32_split" if split else "k_relax_colour"
-        traffic = committed_traffic(kname, args.n)
-        roof = {"bound": "hbm",
-                "kernel": ("finest-level relax, colour-split FP32 red-black sweep, 2 launches per relax "
-                           "(other colour, own colour r+w, own rhs, cc: 24 B/cell)" if split
-                           else "finest-level relax, 2 red-black FP64 colour passes (6 words/cell)"),
-                "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                "peak_kind": peak_kind,
-                "bytes_per_launch": (prof["relax_bytes"] / prof["relax_calls"]) if prof["relax_calls"] else None,
-                "share_of_step": (prof["relax_ms"] / ms) if ms else None}
-        cb = None
-        if ws == 1 and not args.no_cpu_baseline:
-            cb = cpu_baseline(dsg, args.n, args.tol, steps=1)
+        roof = relax_roofline(prof, ms, args.n)
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": "splash-on-wall droplet %d^3 cells (%d^3 nodes), 3 m/s, laminar, "
-                                       "4/4 RBGS sweeps, pressure to %.0e relative residual"
-                                       % (args.n, args.n + 2, args.tol),
+                "warmup": args.warmup, "window": [args.warmup + 1, args.warmup + args.steps],
+                "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": dtype_of(mode, dsg), "data": "synthetic",
+                "config": {"workload": "splash-on-wall droplet %d^3 cells (%d^3 nodes), 3 m/s, %s"
+                                       % (args.n, args.n + 2, LAMINAR),
+                           "solver": schedule(inp, mode, dsg),
                            "mode": [k for k, v in dsg.config.MODE_NAMES.items() if v == mode][0],
                            "l2": "inputs larger than L2: per-step working set %.1f GB >> 129 MB L2, no flush"
                                  % (solver_bytes_estimate(inp) / 1e9),
                            "parallelism": "replicas" if ws > 1 else "single"},
                 "vcycles_per_step": vcycles, "gpu_launches": prof["launches"], "roofline": roof,
                 "phase_ms_per_step": {k: v / args.steps for k, v in prof["phase_ms"].items()},
-                "cpu_baseline": cb, "e2e": e2e, "clocks": clk}
+                "cpu_baseline": cb, "e2e": e2e, "clocks": clk, "error_vs_fp64": err}
         if plain:
             line["plain_fp64"] = plain
         if learned:

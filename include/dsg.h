@@ -107,6 +107,9 @@ typedef struct dsg_config {
   int mg32_small_npre; /* pre-/post-sweeps of the FP32 V-cycles on the levels of at most 18^3 nodes below
                           the finest (<= 0: as on the other levels) */
   int mg32_small_npost;
+  int fp64_exact;      /* DSG_MODE_TOL_FP64: 0 = sweeps, residuals and norm as fused multiply-adds (fewer
+                          FP64 operations, results within ulps of the oracle), 1 = the reference's operation
+                          order (bit-identical to the oracle).  DSG_MODE_REF_EXACT always keeps that order. */
 } dsg_config;
 
 /* Non-dimensional scalars and adaptive counters (COMMON /PHYSICS/, /DIFF/,
@@ -162,20 +165,23 @@ int dsg_set_scalars(dsg_ctx *ctx, const dsg_scalars *in);
 /* initialize, restart=0 drop case: smooth2 (+ seeded noise) + bc_c + bc_v +
  * calcrho (main.f:159-178, 5678-5752). */
 int dsg_init_drop(dsg_ctx *ctx);
-/* VOFmethod(t) main.f:795-824 */
+/* VOFmethod(t) main.f:795-824 (+ fturbdif main.f:1239-1267 when iturb != 0) */
 int dsg_vofmethod(dsg_ctx *ctx);
+/* kepsmodel main.f:1888-2025 (iturb = 3; no-op for iturb = 0) */
+int dsg_kepsmodel(dsg_ctx *ctx);
 /* checktime(t) main.f:2152-2171 (one device max-reduction, one host read) */
-int dsg_kepsmodel(dsg_ctx *ctx); /* kepsmodel main.f:1888-2025 (iturb = 3; no-op for iturb = 0) */
 int dsg_checktime(dsg_ctx *ctx);
-/* csf(ccc,w11,w22,w33) main.f:2363-2481 */
-/* csf main.f:2363-2481 (surfacet = 2), SGIP 2835-3026 (surfacet = 5) or SGIP2 3029-3166 (surfacet = 6) */
+/* csf(ccc,w11,w22,w33) main.f:2363-2481 (surfacet = 2), SGIP main.f:2835-3026
+ * (surfacet = 5) or SGIP2 main.f:3029-3166 (surfacet = 6) */
 int dsg_csf(dsg_ctx *ctx);
 int dsg_calch3d(dsg_ctx *ctx); /* CalcH3d main.f:1312-1810 (the step calls it when hswitch = 1) */
 /* solvelpres(cc,w1..w3,a,b,c,ei,t) main.f:3236-3439, pressure solve per mode */
 int dsg_solvelpres(dsg_ctx *ctx, int t, dsg_mg_stats *stats);
 /* mglin(r1,r2) main.f:3645-3763 on the resident fine rhs and coefficients */
 int dsg_mglin(dsg_ctx *ctx, dsg_mg_stats *stats);
-/* One body of the main.f:19-73 loop with surfacet=2 (CSF), hswitch=0, laminar. */
+/* One body of the main.f:19-73 loop: VOFmethod (+ CalcH3d when hswitch = 1,
+ * + kepsmodel when iturb = 3), checktime, the surface-tension model of
+ * surfacet (2 CSF, 5 SGIP, 6 SGIP2) and solvelpres in the context's mode. */
 int dsg_step(dsg_ctx *ctx, int t, dsg_mg_stats *stats);
 /* dsg_step with the state exchanged through host arrays, as a host that owns
    its fields (the reference's COMMON blocks) needs it: the fields
@@ -343,7 +349,9 @@ int dsg_ensemble_plan(const double *cost, int n, int workers, int *assign);
  * ghosts included), rhs, a, b, c, ei of size nx*ny*nz.  Coarse levels and the
  * finest residual live in one static device array sized for grids up to
  * 66x66x66 nodes (about 5.3 MB, held on every device that loads the library
- * until exit); larger grids return DSG_E_ARG.  Nothing is allocated.  Calls
+ * until exit); larger grids, and grids whose sides do not all halve evenly
+ * down to the coarsest level of min(nx,ny,nz) = 2^ng+2, return DSG_E_ARG.
+ * Nothing is allocated.  Calls
  * share that array: each call clears it first, but calls that overlap on the
  * GPU race and must be serialized.  The first call on a device looks up the
  * array's address with that device current; make it before any stream

@@ -89,10 +89,10 @@ def test_inputdata_positional_order():
 
 
 def test_fortran_binding_matches_config():
-    """The ISO_C_BINDING type in the integration notes lists dsg_config's
-    fields in the C order with matching kinds, so a Fortran host that copies
+    """The ISO_C_BINDING type of include/dsg_binding.f90 lists dsg_config's
+    fields in the C order with matching kinds, so a Fortran host that uses
     it passes its values where the library reads them."""
-    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    text = open(os.path.join(ROOT, "include", "dsg_binding.f90")).read()
     block = re.search(r"type, bind\(C\) :: dsg_config\n(.*?)\n\s*end type", text, re.S).group(1)
     fortran = []
     for line in block.splitlines():
@@ -104,3 +104,19 @@ def test_fortran_binding_matches_config():
     kinds = {C.c_int: "c_int", C.c_double: "c_double", C.c_uint64: "c_int64_t"}
     want = [(n, kinds[t]) for n, t in dsg._lib.DsgConfig._fields_]
     assert fortran == want
+
+
+def test_fortran_interfaces_name_declared_entry_points():
+    """Every bind(C) interface of include/dsg_binding.f90 names a function
+    that dsg.h declares, with the same number of arguments."""
+    f90 = open(os.path.join(ROOT, "include", "dsg_binding.f90")).read()
+    hdr = open(os.path.join(ROOT, "include", "dsg.h")).read()
+    decls = re.findall(r"(?:function|subroutine)\s+(\w+)\(([^)]*)\)\s*(?:&\s*\n\s*([^)]*)\))?\s*bind\(C, name='(\w+)'\)",
+                       f90)
+    assert len(decls) >= 10
+    for fname, args, more, cname in decls:
+        assert fname == cname
+        nargs = len([a for a in (args + ("," + more if more else "")).split(",") if a.strip()])
+        m = re.search(r"\b%s\(([^;]*)\);" % cname, hdr, re.S)
+        assert m, cname
+        assert len([a for a in m.group(1).split(",") if a.strip()]) == nargs, cname

@@ -229,3 +229,25 @@ def test_csf_curvature_of_a_sphere():
     k16 = _sphere_curvature(64, 16.0) * 16.0
     assert abs(k8 - k16) < 0.01 * k16, (k8, k16)
     assert abs(k16 - 2.0) < 0.15 * 2.0, k16
+
+
+def test_oracle_reproduces_committed_trajectory():
+    """The first 20 steps of the committed 64^3 trajectory (made by
+    tests/golden/trajectory.py) come out of the oracle again: the fixture the
+    GPU trajectory tests compare against is the oracle's."""
+    from golden import trajectory as tj
+    inp = tj.cases()["traj64_ref"]["inp"]
+    ref = tj.load("traj64_ref")
+    o = oo.Oracle(inp.as_dict())
+    for t in range(1, 21):
+        o.step(t)
+        s = o.scalars()
+        fields = {f: o.field(f) for f in tj.DIGEST_FIELDS}
+        scal = dict(tau=s.tau, volume=o.liquid_volume(), npre=s.npre, npost=s.npost, ntop=s.ntop,
+                    tswap=s.tswap, vcycles=s.last_vcycles)
+        agg, smp, sc = tj.record(fields, scal)
+        ra = ref["agg"][t - 1]
+        scale = np.maximum(np.abs(ra[:, 1:2]), 1e-300)  # sum |.| of each field
+        assert np.all(np.abs(agg - ra) <= 1e-12 * scale), t
+        assert np.allclose(smp, ref["smp"][t - 1], rtol=1e-12, atol=0.0), t
+        assert np.allclose(sc, ref["sc"][t - 1], rtol=1e-13, atol=0.0), t

@@ -124,3 +124,23 @@ def test_step_against_golden_fixture(gpu_lib):
         vol = float.fromhex(ref["t%d_volume" % t])
         assert abs(gpu.liquid_volume() - vol) <= 1e-12 * vol
         assert gpu.scalars().tau == float.fromhex(ref["t%d_tau" % t])
+
+
+def test_tol_fp64_fma_form_tracks_exact_order(gpu_lib):
+    """The tolerance mode's FP64 multigrid in fused multiply-add form (the
+    default) takes the same V-cycles as the reference's operation order and
+    lands within 1e-12 of it; both stay within the field tolerance of the
+    oracle."""
+    dsg = gpu_lib
+    from oracle import Oracle
+    inp = dsg.config.droplet(32, mode=dsg.config.MODE_TOL_FP64, tol=1e-10, steps=5)
+    ora = Oracle(inp.as_dict())
+    with dsg.Solver(inp) as fma, dsg.Solver(inp.replace(fp64_exact=1)) as exact:
+        for t in range(1, 6):
+            ora.step(t)
+            sf, se = fma.step(t), exact.step(t)
+            assert sf["vcycles"] == se["vcycles"] == ora.scalars().last_vcycles, (t, sf, se)
+            for name in ("p", "u", "v", "w", "cc"):
+                assert relerr(fma.field(name), exact.field(name)) <= 1e-12, (t, name)
+                assert relerr(fma.field(name), ora.field(name)) <= FIELD_TOL, (t, name)
+                assert relerr(exact.field(name), ora.field(name)) <= FIELD_TOL, (t, name)

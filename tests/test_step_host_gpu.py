@@ -2,15 +2,18 @@
 copies overlapped with the step's phases, computes the same bits as
 upload + dsg_step + download.
 
-Each input's device copy is overwritten with zeros before the call, so an
-input that arrived after the first phase touching it would change the result.
+Each input's device copy is overwritten with zeros before the call, and the
+host arrays hold values the step itself overwrites (nonzero ghost faces on the
+stress components, which csf's bc_tensor zeroes; random face coefficients and
+previous pressure, which the pressure phase rebuilds), so an input that
+arrived after the first phase touching it would change the result.
 """
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
 
-INS = ["cc", "u", "v", "w", "s11", "s22", "s33", "s12", "s13", "s23"]
+INS = ["cc", "u", "v", "w", "s11", "s22", "s33", "s12", "s13", "s23", "a", "b", "c", "pprev"]
 OUTS = ["p", "cc", "u", "v", "w", "s11", "s22", "s33", "s12", "s13", "s23", "rhon", "mun"]
 
 
@@ -26,6 +29,19 @@ def _variants(dsg):
     }
 
 
+def _perturbed(name, arr, rng):
+    """The host copy of an input, changed where the step writes before it reads."""
+    a = np.array(arr, order="F")
+    if name in ("s12", "s13", "s23"):
+        for sl in ((0,), (-1,)):
+            a[sl[0], :, :] = 7.0
+            a[:, sl[0], :] = 7.0
+            a[:, :, sl[0]] = 7.0
+    elif name in ("a", "b", "c", "pprev"):
+        a[...] = rng.uniform(1.0, 2.0, a.shape)
+    return np.ascontiguousarray(a.ravel(order="F"))
+
+
 @pytest.mark.parametrize("name", ["csf", "sgip", "sgip2_fp64", "no_tension", "keps"])
 def test_step_host_matches_step(gpu_lib, name):
     dsg = gpu_lib
@@ -35,10 +51,12 @@ def test_step_host_matches_step(gpu_lib, name):
     with dsg.Solver(cfg) as a, dsg.Solver(cfg) as b:
         a.step(1)
         b.step(1)
+        rng = np.random.default_rng(5)
         for t in range(2, 2 + steps):
-            host_in = {k: np.ascontiguousarray(b.field(k).ravel(order="F")) for k in ins}
-            for k in ins:  # stale device copies: only the host arrays hold the state
-                b.set_field(k, np.zeros(b.shape))
+            host_in = {k: _perturbed(k, b.field(k), rng) for k in ins}
+            for k in ins:
+                a.set_field(k, host_in[k].reshape(a.shape, order="F"))
+                b.set_field(k, np.zeros(b.shape))  # stale device copies: only the host arrays hold the state
             host_out = {k: np.empty(b.shape[0] * b.shape[1] * b.shape[2]) for k in outs}
             sa = a.step(t)
             sb = b.step_host(host_in, host_out, t)

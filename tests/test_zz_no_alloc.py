@@ -5,7 +5,8 @@ solve (their host owns the device arrays and forbids allocation after set-up,
 or the solve runs where an allocation would synchronize the device).  It must
 give the same pressure as dsg_mglin in the reference's fixed-cycle mode, on
 two calls in a row (its static scratch keeps the previous call's contents),
-and reject grids beyond its 66^3-node capacity.
+and reject grids beyond its 66^3-node capacity or whose sides do not all halve
+evenly down to the coarsest level.
 """
 import ctypes as C
 
@@ -69,3 +70,16 @@ def test_noalloc_rejects_large_grid(gpu_lib):
     rc = lib.dsg_mglin_noalloc(ptr, ptr, ptr, ptr, ptr, ptr, 130, 130, 130, 2, 4, 4, 4, 1.5, 1.0, 1.0, None)
     assert rc == -1
     assert b"capacity" in lib.dsg_last_error(None)
+
+
+def test_noalloc_rejects_uneven_grid(gpu_lib):
+    """34 x 34 x 64 nodes: the 62-cell side does not halve evenly over the
+    five levels its 32-cell sides give."""
+    import torch
+    dsg = gpu_lib
+    lib = _lib(dsg)
+    x = torch.zeros(8, dtype=torch.float64, device="cuda")
+    ptr = x.data_ptr()
+    rc = lib.dsg_mglin_noalloc(ptr, ptr, ptr, ptr, ptr, ptr, 34, 34, 64, 2, 4, 4, 4, 1.5, 1.0, 1.0, None)
+    assert rc == -1
+    assert b"evenly" in lib.dsg_last_error(None)
