@@ -166,6 +166,11 @@ SIGNATURES = [
     ("dsg_ensemble_step", _i, [_vp, _i, C.POINTER(DsgMgStats)]),
     ("dsg_ensemble_last_ms", _d, [_vp]),
     ("dsg_ensemble_member_ms", _i, [_vp, _DPP]),
+    ("dsg_ensemble_set_batched", _i, [_vp, _i]),
+    ("dsg_ensemble_batched", _i, [_vp]),
+    ("dsg_ensemble_phase_ms", _i, [_vp, _DPP]),
+    ("dsg_ensemble_autotune_tiles", _i, [_vp, _i, C.POINTER(_i)]),
+    ("dsg_ensemble_batch_tail_nodes", C.c_int64, [_vp]),
     ("dsg_ensemble_autotune", _i, [_vp, _i, _i, _IP, _IP]),
     ("dsg_ensemble_plan", _i, [_DPP, _i, _i, _IP]),
 ]

@@ -32,7 +32,9 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-
 # within ulps of the non-contracted oracle, far inside the 1e-10 parity bar).
 # The array-level FP64 kernels (mg64.cu), the VOF geometry and k-epsilon stay
 # uncontracted: they are bit-identical to the oracle.
-FMAD_TRUE = {"mg32.cu", "nn.cu", "momentum.cu", "csf.cu"}
+# batch.cu runs the same FP32 block bodies as mg32.cu (mg32_cells.cuh) and must
+# be compiled the same way so that batched members reproduce standalone bits.
+FMAD_TRUE = {"mg32.cu", "batch.cu", "nn.cu", "momentum.cu", "csf.cu"}
 
 
 def nvcc():

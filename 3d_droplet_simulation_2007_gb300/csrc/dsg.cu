@@ -194,75 +194,7 @@ int relres_host(dsg_ctx *ctx, double *out) {
 }
 
 // ---- mixed precision: FP32 V-cycles inside FP64 defect correction ---------
-enum { U32 = 0, RHS32 = 1, A32 = 2, B32 = 3, C32 = 4, EI32 = 5 };
-
-// Relaxation factor of the FP32 V-cycle (a preconditioner of the FP64 defect
-// correction, so free to differ from the reference's OMEGA).
-inline float omega32(const dsg_ctx *ctx) {
-  return (float)(ctx->cfg.mg32_omega > 0.0 ? ctx->cfg.mg32_omega : ctx->cfg.omega);
-}
-
-// Sweeps of the FP32 V-cycle: the reference's (adaptive) NPRE/NPOST unless
-// the configuration fixes them.
-inline int pre32(const dsg_ctx *ctx) { return ctx->cfg.mg32_npre > 0 ? ctx->cfg.mg32_npre : ctx->s.npre; }
-inline int post32(const dsg_ctx *ctx) { return ctx->cfg.mg32_npost > 0 ? ctx->cfg.mg32_npost : ctx->s.npost; }
-
-// Levels of at most this many nodes may have their own sweep counts
-// (mg32_small_npre/npost): the levels the coarse tail runs by default.
-constexpr long long kSmallLevelNodes = 18LL * 18 * 18;
-
-inline bool small_level(const dsg_ctx *ctx, int l) {
-  return (long long)ctx->lnx[l] * ctx->lny[l] * ctx->lnz[l] <= kSmallLevelNodes;
-}
-
-// Sweeps on level l: the finest level, the one below it and the small levels
-// may have their own counts (a sweep on the finest level costs 8x and on the
-// next 2-3x one of the smaller levels, which are bound by launch latency or,
-// inside the coarse tail, by one SM's issue rate).
-inline int pre32(const dsg_ctx *ctx, int l) {
-  if (l == ctx->ng && ctx->cfg.mg32_fine_npre > 0) return ctx->cfg.mg32_fine_npre;
-  if (l == ctx->ng - 1 && ctx->cfg.mg32_mid_npre > 0) return ctx->cfg.mg32_mid_npre;
-  if (l < ctx->ng && small_level(ctx, l) && ctx->cfg.mg32_small_npre > 0) return ctx->cfg.mg32_small_npre;
-  return pre32(ctx);
-}
-inline int post32(const dsg_ctx *ctx, int l) {
-  if (l == ctx->ng && ctx->cfg.mg32_fine_npost > 0) return ctx->cfg.mg32_fine_npost;
-  if (l == ctx->ng - 1 && ctx->cfg.mg32_mid_npost > 0) return ctx->cfg.mg32_mid_npost;
-  if (l < ctx->ng && small_level(ctx, l) && ctx->cfg.mg32_small_npost > 0) return ctx->cfg.mg32_small_npost;
-  return post32(ctx);
-}
-
-// Prolongation of the FP32 V-cycles and FMG start: trilinear unless the
-// configuration asks for the reference's injection.
-inline int tri32(const dsg_ctx *ctx) { return ctx->cfg.mg32_prolong == 1 ? 0 : 1; }
-
-inline float level_h2(dsg_ctx *ctx, int l) {
-  const double h1 = ctx->s.lengthsize / (ctx->lnx[l] - 2);
-  return (float)(h1 * h1);
-}
-
-// Finest-level colour-split FP32 arrays: {even, odd} halves of U and RHS.
-struct FineSplit {
-  float *u[2];
-  float *r[2];
-};
-
-inline FineSplit fine_split(dsg_ctx *ctx) {
-  float **L = ctx->lv32[ctx->ng];
-  const dsg::Dims d = ctx->fine();
-  const size_t half = (size_t)((d.nx - 2) >> 1) * (d.ny - 2) * (d.nz - 2);
-  return FineSplit{{L[U32], L[U32] + half}, {L[RHS32], L[RHS32] + half}};
-}
-
-inline size_t fine_split_bytes(dsg_ctx *ctx) {
-  const dsg::Dims d = ctx->fine();
-  return 2 * (size_t)((d.nx - 2) >> 1) * (d.ny - 2) * (d.nz - 2) * sizeof(float);
-}
-
-inline void phase_coefs(dsg_ctx *ctx, float *r1, float *r2) {
-  *r1 = (float)(0.5 * (ctx->s.rho1 - ctx->s.rho2));
-  *r2 = (float)ctx->s.rho2;
-}
+using namespace dsg::mixed;
 
 cudaError_t relax32_level(dsg_ctx *ctx, int n, int l) {
   float **L = ctx->lv32[l];
@@ -324,20 +256,6 @@ cudaError_t relax32_level(dsg_ctx *ctx, int n, int l) {
     ctx->prof_relax_bits = 32;
   }
   return e;
-}
-
-// Arguments of the coarse-tail kernel for FP32 levels 1..top of ctx.
-void tail_args(dsg_ctx *ctx, int top, dsg::TailArgs *A) {
-  memset(A, 0, sizeof *A);
-  for (int l = 1; l <= top; l++) {
-    float **L = ctx->lv32[l];
-    A->lv[l] = dsg::TailLevel{L[U32],       L[RHS32],          L[A32],     L[B32],         L[C32],
-                              L[EI32],      ctx->level(l),     level_h2(ctx, l), pre32(ctx, l), post32(ctx, l)};
-  }
-  A->top = top;
-  A->ntop = ctx->s.ntop;
-  A->omega = omega32(ctx);
-  A->tri = tri32(ctx);
 }
 
 int vcycle32(dsg_ctx *ctx, int j) {
@@ -669,6 +587,26 @@ int mixed_solve(dsg_ctx *ctx, dsg_mg_stats *s) {
   return DSG_OK;
 }
 
+}  // namespace
+
+// After a mixed-precision solve (standalone or batched): the training pair of
+// an attached network, the context's record of the solve, the caller's
+// statistics, and DSG_E_NOT_CONVERGED when the cycle cap stopped it.
+int dsg::mixed_finish(dsg_ctx *ctx, dsg_mg_stats *s, dsg_mg_stats *stats) {
+  int rc = record_pair(ctx);
+  if (rc) return rc;
+  ctx->s.last_vcycles = s->vcycles;
+  ctx->s.last_relres = s->relres;
+  ctx->s.last_relres_fmg = s->relres_init;
+  if (stats) *stats = *s;
+  if (!s->converged)
+    return dsg::set_error(ctx, DSG_E_NOT_CONVERGED, "mixed multigrid reached %d cycles at relres %.3e > tol %.3e",
+                          s->vcycles, s->relres, ctx->cfg.tol);
+  return DSG_OK;
+}
+
+namespace {
+
 int mglin(dsg_ctx *ctx, dsg_mg_stats *stats) {
   const int ng = ctx->ng;
   const double om = ctx->cfg.omega;
@@ -683,16 +621,7 @@ int mglin(dsg_ctx *ctx, dsg_mg_stats *stats) {
     s.epsdiv = -1.0;
     int rc = mixed_solve(ctx, &s);
     if (rc) return rc;
-    rc = record_pair(ctx);
-    if (rc) return rc;
-    ctx->s.last_vcycles = s.vcycles;
-    ctx->s.last_relres = s.relres;
-    ctx->s.last_relres_fmg = s.relres_init;
-    if (stats) *stats = s;
-    if (!s.converged)
-      return dsg::set_error(ctx, DSG_E_NOT_CONVERGED, "mixed multigrid reached %d cycles at relres %.3e > tol %.3e",
-                            s.vcycles, s.relres, ctx->cfg.tol);
-    return DSG_OK;
+    return dsg::mixed_finish(ctx, &s, stats);
   }
   for (int g = ng - 1; g >= 1; g--) {
     const Dims dc = ctx->level(g);
@@ -1136,6 +1065,21 @@ int dsg_mglin(dsg_ctx *ctx, dsg_mg_stats *stats) {
 
 int dsg_solvelpres(dsg_ctx *ctx, int t, dsg_mg_stats *stats) {
   if (!ctx) return DSG_E_ARG;
+  int rc = dsg::solvelpres_pre(ctx);
+  if (rc) return rc;
+  dsg_mg_stats ms;
+  memset(&ms, 0, sizeof ms);
+  rc = mglin(ctx, &ms);
+  if (rc && rc != DSG_E_NOT_CONVERGED) return rc;
+  return dsg::solvelpres_post(ctx, t, &ms, rc, stats);
+}
+
+}  // extern "C"
+
+// solvelpres up to the pressure solve (main.f:3236-3355): stresses, the
+// coefficients of abcei, predictor, convection, boundary values and the
+// divergence right-hand side.
+int dsg::solvelpres_pre(dsg_ctx *ctx) {
   dsg_scalars &s = ctx->s;
   const Dims d = ctx->fine();
   cudaStream_t st = ctx->stream;
@@ -1162,12 +1106,24 @@ int dsg_solvelpres(dsg_ctx *ctx, int t, dsg_mg_stats *stats) {
   DSG_CK(ctx, dsg::bc_v(u, v, w, ctx->red_partials, d, s.xvel2, st));
   const double hi2 = 1.0 / (s.h * s.h);
   DSG_CK(ctx, dsg::divergence(w3, u, v, w, d, hi2, st));
-  dsg_mg_stats ms;
-  memset(&ms, 0, sizeof ms);
   DSG_CK(ctx, phase_mark(ctx, 4));
-  int rc = mglin(ctx, &ms);
-  if (rc && rc != DSG_E_NOT_CONVERGED) return rc;
-  const int mg_rc = rc;
+  return DSG_OK;
+}
+
+// solvelpres after the pressure solve (main.f:3371-3439): projection,
+// boundary values and the relaxation-count adaptivity.  ms: the solve's
+// statistics; mg_rc: its status (DSG_OK or DSG_E_NOT_CONVERGED), returned
+// when nothing else fails.
+int dsg::solvelpres_post(dsg_ctx *ctx, int t, dsg_mg_stats *ms_in, int mg_rc, dsg_mg_stats *stats) {
+  dsg_scalars &s = ctx->s;
+  const Dims d = ctx->fine();
+  cudaStream_t st = ctx->stream;
+  double *w1 = ctx->f[DSG_F_P], *w3 = ctx->f[DSG_F_RHS];
+  double *a = ctx->f[DSG_F_A], *b = ctx->f[DSG_F_B], *c = ctx->f[DSG_F_C];
+  double *u = ctx->f[DSG_F_U], *v = ctx->f[DSG_F_V], *w = ctx->f[DSG_F_W];
+  const double hi2 = 1.0 / (s.h * s.h);
+  dsg_mg_stats ms = *ms_in;
+  int rc;
   if ((rc = sync_point(ctx, SP_MG))) return rc;
   DSG_CK(ctx, phase_mark(ctx, 5));
   if (ctx->net)
@@ -1202,8 +1158,6 @@ int dsg_solvelpres(dsg_ctx *ctx, int t, dsg_mg_stats *stats) {
   return mg_rc;
 }
 
-}  // extern "C"
-
 namespace {
 
 // One time step in the order of the main.f:19-73 loop body: VOF (VOFmethod,
@@ -1212,6 +1166,21 @@ namespace {
 // solve that stops at its cycle cap still completes the step and its
 // DSG_E_NOT_CONVERGED is returned after the last sync point.
 int step_phases(dsg_ctx *ctx, int t, dsg_mg_stats *stats) {
+  int rc = dsg::step_pre_solve(ctx, t);
+  if (rc) return rc;
+  dsg_mg_stats ms;
+  memset(&ms, 0, sizeof ms);
+  rc = mglin(ctx, &ms);
+  if (rc && rc != DSG_E_NOT_CONVERGED) return rc;
+  return dsg::step_post_solve(ctx, t, &ms, rc, stats);
+}
+
+}  // namespace
+
+// The step up to the pressure solve: VOF, CFL, surface tension and the first
+// part of solvelpres.
+int dsg::step_pre_solve(dsg_ctx *ctx, int t) {
+  (void)t;
   DSG_CK(ctx, phase_mark(ctx, 0));
   int rc = dsg_vofmethod(ctx);
   if (rc) return rc;
@@ -1227,12 +1196,20 @@ int step_phases(dsg_ctx *ctx, int t, dsg_mg_stats *stats) {
   DSG_CK(ctx, phase_mark(ctx, 2));
   rc = dsg_csf(ctx);
   if (rc || (rc = sync_point(ctx, SP_CSF))) return rc;
-  rc = dsg_solvelpres(ctx, t, stats);
+  return dsg::solvelpres_pre(ctx);
+}
+
+// The step after the pressure solve (ms, mg_rc: the solve's statistics and
+// status, DSG_OK or DSG_E_NOT_CONVERGED, returned when nothing else fails).
+int dsg::step_post_solve(dsg_ctx *ctx, int t, dsg_mg_stats *ms, int mg_rc, dsg_mg_stats *stats) {
+  int rc = dsg::solvelpres_post(ctx, t, ms, mg_rc, stats);
   if (rc && rc != DSG_E_NOT_CONVERGED) return rc;
   DSG_CK(ctx, phase_mark(ctx, -1));
   const int rh = sync_point(ctx, SP_END);
   return rh ? rh : rc;
 }
+
+namespace {
 
 // Sync point before which an input of field f must have arrived from the
 // host: before the first work that reads or writes it.  u, v, w are read first

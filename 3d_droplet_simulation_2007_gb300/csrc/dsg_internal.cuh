@@ -303,8 +303,114 @@ struct dsg_ctx {
 };
 
 namespace dsg {
+// ---- settings of the mixed-precision solve, shared by the standalone solve
+// (dsg.cu) and the batched ensemble solve (batch.cu) ----------------------
+namespace mixed {
+enum { U32 = 0, RHS32 = 1, A32 = 2, B32 = 3, C32 = 4, EI32 = 5 };
+
+// Relaxation factor of the FP32 V-cycle (a preconditioner of the FP64 defect
+// correction, so free to differ from the reference's OMEGA).
+inline float omega32(const dsg_ctx *ctx) {
+  return (float)(ctx->cfg.mg32_omega > 0.0 ? ctx->cfg.mg32_omega : ctx->cfg.omega);
+}
+
+// Sweeps of the FP32 V-cycle: the reference's (adaptive) NPRE/NPOST unless
+// the configuration fixes them.
+inline int pre32(const dsg_ctx *ctx) { return ctx->cfg.mg32_npre > 0 ? ctx->cfg.mg32_npre : ctx->s.npre; }
+inline int post32(const dsg_ctx *ctx) { return ctx->cfg.mg32_npost > 0 ? ctx->cfg.mg32_npost : ctx->s.npost; }
+
+// Levels of at most this many nodes may have their own sweep counts
+// (mg32_small_npre/npost): the levels the coarse tail runs by default.
+constexpr long long kSmallLevelNodes = 18LL * 18 * 18;
+
+inline bool small_level(const dsg_ctx *ctx, int l) {
+  return (long long)ctx->lnx[l] * ctx->lny[l] * ctx->lnz[l] <= kSmallLevelNodes;
+}
+
+// Sweeps on level l: the finest level, the one below it and the small levels
+// may have their own counts (a sweep on the finest level costs 8x and on the
+// next 2-3x one of the smaller levels, which are bound by launch latency or,
+// inside the coarse tail, by one SM's issue rate).
+inline int pre32(const dsg_ctx *ctx, int l) {
+  if (l == ctx->ng && ctx->cfg.mg32_fine_npre > 0) return ctx->cfg.mg32_fine_npre;
+  if (l == ctx->ng - 1 && ctx->cfg.mg32_mid_npre > 0) return ctx->cfg.mg32_mid_npre;
+  if (l < ctx->ng && small_level(ctx, l) && ctx->cfg.mg32_small_npre > 0) return ctx->cfg.mg32_small_npre;
+  return pre32(ctx);
+}
+inline int post32(const dsg_ctx *ctx, int l) {
+  if (l == ctx->ng && ctx->cfg.mg32_fine_npost > 0) return ctx->cfg.mg32_fine_npost;
+  if (l == ctx->ng - 1 && ctx->cfg.mg32_mid_npost > 0) return ctx->cfg.mg32_mid_npost;
+  if (l < ctx->ng && small_level(ctx, l) && ctx->cfg.mg32_small_npost > 0) return ctx->cfg.mg32_small_npost;
+  return post32(ctx);
+}
+
+// Prolongation of the FP32 V-cycles and FMG start: trilinear unless the
+// configuration asks for the reference's injection.
+inline int tri32(const dsg_ctx *ctx) { return ctx->cfg.mg32_prolong == 1 ? 0 : 1; }
+
+inline float level_h2(dsg_ctx *ctx, int l) {
+  const double h1 = ctx->s.lengthsize / (ctx->lnx[l] - 2);
+  return (float)(h1 * h1);
+}
+
+// Finest-level colour-split FP32 arrays: {even, odd} halves of U and RHS.
+struct FineSplit {
+  float *u[2];
+  float *r[2];
+};
+
+inline FineSplit fine_split(dsg_ctx *ctx) {
+  float **L = ctx->lv32[ctx->ng];
+  const dsg::Dims d = ctx->fine();
+  const size_t half = (size_t)((d.nx - 2) >> 1) * (d.ny - 2) * (d.nz - 2);
+  return FineSplit{{L[U32], L[U32] + half}, {L[RHS32], L[RHS32] + half}};
+}
+
+inline size_t fine_split_bytes(dsg_ctx *ctx) {
+  const dsg::Dims d = ctx->fine();
+  return 2 * (size_t)((d.nx - 2) >> 1) * (d.ny - 2) * (d.nz - 2) * sizeof(float);
+}
+
+inline void phase_coefs(dsg_ctx *ctx, float *r1, float *r2) {
+  *r1 = (float)(0.5 * (ctx->s.rho1 - ctx->s.rho2));
+  *r2 = (float)ctx->s.rho2;
+}
+
+// Arguments of the coarse-tail kernel for FP32 levels 1..top of ctx.
+inline void tail_args(dsg_ctx *ctx, int top, dsg::TailArgs *A) {
+  memset(A, 0, sizeof *A);
+  for (int l = 1; l <= top; l++) {
+    float **L = ctx->lv32[l];
+    A->lv[l] = TailLevel{L[U32],       L[RHS32],          L[A32],     L[B32],         L[C32],
+                              L[EI32],      ctx->level(l),     level_h2(ctx, l), pre32(ctx, l), post32(ctx, l)};
+  }
+  A->top = top;
+  A->ntop = ctx->s.ntop;
+  A->omega = omega32(ctx);
+  A->tri = tri32(ctx);
+}
+
+}  // namespace mixed
+
 int set_error(dsg_ctx *ctx, int code, const char *fmt, ...);
 int cuda_fail(dsg_ctx *ctx, cudaError_t e, const char *where);
+// A time step in two halves around its pressure solve (dsg.cu), and the
+// bookkeeping after a mixed-precision solve; the batched ensemble solve
+// (batch.cu) runs between the halves for all members at once.
+int step_pre_solve(dsg_ctx *ctx, int t);
+int step_post_solve(dsg_ctx *ctx, int t, dsg_mg_stats *ms, int mg_rc, dsg_mg_stats *stats);
+int solvelpres_pre(dsg_ctx *ctx);
+int solvelpres_post(dsg_ctx *ctx, int t, dsg_mg_stats *ms, int mg_rc, dsg_mg_stats *stats);
+int mixed_finish(dsg_ctx *ctx, dsg_mg_stats *s, dsg_mg_stats *stats);
+// batch.cu: the batched mixed-precision solve of ensemble members
+struct BatchSolve;
+int batch_eligible(const dsg_ctx *c, char *why, size_t nwhy);
+BatchSolve *batch_create(const std::vector<dsg_ctx *> &members, int *rc);
+void batch_destroy(BatchSolve *b);
+int batch_solve(BatchSolve *b, const std::vector<int> &active, std::vector<dsg_mg_stats> &stats,
+                std::vector<int> &mg_rc);
+int batch_autotune(BatchSolve *b, int reps, int *slots_tuned);
+long long batch_tail_nodes(const BatchSolve *b);
 // boundary conditions and derived fields after the state was loaded (the
 // restart branch of initialize, main.f:174-177), k-epsilon seeding included
 int restart_state(dsg_ctx *ctx);

@@ -16,6 +16,15 @@
 // Workers take members only between steps, so a failing member (its step
 // returns an error code) never leaves kernels of its own in flight while the
 // others continue; the ensemble step reports the first failing member.
+//
+// Batched mode (dsg_ensemble_set_batched): a step runs in three phases.  The
+// workers take every member up to its pressure solve; then the members'
+// pressure solves run as batched solves (batch.cu: one launch per multigrid
+// pass over all members of a group, under CUDA graphs), the cost-balanced
+// groups side by side on their own streams, one worker each; then the workers
+// finish every member's step.  Each member's results are bit for bit those of
+// its own step.  A member that fails before its solve ends the step with its
+// error, with the others stopped before their solves.
 #include <math.h>
 #include <string.h>
 
@@ -44,8 +53,18 @@ struct dsg_ensemble {
   bool stop = false;
   int t = 0;
   int workers = 0;
+  int phase = 0;  // what the workers run: 0 whole steps, 1 up to the solve, 2 the rest, 3 the batched solves
   double last_ms = 0.0;
+  double phase_ms[3] = {0.0, 0.0, 0.0};  // batched mode: host time of the three phases of the last step
   std::string err;
+  // batched mode: the members split into groups, each group's pressure solves
+  // one batched solve on its own stream
+  std::vector<dsg::BatchSolve *> batch;
+  std::vector<std::vector<int>> group;  // members of each group
+  std::vector<int> group_rc;            // status of each group's batched solve
+  std::vector<dsg_mg_stats> ms;         // per member: statistics and status of its solve
+  std::vector<int> mg_rc;
+  std::vector<int> reached;             // per member: 1 once its step reached the solve
 };
 
 namespace {
@@ -63,7 +82,7 @@ void worker_main(dsg_ensemble *e, int w, long long gen0) {
   long long seen = gen0;
   for (;;) {
     std::vector<int> mine;
-    int t;
+    int t, phase, workers;
     {
       std::unique_lock<std::mutex> lk(e->mu);
       e->go.wait(lk, [&] { return e->stop || e->gen != seen; });
@@ -71,17 +90,54 @@ void worker_main(dsg_ensemble *e, int w, long long gen0) {
       seen = e->gen;
       mine = e->plan[w];
       t = e->t;
+      phase = e->phase;
+      workers = e->workers;
+    }
+    if (phase == 3) {
+      // batched solves: worker w takes groups w, w + workers, ...
+      for (size_t g = (size_t)w; g < e->batch.size(); g += (size_t)workers) {
+        const std::vector<int> &mem = e->group[g];
+        std::vector<int> act(mem.size()), rc(mem.size());
+        std::vector<dsg_mg_stats> st(mem.size());
+        for (size_t q = 0; q < mem.size(); q++) act[q] = e->reached[mem[q]];
+        cudaError_t ce = cudaSetDevice(e->m[mem[0]]->device);
+        e->group_rc[g] = ce == cudaSuccess ? dsg::batch_solve(e->batch[g], act, st, rc)
+                                           : dsg::set_error(nullptr, DSG_E_CUDA, "cudaSetDevice");
+        if (e->group_rc[g]) e->m[mem[0]]->err = dsg_last_error(nullptr);
+        for (size_t q = 0; q < mem.size(); q++) {
+          e->ms[mem[q]] = st[q];
+          e->mg_rc[mem[q]] = rc[q];
+        }
+      }
+      mine.clear();
     }
     for (int i : mine) {
       dsg_ctx *c = e->m[i];
       const auto t0 = Clock::now();
       cudaError_t ce = cudaSetDevice(c->device);
-      e->rc[i] = ce == cudaSuccess ? dsg_step(c, t, &e->st[i]) : dsg::cuda_fail(c, ce, "cudaSetDevice");
-      e->member_ms[i] = std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
+      if (ce != cudaSuccess) {
+        e->rc[i] = dsg::cuda_fail(c, ce, "cudaSetDevice");
+      } else if (phase == 0) {
+        e->rc[i] = dsg_step(c, t, &e->st[i]);
+      } else if (phase == 1) {
+        e->rc[i] = dsg::step_pre_solve(c, t);
+        e->reached[i] = e->rc[i] == DSG_OK;
+      } else {
+        e->rc[i] = dsg::step_post_solve(c, t, &e->ms[i], e->mg_rc[i], &e->st[i]);
+      }
+      const double ms = std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
+      e->member_ms[i] = phase == 2 ? e->member_ms[i] + ms : ms;
     }
     std::lock_guard<std::mutex> lk(e->mu);
     if (--e->busy == 0) e->done.notify_all();
   }
+}
+
+void release_batches(dsg_ensemble *e) {
+  for (dsg::BatchSolve *b : e->batch) dsg::batch_destroy(b);
+  e->batch.clear();
+  e->group.clear();
+  e->group_rc.clear();
 }
 
 void stop_workers(dsg_ensemble *e) {
@@ -177,6 +233,7 @@ int dsg_ensemble_create(const dsg_config *cfgs, int n, int workers, dsg_ensemble
 void dsg_ensemble_destroy(dsg_ensemble *e) {
   if (!e) return;
   stop_workers(e);
+  release_batches(e);
   for (dsg_ctx *c : e->m) dsg_destroy(c);
   delete e;
 }
@@ -191,22 +248,57 @@ dsg_ctx *dsg_ensemble_member(dsg_ensemble *e, int i) {
 
 const char *dsg_ensemble_last_error(const dsg_ensemble *e) { return e ? e->err.c_str() : ""; }
 
-int dsg_ensemble_step(dsg_ensemble *e, int t, dsg_mg_stats *stats) {
-  if (!e || e->workers < 1) return dsg::set_error(nullptr, DSG_E_ARG, "ensemble without workers");
-  const auto t0 = Clock::now();
+namespace {
+
+// Run `phase` of step t through the worker pool.
+void run_phase(dsg_ensemble *e, int t, int phase) {
   {
     std::lock_guard<std::mutex> lk(e->mu);
     e->t = t;
+    e->phase = phase;
     e->busy = e->workers;
     e->gen++;
   }
   e->go.notify_all();
-  {
-    std::unique_lock<std::mutex> lk(e->mu);
-    e->done.wait(lk, [&] { return e->busy == 0; });
+  std::unique_lock<std::mutex> lk(e->mu);
+  e->done.wait(lk, [&] { return e->busy == 0; });
+}
+
+}  // namespace
+
+int dsg_ensemble_step(dsg_ensemble *e, int t, dsg_mg_stats *stats) {
+  if (!e || e->workers < 1) return dsg::set_error(nullptr, DSG_E_ARG, "ensemble without workers");
+  const auto t0 = Clock::now();
+  const int n = (int)e->m.size();
+  if (e->batch.empty()) {
+    run_phase(e, t, 0);
+  } else {
+    for (int i = 0; i < n; i++) e->reached[i] = 0;
+    run_phase(e, t, 1);
+    const auto t1 = Clock::now();
+    e->phase_ms[0] = std::chrono::duration<double, std::milli>(t1 - t0).count();
+    for (int i = 0; i < n; i++)
+      if (e->rc[i]) {
+        e->err = std::string("member ") + std::to_string(i) + ": " + e->m[i]->err;
+        return e->rc[i];
+      }
+    run_phase(e, t, 3);
+    for (size_t g = 0; g < e->batch.size(); g++)
+      if (e->group_rc[g]) {
+        e->err = std::string("batched solve: ") + e->m[e->group[g][0]]->err;
+        return e->group_rc[g];
+      }
+    for (int i = 0; i < n; i++)
+      if (e->mg_rc[i] && e->mg_rc[i] != DSG_E_NOT_CONVERGED) {
+        e->err = std::string("member ") + std::to_string(i) + ": " + e->m[i]->err;
+        return e->mg_rc[i];
+      }
+    const auto t2 = Clock::now();
+    e->phase_ms[1] = std::chrono::duration<double, std::milli>(t2 - t1).count();
+    run_phase(e, t, 2);
+    e->phase_ms[2] = std::chrono::duration<double, std::milli>(Clock::now() - t2).count();
   }
   e->last_ms = std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
-  const int n = (int)e->m.size();
   if (stats)
     for (int i = 0; i < n; i++) stats[i] = e->st[i];
   for (int i = 0; i < n; i++)
@@ -215,6 +307,77 @@ int dsg_ensemble_step(dsg_ensemble *e, int t, dsg_mg_stats *stats) {
       return e->rc[i];
     }
   e->err.clear();
+  return DSG_OK;
+}
+
+int dsg_ensemble_set_batched(dsg_ensemble *e, int groups) {
+  if (!e) return dsg::set_error(nullptr, DSG_E_ARG, "null ensemble");
+  const int n = (int)e->m.size();
+  if (groups <= 0) {
+    release_batches(e);
+    return DSG_OK;
+  }
+  if (groups > n) groups = n;
+  for (int i = 0; i < n; i++) {
+    char why[160];
+    if (dsg::batch_eligible(e->m[i], why, sizeof why))
+      return dsg::set_error(nullptr, DSG_E_ARG, "member %d cannot be batched: %s", i, why);
+  }
+  for (int i = 0; i < n; i++) {  // no member work in flight while the batches are set up
+    cudaError_t ce = cudaStreamSynchronize(e->m[i]->stream);
+    if (ce != cudaSuccess) return dsg::cuda_fail(e->m[i], ce, "dsg_ensemble_set_batched");
+  }
+  release_batches(e);
+  // groups balanced by cost, longest processing time first
+  std::vector<int> assign(n);
+  int rc = dsg_ensemble_plan(e->cost.data(), n, groups, assign.data());
+  if (rc) return rc;
+  e->group.assign(groups, {});
+  for (int i = 0; i < n; i++) e->group[assign[i]].push_back(i);
+  for (int g = 0; g < groups; g++) {
+    std::vector<dsg_ctx *> mem;
+    for (int i : e->group[g]) mem.push_back(e->m[i]);
+    dsg::BatchSolve *b = mem.empty() ? nullptr : dsg::batch_create(mem, &rc);
+    if (!b) {
+      release_batches(e);
+      return rc ? rc : DSG_E_ARG;
+    }
+    e->batch.push_back(b);
+  }
+  e->group_rc.assign(groups, 0);
+  e->ms.assign(n, dsg_mg_stats{});
+  e->mg_rc.assign(n, 0);
+  e->reached.assign(n, 0);
+  return DSG_OK;
+}
+
+int dsg_ensemble_batched(const dsg_ensemble *e) { return e ? (int)e->batch.size() : 0; }
+
+int64_t dsg_ensemble_batch_tail_nodes(const dsg_ensemble *e) {
+  return e && !e->batch.empty() ? dsg::batch_tail_nodes(e->batch[0]) : 0;
+}
+
+int dsg_ensemble_phase_ms(const dsg_ensemble *e, double *out) {
+  if (!e || !out) return DSG_E_ARG;
+  for (int q = 0; q < 3; q++) out[q] = e->phase_ms[q];
+  return DSG_OK;
+}
+
+int dsg_ensemble_autotune_tiles(dsg_ensemble *e, int reps, int *slots_tuned) {
+  if (!e || e->batch.empty()) return dsg::set_error(nullptr, DSG_E_STATE, "tile autotuning needs the batched mode");
+  if (reps < 1) return dsg::set_error(nullptr, DSG_E_ARG, "reps must be positive");
+  for (dsg_ctx *c : e->m) {
+    cudaError_t ce = cudaStreamSynchronize(c->stream);
+    if (ce != cudaSuccess) return dsg::cuda_fail(c, ce, "dsg_ensemble_autotune_tiles");
+  }
+  int total = 0;
+  for (dsg::BatchSolve *b : e->batch) {
+    int k = 0;
+    int rc = dsg::batch_autotune(b, reps, &k);
+    if (rc) return rc;
+    total += k;
+  }
+  if (slots_tuned) *slots_tuned = total;
   return DSG_OK;
 }
 

@@ -4,8 +4,13 @@
 full simulation with its fields resident in HBM, stepped by a pool of host
 threads on their own CUDA streams so that the members' kernels overlap on the
 GPU.  The autotuner measures each member's step time and picks the number of
-worker threads by timing real steps.  The reference runs one case per
-process; this is the batched study of droplet sizes and Weber numbers.
+worker threads by timing real steps.  In batched mode (``batched=groups``) the
+members' pressure solves run as batched solves -- one launch per multigrid
+pass over all members of a cost-balanced group, under CUDA graphs, the groups
+side by side -- and ``autotune_tiles`` picks the coarse-tail depth and the
+thread-block shape of every batched pass by timing.  The reference runs one
+case per process; this is the batched study of droplet sizes and Weber
+numbers.
 """
 import ctypes as C
 import math
@@ -36,7 +41,7 @@ def study_configs(count=64, sides=(48, 64, 96, 128, 160), we_range=(50.0, 800.0)
 class Ensemble:
     """n simulations stepped together; ``member(i)`` is a Solver view."""
 
-    def __init__(self, inputs, workers=0):
+    def __init__(self, inputs, workers=0, batched=0):
         self.lib = _lib.load()
         self.inputs = [x if isinstance(x, InputData) else InputData(**x) for x in inputs]
         n = len(self.inputs)
@@ -47,6 +52,38 @@ class Ensemble:
         self.n = n
         self.t = 0
         self._members = [Solver(self.inputs[i], ctx=self.lib.dsg_ensemble_member(h, i)) for i in range(n)]
+        if batched:
+            self.set_batched(int(batched))
+
+    def set_batched(self, groups=1):
+        """Solve the members' pressures as `groups` batched solves per step
+        (True = 1 group), each over a cost-balanced group of members on its
+        own stream, or each member on its own (0 / False)."""
+        self._ck(self.lib.dsg_ensemble_set_batched(self.h, int(groups)))
+
+    @property
+    def batched(self):
+        """Number of batched groups (0: per-member solves)."""
+        return int(self.lib.dsg_ensemble_batched(self.h))
+
+    @property
+    def batch_tail_nodes(self):
+        """Largest level (nodes) of the members' coarse tails in the batch."""
+        return int(self.lib.dsg_ensemble_batch_tail_nodes(self.h))
+
+    def autotune_tiles(self, reps=5):
+        """Pick the coarse-tail depth and the thread-block shape of every
+        batched pass by timing; returns the number of passes tuned."""
+        k = C.c_int()
+        self._ck(self.lib.dsg_ensemble_autotune_tiles(self.h, reps, C.byref(k)))
+        return k.value
+
+    def phase_ms(self):
+        """Batched mode: host time of the last step's phases (up to the
+        solves, the batched solves, after the solves), ms."""
+        out = np.zeros(3)
+        self._ck(self.lib.dsg_ensemble_phase_ms(self.h, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
 
     def close(self):
         if getattr(self, "h", None):

@@ -78,6 +78,11 @@ def parse():
     ap.add_argument("--ensemble", type=int, default=0,
                     help="time the droplet-study ensemble of this many members instead (48-160^3 grids)")
     ap.add_argument("--workers", type=int, default=0, help="ensemble host threads (0: autotune)")
+    ap.add_argument("--ensemble-mode", default="batched", choices=["batched", "members"],
+                    help="ensemble pressure solves: batched solves (a launch per multigrid pass over a group of "
+                         "members, CUDA graphs, autotuned tiles) or one solve per member")
+    ap.add_argument("--groups", type=int, default=0,
+                    help="batched ensemble: cost-balanced groups solved side by side (0: the fastest of 1, 2, 4, 8)")
     return ap.parse_args()
 
 
@@ -545,8 +550,25 @@ def run_ensemble(args):
     cfgs = dsg.ensemble.study_configs(args.ensemble, tol=args.tol)
     mine = dsg.ensemble.shard(cfgs, rank, ws)
     cells = sum((c.nx - 2) * (c.ny - 2) * (c.nz - 2) for c in cfgs)
+    batched = args.ensemble_mode == "batched"
     with dsg.Ensemble([cfgs[i] for i in mine], workers=max(args.workers, 1)) as e:
         tuned = e.autotune(steps_per_trial=2) if args.workers <= 0 else None
+        tiles, tail_nodes, groups, group_ms = 0, 0, 0, {}
+        if batched:
+            # group count: fixed, or the fastest of 1, 2, 4, 8 over two steps each
+            cands = [args.groups] if args.groups > 0 else [g for g in (1, 2, 4, 8) if g <= len(mine)]
+            for g in cands:
+                e.set_batched(g)
+                e.autotune_tiles(reps=3)
+                e.step()
+                t0 = time.perf_counter()
+                e.step()
+                e.step()
+                group_ms[g] = 1e3 * (time.perf_counter() - t0) / 2
+            groups = min(group_ms, key=group_ms.get)
+            e.set_batched(groups)
+            tiles = e.autotune_tiles(reps=3)
+            tail_nodes = e.batch_tail_nodes
         for _ in range(args.warmup):
             e.step()
 
@@ -584,6 +606,13 @@ def run_ensemble(args):
                                        "log-uniform, D = 2 mm, mixed-precision pressure to %.0e"
                                        % (args.ensemble, args.tol),
                            "cells_per_step": cells, "workers": workers, "autotuned": tuned is not None,
+                           "pressure_solve": ("batched solves: one launch per multigrid pass over each of %d "
+                                              "cost-balanced groups (solved side by side), CUDA graphs, %d pass "
+                                              "tile shapes autotuned, levels of at most %d nodes in each member's "
+                                              "single-block tail; step ms per group count %s"
+                                              % (groups, tiles, tail_nodes,
+                                                 {k: round(v, 1) for k, v in group_ms.items()})
+                                              if batched else "one solve per member"),
                            "members_rank0": len(mine),
                            "parallelism": "members sharded by cost over %d GPU(s)" % ws,
                            "timing": "host clock between synchronisations of all member streams"},

@@ -338,6 +338,34 @@ int dsg_ensemble_member_ms(const dsg_ensemble *e, double *out);
 int dsg_ensemble_autotune(dsg_ensemble *e, int t0, int steps_per_trial, int *t_next, int *best_workers);
 /* The plan alone: assign[i] = worker of member i for the given costs. */
 int dsg_ensemble_plan(const double *cost, int n, int workers, int *assign);
+/* Batched mode (groups >= 1): each ensemble step takes every member up to its
+ * pressure solve on the workers, then solves the members' pressures as
+ * `groups` batched mixed-precision solves -- the members split into
+ * cost-balanced groups; per group one launch per multigrid pass over all its
+ * members, the start and each outer iteration replayed as CUDA graphs on the
+ * group's own stream, converged members masked on the device; the groups
+ * solved side by side by the workers -- and finishes the steps on the
+ * workers.  Every member's results are bit for bit those of its own dsg_step.
+ * Needs every member in DSG_MODE_TOL_MIXED with the FP32 full-multigrid
+ * start, CUDA graphs and the coarse tail on, no network attached (DSG_E_ARG
+ * otherwise).  groups = 0 returns to per-member solves.  mglin
+ * main.f:3645-3763 per member.  dsg_ensemble_batched: the group count. */
+int dsg_ensemble_set_batched(dsg_ensemble *e, int groups);
+int dsg_ensemble_batched(const dsg_ensemble *e);
+/* Batched mode: host wall time (ms) of the last step's three phases: every
+ * member up to its solve, the batched solves, every member after its solve. */
+int dsg_ensemble_phase_ms(const dsg_ensemble *e, double *out);
+/* Autotuner of the batched solves: first the coarse-tail threshold (one
+ * batched V-cycle timed per candidate), then the thread-block shape of each
+ * sweep, restriction and prolongation launch of an outer iteration (reps
+ * timed launches per candidate shape, on the members' own FP32 arrays between
+ * steps), keeping the fastest; the results do not change (the cells of a
+ * pass are independent).  *slots_tuned = passes tuned over all groups. */
+int dsg_ensemble_autotune_tiles(dsg_ensemble *e, int reps, int *slots_tuned);
+/* Batched mode: levels of at most this many nodes run in each member's
+ * single-block coarse tail (picked by the autotuner; it does not change
+ * results); 0 if not batched. */
+int64_t dsg_ensemble_batch_tail_nodes(const dsg_ensemble *e);
 
 /* ---- allocation-free pressure solve -------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
