@@ -80,62 +80,61 @@ struct ASplit64 { float *ev, *od; const double *src; Dims d; Split sp; };
 struct ARestrSplit { float *uc; const float *re, *ro; Dims dc; Split sp; };
 struct ARestr { float *uc; const float *uf; Dims dc, df; };
 
-// Members per batch (the block bases of a launch are staged in shared memory).
-constexpr int kMaxBatch = 1024;
+// Members per batched solve: a launch's entry table travels as a kernel
+// parameter (at most 32 KB), so that the member lookup and the members'
+// arguments are read through the constant cache like a standalone kernel's.
+constexpr int kMaxBatch = 128;
 
-// A CTA stages the launch's block bases in shared memory, then walks the
-// virtual blocks blockIdx.x + i * gridDim.x (one each unless the launch is
-// very large).  The member of a virtual block comes from a binary search in
-// shared memory; consecutive virtual blocks of a CTA mostly belong to the same
-// member, whose block range and arguments stay in registers.  body(B, G, a)
-// runs one virtual block: B its index inside the member's grid G, a the
-// member's arguments.  Members whose gate is at most q, or whose sweep count
-// is at most `sweep`, sit the launch out.
+template <class A>
+struct Table {
+  unsigned total;  // virtual blocks of the launch
+  int n;           // entries
+  Entry<A> e[kMaxBatch];
+};
+
+// A CTA walks the virtual blocks blockIdx.x + i * gridDim.x (one each unless
+// the launch is very large).  The member of a virtual block comes from a
+// binary search over the entries' block bases; consecutive virtual blocks of
+// a CTA mostly belong to the same member.  body(B, G, a) runs one virtual
+// block: B its index inside the member's grid G, a the member's arguments.
+// Members whose gate is at most q, or whose sweep count is at most `sweep`,
+// sit the launch out.
 template <class A, class F>
-__device__ __forceinline__ void for_member_blocks(const Entry<A> *__restrict__ e, int n, unsigned total,
-                                                  const int *__restrict__ gate, int q, int sweep, F body) {
-  __shared__ unsigned s_base[kMaxBatch];
-  const int nt = blockDim.x * blockDim.y * blockDim.z;
-  const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
-  for (int i = tid; i < n; i += nt) s_base[i] = e[i].base;
-  __syncthreads();
+__device__ __forceinline__ void for_member_blocks(const Table<A> &t, const int *__restrict__ gate, int q, int sweep,
+                                                  F body) {
+  int l = 0;
   unsigned lo = 1, hi = 0;  // block range of the current member (none yet)
   bool run = false;
-  uint3 G = make_uint3(1, 1, 1);
-  A a;
-  for (unsigned vb = blockIdx.x; vb < total; vb += gridDim.x) {
+  for (unsigned vb = blockIdx.x; vb < t.total; vb += gridDim.x) {
     if (vb < lo || vb >= hi) {
-      int l = 0, h = n - 1;
-      while (l < h) {
-        const int mid = (l + h + 1) >> 1;
-        if (s_base[mid] <= vb) l = mid;
+      int a = 0, h = t.n - 1;
+      while (a < h) {
+        const int mid = (a + h + 1) >> 1;
+        if (t.e[mid].base <= vb) a = mid;
         else h = mid - 1;
       }
-      const Entry<A> &x = e[l];
-      lo = s_base[l];
-      hi = l + 1 < n ? s_base[l + 1] : total;
-      run = gate[x.member] > q && sweep < x.n;
-      G = make_uint3(x.gx, x.gy, x.gz);
-      if (run) a = x.a;
+      l = a;
+      lo = t.e[l].base;
+      hi = l + 1 < t.n ? t.e[l + 1].base : t.total;
+      run = gate[t.e[l].member] > q && sweep < t.e[l].n;
     }
     if (!run) continue;
+    const Entry<A> &x = t.e[l];
     const unsigned b = vb - lo;
-    body(make_uint3(b % G.x, (b / G.x) % G.y, b / (G.x * G.y)), G, a);
+    body(make_uint3(b % x.gx, (b / x.gx) % x.gy, b / (x.gx * x.gy)), make_uint3(x.gx, x.gy, x.gz), x.a);
   }
 }
 
 // CTAs of a batched launch of `total` virtual blocks of `threads`: one CTA per
-// virtual block up to 64 resident waves (measured faster than a few
-// persistent CTAs per SM walking many virtual blocks each).
+// virtual block up to 64 resident waves.
 unsigned launch_grid(unsigned total, unsigned threads) {
   const unsigned per_sm = threads >= 1024 ? 2u : 2048u / threads;
   const unsigned cap = 152u * per_sm * 64u;
   return total < cap ? total : cap;
 }
 
-#define BATCH_PARAMS(A) \
-  const Entry<A> *__restrict__ e, int n, unsigned total, const int *__restrict__ gate, int q, int sweep
-#define FOR_MEMBER_BLOCKS(A) for_member_blocks(e, n, total, gate, q, sweep, [&](uint3 B, uint3 G, const A &a)
+#define BATCH_PARAMS(A) const __grid_constant__ Table<A> t, const int *__restrict__ gate, int q, int sweep
+#define FOR_MEMBER_BLOCKS(A) for_member_blocks(t, gate, q, sweep, [&](uint3 B, uint3 G, const A &a)
 
 __global__ void kb_relax32_split(BATCH_PARAMS(ARelaxSplit), int colour) {
   FOR_MEMBER_BLOCKS(ARelaxSplit) {
@@ -171,7 +170,8 @@ __global__ void kb_prolong32(BATCH_PARAMS(APro)) {
 
 // One virtual block per member; TailArgs is large, so the block reads it in
 // place instead of copying it.
-__global__ void __launch_bounds__(kTailThreads, 1) kb_vtail32(BATCH_PARAMS(TailArgs)) {
+__global__ void __launch_bounds__(kTailThreads, 1) kb_vtail32(const Entry<TailArgs> *__restrict__ e, unsigned total,
+                                                                const int *__restrict__ gate, int q, int sweep) {
   for (unsigned vb = blockIdx.x; vb < total; vb += gridDim.x) {
     const Entry<TailArgs> &x = e[vb];
     if (gate[x.member] <= q || sweep >= x.n) continue;
@@ -226,6 +226,12 @@ __global__ void kb_restrict32(BATCH_PARAMS(ARestr)) {
 #undef FOR_MEMBER_BLOCKS
 #undef BATCH_PARAMS
 
+// Kernel parameters are limited to 32764 bytes.
+static_assert(sizeof(Table<ARelaxSplit>) <= 32000 && sizeof(Table<ARRSplit>) <= 32000 &&
+                  sizeof(Table<ADefect>) <= 32000 && sizeof(Table<AAcf64>) <= 32000 &&
+                  sizeof(Table<AAcf32>) <= 32000 && sizeof(Table<ACorrect>) <= 32000,
+              "batched entry table exceeds the kernel parameter space");
+
 // ---- host side ---------------------------------------------------------------
 
 enum Kind {
@@ -252,7 +258,8 @@ unsigned cdiv(size_t a, size_t b) { return (unsigned)((a + b - 1) / b); }
 // One batched launch of a plan.
 struct Launch {
   int kind;
-  size_t off;       // byte offset of its entry table in the device table buffer
+  std::vector<unsigned char> blob;  // the entry table (a kernel parameter)
+  size_t off;       // coarse tail: byte offset of its entry table in the device table buffer
   int n;            // entries
   unsigned blocks;  // total virtual blocks
   dim3 blk;
@@ -274,7 +281,7 @@ struct BatchSolve {
   cudaStream_t st = nullptr;
   cudaEvent_t ev_join = nullptr;
   std::vector<cudaEvent_t> ev_member;
-  std::vector<unsigned char> tab;  // host image of the entry tables
+  std::vector<unsigned char> tab;  // host image of the coarse-tail entry tables
   void *tab_dev = nullptr;
   size_t tab_cap = 0;
   int *gate_ones = nullptr, *gate_inner = nullptr;  // device
@@ -367,11 +374,18 @@ struct Planner {
   void emit(std::vector<Launch> &out, int kind, TableBuilder<A> &t, dim3 blk, int q, int sweep, int colour, int tri,
             int gate, int slot) {
     if (t.e.empty()) return;
-    const size_t align = 16;
-    const size_t off = (b.tab.size() + align - 1) / align * align;
-    b.tab.resize(off + t.e.size() * sizeof(Entry<A>));
-    memcpy(b.tab.data() + off, t.e.data(), t.e.size() * sizeof(Entry<A>));
-    out.push_back(Launch{kind, off, (int)t.e.size(), t.blocks, blk, q, sweep, colour, tri, gate, slot});
+    const size_t bytes = t.e.size() * sizeof(Entry<A>);
+    Launch L{kind, {}, 0, (int)t.e.size(), t.blocks, blk, q, sweep, colour, tri, gate, slot};
+    if (kind == K_TAIL) {
+      const size_t align = 16;
+      L.off = (b.tab.size() + align - 1) / align * align;
+      b.tab.resize(L.off + bytes);
+      memcpy(b.tab.data() + L.off, t.e.data(), bytes);
+    } else {
+      L.blob.resize(bytes);
+      memcpy(L.blob.data(), t.e.data(), bytes);
+    }
+    out.push_back(std::move(L));
   }
 
   // Split member levels lv into those on the finest level and the others.
@@ -686,41 +700,48 @@ struct Planner {
 };
 
 // Launch one batched pass.
-cudaError_t launch(const BatchSolve &b, const Launch &L, cudaStream_t st) {
-  const unsigned char *base = static_cast<const unsigned char *>(b.tab_dev) + L.off;
-  const int *gate = L.gate ? b.gate_inner : b.gate_ones;
+template <class A, class K, class... X>
+cudaError_t launch_table(K kernel, const Launch &L, const int *gate, cudaStream_t st, X... extra) {
+  Table<A> t;
+  t.total = L.blocks;
+  t.n = L.n;
+  memcpy(t.e, L.blob.data(), L.blob.size());
   const unsigned g = launch_grid(L.blocks, L.blk.x * L.blk.y * L.blk.z);
-#define LAUNCH(KERNEL, A, ...)                                                                                 \
-  DSG_COUNT KERNEL<<<g, L.blk, 0, st>>>(reinterpret_cast<const Entry<A> *>(base), L.n, L.blocks, gate, L.q, L.sweep, \
-                                        ##__VA_ARGS__)
+  DSG_COUNT kernel<<<g, L.blk, 0, st>>>(t, gate, L.q, L.sweep, extra...);
+  return cudaGetLastError();
+}
+
+cudaError_t launch(const BatchSolve &b, const Launch &L, cudaStream_t st) {
+  const int *gate = L.gate ? b.gate_inner : b.gate_ones;
   switch (L.kind) {
-    case K_RELAX_SPLIT: LAUNCH(kb_relax32_split, ARelaxSplit, L.colour); break;
-    case K_RELAX: LAUNCH(kb_relax32, ARelax, L.colour); break;
-    case K_RR_SPLIT: LAUNCH(kb_resid_restrict32_split, ARRSplit); break;
-    case K_RR: LAUNCH(kb_resid_restrict32, ARR); break;
+    case K_RELAX_SPLIT: return launch_table<ARelaxSplit>(kb_relax32_split, L, gate, st, L.colour);
+    case K_RELAX: return launch_table<ARelax>(kb_relax32, L, gate, st, L.colour);
+    case K_RR_SPLIT: return launch_table<ARRSplit>(kb_resid_restrict32_split, L, gate, st);
+    case K_RR: return launch_table<ARR>(kb_resid_restrict32, L, gate, st);
     case K_PRO_SPLIT:
-      if (L.tri) LAUNCH(kb_prolong32_split<true>, AProSplit);
-      else LAUNCH(kb_prolong32_split<false>, AProSplit);
-      break;
+      return L.tri ? launch_table<AProSplit>(kb_prolong32_split<true>, L, gate, st)
+                   : launch_table<AProSplit>(kb_prolong32_split<false>, L, gate, st);
     case K_PRO:
-      if (L.tri) LAUNCH(kb_prolong32<true>, APro);
-      else LAUNCH(kb_prolong32<false>, APro);
-      break;
-    case K_TAIL: LAUNCH(kb_vtail32, TailArgs); break;
-    case K_CORRECT: LAUNCH(kb_correct64, ACorrect); break;
-    case K_DEFECT: LAUNCH(kb_defect64, ADefect); break;
-    case K_FOLD: LAUNCH(kb_fold2, AFold); break;
-    case K_ZERO: LAUNCH(kb_zero32, AZero); break;
-    case K_TO32: LAUNCH(kb_to32, ATo32); break;
-    case K_ACF64: LAUNCH(kb_acfromac64to32, AAcf64); break;
-    case K_ACF32: LAUNCH(kb_acfromac32, AAcf32); break;
-    case K_SPLIT64: LAUNCH(kb_split_from64, ASplit64); break;
-    case K_RESTR_SPLIT: LAUNCH(kb_restrict32_split, ARestrSplit); break;
-    case K_RESTR: LAUNCH(kb_restrict32, ARestr); break;
+      return L.tri ? launch_table<APro>(kb_prolong32<true>, L, gate, st)
+                   : launch_table<APro>(kb_prolong32<false>, L, gate, st);
+    case K_TAIL: {
+      const Entry<TailArgs> *e =
+          reinterpret_cast<const Entry<TailArgs> *>(static_cast<const unsigned char *>(b.tab_dev) + L.off);
+      DSG_COUNT kb_vtail32<<<L.blocks, L.blk, 0, st>>>(e, L.blocks, gate, L.q, L.sweep);
+      return cudaGetLastError();
+    }
+    case K_CORRECT: return launch_table<ACorrect>(kb_correct64, L, gate, st);
+    case K_DEFECT: return launch_table<ADefect>(kb_defect64, L, gate, st);
+    case K_FOLD: return launch_table<AFold>(kb_fold2, L, gate, st);
+    case K_ZERO: return launch_table<AZero>(kb_zero32, L, gate, st);
+    case K_TO32: return launch_table<ATo32>(kb_to32, L, gate, st);
+    case K_ACF64: return launch_table<AAcf64>(kb_acfromac64to32, L, gate, st);
+    case K_ACF32: return launch_table<AAcf32>(kb_acfromac32, L, gate, st);
+    case K_SPLIT64: return launch_table<ASplit64>(kb_split_from64, L, gate, st);
+    case K_RESTR_SPLIT: return launch_table<ARestrSplit>(kb_restrict32_split, L, gate, st);
+    case K_RESTR: return launch_table<ARestr>(kb_restrict32, L, gate, st);
     default: return cudaErrorInvalidValue;
   }
-#undef LAUNCH
-  return cudaGetLastError();
 }
 
 void release_graphs(BatchSolve &b) {
@@ -812,8 +833,8 @@ int run_graph(BatchSolve &b, cudaGraphExec_t g, long long kernels) {
 
 // Time `reps` rounds of one FP32 V-cycle of every member under the current
 // tail threshold (direct launches of the probe plan; FP32 scratch only).  The
-// probe's tables go to the start of the table buffer; the plans' tables
-// there are uploaded again by build_plans before any graph runs.
+// probe's coarse-tail table goes to the start of the table buffer; the
+// plans' tables there are uploaded again by build_plans before any graph runs.
 int time_probe(BatchSolve *b, int reps, float *ms) {
   std::vector<Launch> probe;
   std::vector<unsigned char> saved;
@@ -824,7 +845,8 @@ int time_probe(BatchSolve *b, int reps, float *ms) {
   ptab.swap(b->tab);
   b->tab.swap(saved);
   if (ptab.size() > b->tab_cap) return set_error(nullptr, DSG_E_STATE, "autotune: probe tables exceed the table buffer");
-  cudaError_t e = cudaMemcpyAsync(b->tab_dev, ptab.data(), ptab.size(), cudaMemcpyHostToDevice, b->st);
+  cudaError_t e = ptab.empty() ? cudaSuccess
+                               : cudaMemcpyAsync(b->tab_dev, ptab.data(), ptab.size(), cudaMemcpyHostToDevice, b->st);
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (e == cudaSuccess) e = cudaEventCreate(&e0);
   if (e == cudaSuccess) e = cudaEventCreate(&e1);
@@ -1069,7 +1091,6 @@ int batch_autotune(BatchSolve *b, int reps, int *slots_tuned) {
   if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
   if (e != cudaSuccess) return set_error(nullptr, DSG_E_CUDA, "autotune: %s", cudaGetErrorString(e));
   const std::vector<Launch> plan = b->iter[1];
-  const std::vector<unsigned char> tab_save = b->tab;
   std::vector<int> seen(b->slot_keys.size(), 0);
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   e = cudaEventCreate(&e0);
@@ -1094,7 +1115,7 @@ int batch_autotune(BatchSolve *b, int reps, int *slots_tuned) {
       const dim3 blk = kShapes[c];
       Launch L = L0;
       L.blk = blk;
-      std::vector<unsigned char> tab(tab_save.begin() + L.off, tab_save.begin() + L.off + L.n * esz);
+      std::vector<unsigned char> &tab = L.blob;
       unsigned blocks = 0;
       for (int q = 0; q < L.n; q++) {
         unsigned char *p = tab.data() + q * esz;
@@ -1117,9 +1138,7 @@ int batch_autotune(BatchSolve *b, int reps, int *slots_tuned) {
         blocks += g.x * g.y * g.z;
       }
       L.blocks = blocks;
-      e = cudaMemcpyAsync(static_cast<unsigned char *>(b->tab_dev) + L.off, tab.data(), tab.size(),
-                          cudaMemcpyHostToDevice, b->st);
-      if (e == cudaSuccess) e = launch(*b, L, b->st);  // warm-up
+      e = launch(*b, L, b->st);  // warm-up
       if (e == cudaSuccess) e = cudaEventRecord(e0, b->st);
       for (int r = 0; r < reps && e == cudaSuccess; r++) e = launch(*b, L, b->st);
       if (e == cudaSuccess) e = cudaEventRecord(e1, b->st);

@@ -17,14 +17,15 @@
 // returns an error code) never leaves kernels of its own in flight while the
 // others continue; the ensemble step reports the first failing member.
 //
-// Batched mode (dsg_ensemble_set_batched): a step runs in three phases.  The
-// workers take every member up to its pressure solve; then the members'
-// pressure solves run as batched solves (batch.cu: one launch per multigrid
-// pass over all members of a group, under CUDA graphs), the cost-balanced
-// groups side by side on their own streams, one worker each; then the workers
-// finish every member's step.  Each member's results are bit for bit those of
-// its own step.  A member that fails before its solve ends the step with its
-// error, with the others stopped before their solves.
+// Batched mode (dsg_ensemble_set_batched): the members form cost-balanced
+// groups, and a worker steps whole groups: every member of the group up to
+// its pressure solve, the group's pressure solves as one batched solve
+// (batch.cu: one launch per multigrid pass over all members of the group,
+// under CUDA graphs, on the group's own stream), then every member after its
+// solve.  The groups of different workers overlap on the GPU.  Each member's
+// results are bit for bit those of its own step.  A member that fails before
+// its solve stops the other members of its group before their solves; the
+// step reports the first failing member.
 #include <math.h>
 #include <string.h>
 
@@ -53,9 +54,9 @@ struct dsg_ensemble {
   bool stop = false;
   int t = 0;
   int workers = 0;
-  int phase = 0;  // what the workers run: 0 whole steps, 1 up to the solve, 2 the rest, 3 the batched solves
+  int phase = 0;  // what the workers run: 0 whole member steps, 3 whole group steps (batched mode)
   double last_ms = 0.0;
-  double phase_ms[3] = {0.0, 0.0, 0.0};  // batched mode: host time of the three phases of the last step
+  double phase_ms[3] = {0.0, 0.0, 0.0};  // batched mode: worker time of the last step's phases, summed
   std::string err;
   // batched mode: the members split into groups, each group's pressure solves
   // one batched solve on its own stream
@@ -94,20 +95,54 @@ void worker_main(dsg_ensemble *e, int w, long long gen0) {
       workers = e->workers;
     }
     if (phase == 3) {
-      // batched solves: worker w takes groups w, w + workers, ...
+      // batched mode: worker w takes groups w, w + workers, ... through the
+      // whole step (its members up to their solves, the group's batched
+      // solve, its members after their solves), so the groups of different
+      // workers overlap on the GPU like single members do
+      double pm[3] = {0.0, 0.0, 0.0};
       for (size_t g = (size_t)w; g < e->batch.size(); g += (size_t)workers) {
         const std::vector<int> &mem = e->group[g];
-        std::vector<int> act(mem.size()), rc(mem.size());
-        std::vector<dsg_mg_stats> st(mem.size());
-        for (size_t q = 0; q < mem.size(); q++) act[q] = e->reached[mem[q]];
-        cudaError_t ce = cudaSetDevice(e->m[mem[0]]->device);
-        e->group_rc[g] = ce == cudaSuccess ? dsg::batch_solve(e->batch[g], act, st, rc)
-                                           : dsg::set_error(nullptr, DSG_E_CUDA, "cudaSetDevice");
-        if (e->group_rc[g]) e->m[mem[0]]->err = dsg_last_error(nullptr);
-        for (size_t q = 0; q < mem.size(); q++) {
-          e->ms[mem[q]] = st[q];
-          e->mg_rc[mem[q]] = rc[q];
+        const auto t0 = Clock::now();
+        bool all = true;
+        for (int i : mem) {
+          dsg_ctx *c = e->m[i];
+          cudaError_t ce = cudaSetDevice(c->device);
+          e->rc[i] = ce == cudaSuccess ? dsg::step_pre_solve(c, t) : dsg::cuda_fail(c, ce, "cudaSetDevice");
+          e->reached[i] = e->rc[i] == DSG_OK;
+          all = all && e->reached[i];
         }
+        const auto t1 = Clock::now();
+        e->group_rc[g] = DSG_OK;
+        if (all) {
+          std::vector<int> act(mem.size(), 1), rc(mem.size());
+          std::vector<dsg_mg_stats> st(mem.size());
+          e->group_rc[g] = dsg::batch_solve(e->batch[g], act, st, rc);
+          if (e->group_rc[g]) e->m[mem[0]]->err = dsg_last_error(nullptr);
+          for (size_t q = 0; q < mem.size(); q++) {
+            e->ms[mem[q]] = st[q];
+            e->mg_rc[mem[q]] = rc[q];
+          }
+        }
+        const auto t2 = Clock::now();
+        if (all && !e->group_rc[g])
+          for (int i : mem) {
+            const int mrc = e->mg_rc[i];
+            if (mrc && mrc != DSG_E_NOT_CONVERGED) {
+              e->rc[i] = mrc;
+              continue;
+            }
+            e->rc[i] = dsg::step_post_solve(e->m[i], t, &e->ms[i], mrc, &e->st[i]);
+          }
+        const auto t3 = Clock::now();
+        pm[0] += std::chrono::duration<double, std::milli>(t1 - t0).count();
+        pm[1] += std::chrono::duration<double, std::milli>(t2 - t1).count();
+        pm[2] += std::chrono::duration<double, std::milli>(t3 - t2).count();
+        const double per = std::chrono::duration<double, std::milli>(t3 - t0).count() / (double)mem.size();
+        for (int i : mem) e->member_ms[i] = per;
+      }
+      {
+        std::lock_guard<std::mutex> lk(e->mu);
+        for (int q = 0; q < 3; q++) e->phase_ms[q] += pm[q];
       }
       mine.clear();
     }
@@ -117,16 +152,10 @@ void worker_main(dsg_ensemble *e, int w, long long gen0) {
       cudaError_t ce = cudaSetDevice(c->device);
       if (ce != cudaSuccess) {
         e->rc[i] = dsg::cuda_fail(c, ce, "cudaSetDevice");
-      } else if (phase == 0) {
-        e->rc[i] = dsg_step(c, t, &e->st[i]);
-      } else if (phase == 1) {
-        e->rc[i] = dsg::step_pre_solve(c, t);
-        e->reached[i] = e->rc[i] == DSG_OK;
       } else {
-        e->rc[i] = dsg::step_post_solve(c, t, &e->ms[i], e->mg_rc[i], &e->st[i]);
+        e->rc[i] = dsg_step(c, t, &e->st[i]);
       }
-      const double ms = std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
-      e->member_ms[i] = phase == 2 ? e->member_ms[i] + ms : ms;
+      e->member_ms[i] = std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
     }
     std::lock_guard<std::mutex> lk(e->mu);
     if (--e->busy == 0) e->done.notify_all();
@@ -273,30 +302,13 @@ int dsg_ensemble_step(dsg_ensemble *e, int t, dsg_mg_stats *stats) {
   if (e->batch.empty()) {
     run_phase(e, t, 0);
   } else {
-    for (int i = 0; i < n; i++) e->reached[i] = 0;
-    run_phase(e, t, 1);
-    const auto t1 = Clock::now();
-    e->phase_ms[0] = std::chrono::duration<double, std::milli>(t1 - t0).count();
-    for (int i = 0; i < n; i++)
-      if (e->rc[i]) {
-        e->err = std::string("member ") + std::to_string(i) + ": " + e->m[i]->err;
-        return e->rc[i];
-      }
+    for (int q = 0; q < 3; q++) e->phase_ms[q] = 0.0;
     run_phase(e, t, 3);
     for (size_t g = 0; g < e->batch.size(); g++)
       if (e->group_rc[g]) {
         e->err = std::string("batched solve: ") + e->m[e->group[g][0]]->err;
         return e->group_rc[g];
       }
-    for (int i = 0; i < n; i++)
-      if (e->mg_rc[i] && e->mg_rc[i] != DSG_E_NOT_CONVERGED) {
-        e->err = std::string("member ") + std::to_string(i) + ": " + e->m[i]->err;
-        return e->mg_rc[i];
-      }
-    const auto t2 = Clock::now();
-    e->phase_ms[1] = std::chrono::duration<double, std::milli>(t2 - t1).count();
-    run_phase(e, t, 2);
-    e->phase_ms[2] = std::chrono::duration<double, std::milli>(Clock::now() - t2).count();
   }
   e->last_ms = std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
   if (stats)

@@ -78,9 +78,9 @@ def parse():
     ap.add_argument("--ensemble", type=int, default=0,
                     help="time the droplet-study ensemble of this many members instead (48-160^3 grids)")
     ap.add_argument("--workers", type=int, default=0, help="ensemble host threads (0: autotune)")
-    ap.add_argument("--ensemble-mode", default="batched", choices=["batched", "members"],
-                    help="ensemble pressure solves: batched solves (a launch per multigrid pass over a group of "
-                         "members, CUDA graphs, autotuned tiles) or one solve per member")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="ensemble: skip the batched-solve point (a launch per multigrid pass over a group of "
+                         "members, CUDA graphs, autotuned tiles)")
     ap.add_argument("--groups", type=int, default=0,
                     help="batched ensemble: cost-balanced groups solved side by side (0: the fastest of 1, 2, 4, 8)")
     return ap.parse_args()
@@ -550,25 +550,8 @@ def run_ensemble(args):
     cfgs = dsg.ensemble.study_configs(args.ensemble, tol=args.tol)
     mine = dsg.ensemble.shard(cfgs, rank, ws)
     cells = sum((c.nx - 2) * (c.ny - 2) * (c.nz - 2) for c in cfgs)
-    batched = args.ensemble_mode == "batched"
     with dsg.Ensemble([cfgs[i] for i in mine], workers=max(args.workers, 1)) as e:
         tuned = e.autotune(steps_per_trial=2) if args.workers <= 0 else None
-        tiles, tail_nodes, groups, group_ms = 0, 0, 0, {}
-        if batched:
-            # group count: fixed, or the fastest of 1, 2, 4, 8 over two steps each
-            cands = [args.groups] if args.groups > 0 else [g for g in (1, 2, 4, 8) if g <= len(mine)]
-            for g in cands:
-                e.set_batched(g)
-                e.autotune_tiles(reps=3)
-                e.step()
-                t0 = time.perf_counter()
-                e.step()
-                e.step()
-                group_ms[g] = 1e3 * (time.perf_counter() - t0) / 2
-            groups = min(group_ms, key=group_ms.get)
-            e.set_batched(groups)
-            tiles = e.autotune_tiles(reps=3)
-            tail_nodes = e.batch_tail_nodes
         for _ in range(args.warmup):
             e.step()
 
@@ -592,8 +575,33 @@ def run_ensemble(args):
         el, launches, stats = timed(args.steps)
         clk = clocks.stop()
         workers = e.workers
+        # the batched pressure solve, same members and workers, after the
+        # timed steps: group count tried over 1, 2, 4, 8 and 16 (or fixed),
+        # coarse-tail depth and tile shapes autotuned, then timed the same way
+        batched = None
+        if not args.no_batched:
+            cands = [args.groups] if args.groups > 0 else [g for g in (1, 2, 4, 8, 16) if g <= len(mine)]
+            group_ms = {}
+            for g in cands:
+                e.set_batched(g)
+                e.autotune_tiles(reps=3)
+                e.step()
+                t0 = time.perf_counter()
+                e.step()
+                e.step()
+                group_ms[g] = 1e3 * (time.perf_counter() - t0) / 2
+            groups = min(group_ms, key=group_ms.get)
+            e.set_batched(groups)
+            tiles = e.autotune_tiles(reps=3)
+            e.step()
+            bel, blaunch, _ = timed(args.steps)
+            batched = {"el": bel, "groups": groups, "tiles": tiles, "tail_nodes": e.batch_tail_nodes,
+                       "launches": blaunch, "group_ms": {k: round(v, 1) for k, v in group_ms.items()}}
+            e.set_batched(0)
         e.set_workers(1)
         el1, _, _ = timed(1)
+    if batched:
+        batched["el"] = max_over_ranks(batched["el"], dist, "cuda")
     el = max_over_ranks(el, dist, "cuda")
     el1 = max_over_ranks(el1, dist, "cuda")
     value = args.ensemble * args.steps / el
@@ -606,19 +614,22 @@ def run_ensemble(args):
                                        "log-uniform, D = 2 mm, mixed-precision pressure to %.0e"
                                        % (args.ensemble, args.tol),
                            "cells_per_step": cells, "workers": workers, "autotuned": tuned is not None,
-                           "pressure_solve": ("batched solves: one launch per multigrid pass over each of %d "
-                                              "cost-balanced groups (solved side by side), CUDA graphs, %d pass "
-                                              "tile shapes autotuned, levels of at most %d nodes in each member's "
-                                              "single-block tail; step ms per group count %s"
-                                              % (groups, tiles, tail_nodes,
-                                                 {k: round(v, 1) for k, v in group_ms.items()})
-                                              if batched else "one solve per member"),
+                           "pressure_solve": "one mixed-precision solve per member (CUDA graphs per member)",
                            "members_rank0": len(mine),
                            "parallelism": "members sharded by cost over %d GPU(s)" % ws,
                            "timing": "host clock between synchronisations of all member streams"},
                 "one_worker_value": args.ensemble / el1,
                 "vcycles_mean": float(sum(s["vcycles"] for st in stats for s in st) / max(1, len(stats) * e.n)),
                 "gpu_launches": launches, "clocks": clk}
+        if batched:
+            line["batched"] = {
+                "value": args.ensemble * args.steps / batched["el"], "unit": "member-steps/s",
+                "ms_per_step": 1e3 * batched["el"] / args.steps,
+                "solve": ("batched pressure solves: one launch per multigrid pass over each of %d cost-balanced "
+                          "groups (each worker steps whole groups), CUDA graphs, %d pass tile shapes autotuned, "
+                          "levels of at most %d nodes in each member's single-block tail"
+                          % (batched["groups"], batched["tiles"], batched["tail_nodes"])),
+                "step_ms_per_group_count": batched["group_ms"], "gpu_launches": batched["launches"]}
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

@@ -338,22 +338,24 @@ int dsg_ensemble_member_ms(const dsg_ensemble *e, double *out);
 int dsg_ensemble_autotune(dsg_ensemble *e, int t0, int steps_per_trial, int *t_next, int *best_workers);
 /* The plan alone: assign[i] = worker of member i for the given costs. */
 int dsg_ensemble_plan(const double *cost, int n, int workers, int *assign);
-/* Batched mode (groups >= 1): each ensemble step takes every member up to its
- * pressure solve on the workers, then solves the members' pressures as
- * `groups` batched mixed-precision solves -- the members split into
- * cost-balanced groups; per group one launch per multigrid pass over all its
+/* Batched mode (groups >= 1): the members split into `groups` cost-balanced
+ * groups and each worker steps whole groups: every member of the group up to
+ * its pressure solve, the group's pressure solves as one batched
+ * mixed-precision solve -- one launch per multigrid pass over all its
  * members, the start and each outer iteration replayed as CUDA graphs on the
- * group's own stream, converged members masked on the device; the groups
- * solved side by side by the workers -- and finishes the steps on the
- * workers.  Every member's results are bit for bit those of its own dsg_step.
+ * group's own stream, converged members masked on the device -- then every
+ * member after its solve; the groups of different workers overlap on the
+ * GPU.  Every member's results are bit for bit those of its own dsg_step.
  * Needs every member in DSG_MODE_TOL_MIXED with the FP32 full-multigrid
  * start, CUDA graphs and the coarse tail on, no network attached (DSG_E_ARG
- * otherwise).  groups = 0 returns to per-member solves.  mglin
+ * otherwise), and at most 128 members per group.  groups = 0 returns to
+ * per-member solves.  mglin
  * main.f:3645-3763 per member.  dsg_ensemble_batched: the group count. */
 int dsg_ensemble_set_batched(dsg_ensemble *e, int groups);
 int dsg_ensemble_batched(const dsg_ensemble *e);
-/* Batched mode: host wall time (ms) of the last step's three phases: every
- * member up to its solve, the batched solves, every member after its solve. */
+/* Batched mode: worker time (ms) of the last step's three phases, summed over
+ * the workers: members up to their solves, the batched solves, members after
+ * their solves. */
 int dsg_ensemble_phase_ms(const dsg_ensemble *e, double *out);
 /* Autotuner of the batched solves: first the coarse-tail threshold (one
  * batched V-cycle timed per candidate), then the thread-block shape of each
