@@ -10,12 +10,15 @@
 //   D3 conv 64->32 + ReLU  on up(E4) + E3
 //   D2 conv 32->16 + ReLU  on up(D3) + E2
 //   D1 conv 16->1          on up(D2) + E1  (linear output, channel padded to 8)
-// All convolutions are 3x3x3, zero padded.  They run as implicit GEMMs on the
-// tensor cores with mma.sync m16n8k16 (BF16 inputs, FP32 accumulation):
-// M = voxels (16 per warp), N = output channels, K = 27 taps x input channels.
-// The backward pass uses the same kernel for the data gradient (flipped,
-// transposed weights) and a second implicit GEMM for the weight gradient
-// (M = input channels, N = output channels, K = voxels).
+// All convolutions are 3x3x3, zero padded, implicit GEMMs on the tensor cores
+// with BF16 inputs and FP32 accumulation.  Forward and data gradient run on
+// Blackwell's tcgen05 MMA (k_conv3_tc): M = 128 voxels (an 8 x 16 x 1 tile),
+// N = output channels, K = 27 taps x input channels; the input halo arrives
+// by TMA, the weights stay in shared memory, the accumulator lives in tensor
+// memory.  The data gradient uses flipped, transposed weights.  The weight
+// gradient is a second implicit GEMM (M = input channels, N = output channels,
+// K = voxels) on mma.sync m16n8k16.
+#include <cuda.h>
 #include <cuda_bf16.h>
 
 #include <math.h>
@@ -24,6 +27,7 @@
 #include <vector>
 
 #include "dsg_internal.cuh"
+#include "tc05.cuh"
 
 namespace dsg {
 namespace nn {
@@ -89,89 +93,212 @@ __device__ __forceinline__ void mma_bf16(float (&c)[4], unsigned a0, unsigned a1
       : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
 }
 
-// ---- convolution forward / data gradient (implicit GEMM) -----------------------
-// X: [D][H][W][CIN] bf16, Wp: packed B fragments [27][CIN/16][COUT/8][32 lanes] x uint2,
-// Y: [D][H][W][COUT] (bf16, or float when OUTF).  CTA = 8 warps, tile 16 (x) x 8 (y)
-// x 1 (z) voxels; warp w computes the 16 voxels of row y0+w for all COUT.
-// Tap t = (dz+1)*9 + (dy+1)*3 + (dx+1) reads X at (x+dx, y+dy, z+dz).
+// Tile geometry of the mma.sync weight-gradient kernel below.
 constexpr int CTX = 16, CTY = 8;
 
-template <int CIN, int COUT, bool RELU, bool OUTF>
-__global__ void __launch_bounds__(256) k_conv3(const bf16 *__restrict__ X, const uint2 *__restrict__ Wp,
-                                               const float *__restrict__ bias, void *__restrict__ Yv, int W, int H,
-                                               int D) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  bf16 *tile = reinterpret_cast<bf16 *>(smem);  // [3][CTY+2][CTX+2][CIN]
-  constexpr int HX = CTX + 2, HY = CTY + 2;
-  const int x0 = blockIdx.x * CTX, y0 = blockIdx.y * CTY, z = blockIdx.z;
+// ---- convolution forward / data gradient on tcgen05 ------------------------------
+// X: [D][H][W][CIN] bf16 (read through the TMA map xmap), Wt: packed weights
+// [27][CIN/8][NT][8] bf16 (tap, 8-channel input block, output channel, 8
+// inputs), the CTA uses output channels co0 .. co0+N-1; Y: [D][H][W][ystride]
+// (bf16, or float when OUTF, of which channels co0 .. co0+ywrite-1 are
+// written).  A CTA walks voxel tiles of 8 (x) x 16 (y) x 1 (z) = the 128 rows
+// of one MMA.  Per tile: TMA loads the 10 x 18 x 3 halo as CIN/8 slabs of 8
+// channels, which is the no-swizzle K-major core-matrix layout (8 voxels along
+// x x 16 bytes per core matrix, the next tile row 160 bytes on, the next 8
+// channels one slab on); one thread issues 27 x CIN/16 MMAs (M=128, N, K=16)
+// into a TMEM accumulator, each tap a shifted window of the same halo; the
+// four warps read their 32 TMEM lanes (= voxels) back, add the bias, apply
+// the ReLU and store.  With two halo stages the TMA of the next tile overlaps
+// the MMAs and epilogue of the current one; two TMEM accumulators alternate.
+// Every wait is bounded: on a timeout the CTA records it in *err, waits (again
+// bounded) for its copies and MMAs in flight, frees its TMEM and returns.
+namespace tc {
+constexpr int TX = 8, TY = 16, HX = TX + 2, HY = TY + 2, HZ = 3;
+constexpr uint32_t SLAB = 8704;        // 3 x 18 x 10 voxels x 16 bytes = 8640, padded to 128 bytes
+constexpr uint32_t SLAB_BYTES = 8640;  // bytes a slab's TMA box delivers
+constexpr uint32_t SBO_A = HX * 16;    // next tile row: 8 more M rows
+constexpr int THREADS = 128;
+constexpr uint32_t kWaitPolls = 1u << 26;
+
+__host__ __device__ constexpr int acc_cols(int n) { return n < 32 ? 32 : n; }
+__host__ __device__ constexpr int tmem_cols(int n) { return 2 * acc_cols(n) <= 64 ? 64 : 2 * acc_cols(n); }
+template <int CIN, int N, int STAGES>
+__host__ __device__ constexpr size_t smem_bytes() {
+  return 1024 + (size_t)STAGES * (CIN / 8) * SLAB + (size_t)27 * CIN * N * 2 + 128;
+}
+}  // namespace tc
+
+template <int CIN, int N, int STAGES, bool RELU, bool OUTF>
+__global__ void __launch_bounds__(tc::THREADS) k_conv3_tc(const __grid_constant__ CUtensorMap xmap,
+                                                          const bf16 *__restrict__ Wt, int NT, int co0,
+                                                          const float *__restrict__ bias, int nbias,
+                                                          void *__restrict__ Yv, int ystride, int ywrite, int W,
+                                                          int H, int D, int *__restrict__ err) {
+  using namespace tc;
+  using namespace dsg::tc05;
+  static_assert(N % 16 == 0 && N <= 256 && CIN % 16 == 0, "MMA shape");
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *sm = reinterpret_cast<unsigned char *>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  unsigned char *halo = sm;
+  unsigned char *wts = sm + (size_t)STAGES * (CIN / 8) * SLAB;
+  uint64_t *bar_load = reinterpret_cast<uint64_t *>(wts + (size_t)27 * CIN * N * 2);  // [2]
+  uint64_t *bar_mma = bar_load + 2;                                                   // [2]
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(bar_mma + 2);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  // cooperative halo load, 16-byte vectors of 8 channels
-  constexpr int VPV = CIN / 8;  // vectors per voxel
-  const int nvec = 3 * HY * HX * VPV;
-  for (int e = tid; e < nvec; e += 256) {
-    const int c8 = e % VPV;
-    const int v = e / VPV;
-    const int hx = v % HX, hy = (v / HX) % HY, hz = v / (HX * HY);
-    const int gx = x0 + hx - 1, gy = y0 + hy - 1, gz = z + hz - 1;
-    uint4 val = make_uint4(0u, 0u, 0u, 0u);
-    if (gx >= 0 && gx < W && gy >= 0 && gy < H && gz >= 0 && gz < D)
-      val = reinterpret_cast<const uint4 *>(X + (((size_t)gz * H + gy) * W + gx) * CIN)[c8];
-    reinterpret_cast<uint4 *>(tile + (size_t)v * CIN)[c8] = val;
+  const int tilesx = (W + TX - 1) / TX, tilesy = (H + TY - 1) / TY;
+  const int ntiles = tilesx * tilesy * D;
+  // weights of output channels co0 .. co0+N-1, [27][CIN/8][N][8]
+  for (int e = tid; e < 27 * (CIN / 8) * N; e += THREADS) {
+    const int n = e % N, tk = e / N;
+    reinterpret_cast<uint4 *>(wts)[e] = reinterpret_cast<const uint4 *>(Wt)[(size_t)tk * NT + co0 + n];
   }
+  if (tid == 0) {
+    mbar_init(&bar_load[0], 1);
+    mbar_init(&bar_load[1], 1);
+    mbar_init(&bar_mma[0], 1);
+    mbar_init(&bar_mma[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    tmem_alloc(tslot, tmem_cols(N));
+    tmem_relinquish();
+  }
+  fence_proxy_async();  // the weights, written by plain stores, are read by the tensor cores
+  fence_before_sync();
   __syncthreads();
-  float acc[COUT / 8][4];
+  fence_after_sync();
+  const uint32_t tbase = *tslot;
+  const uint32_t hbase = smem_addr(halo), wbase = smem_addr(wts);
+  constexpr uint32_t idesc = idesc_bf16(128, N);
+  // issue and completion counts of the barriers (uniform over the CTA)
+  uint32_t ld_issued[2] = {0, 0}, ld_done[2] = {0, 0}, mma_issued[2] = {0, 0}, mma_done[2] = {0, 0};
+  auto issue_load = [&](int tile, int s) {
+    if (tid == 0) {
+      const int txi = tile % tilesx, tyi = (tile / tilesx) % tilesy, z = tile / (tilesx * tilesy);
+      mbar_expect_tx(&bar_load[s], (CIN / 8) * SLAB_BYTES);
 #pragma unroll
-  for (int n = 0; n < COUT / 8; n++) acc[n][0] = acc[n][1] = acc[n][2] = acc[n][3] = 0.f;
-  // ldmatrix row owned by this lane: matrix mi = lane/8 -> A rows (mi&1)*8 + lane%8,
-  // channel offset (mi>>1)*8
-  const int arow = ((lane >> 3) & 1) * 8 + (lane & 7);
-  const int acol = (lane >> 4) * 8;
-  for (int tap = 0; tap < 27; tap++) {
-    const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;  // halo offsets 0..2
-    const int hv = (dz * HY + (warp + dy)) * HX + (arow + dx);
-    const unsigned abase = smem_u32(tile + (size_t)hv * CIN + acol);
-#pragma unroll
-    for (int kk = 0; kk < CIN / 16; kk++) {
-      unsigned a0, a1, a2, a3;
-      ldmatrix_x4(a0, a1, a2, a3, abase + kk * 32);
-      const uint2 *wp = Wp + ((size_t)(tap * (CIN / 16) + kk) * (COUT / 8)) * 32 + lane;
-#pragma unroll
-      for (int n = 0; n < COUT / 8; n++) {
-        const uint2 b = __ldg(wp + n * 32);
-        mma_bf16(acc[n], a0, a1, a2, a3, b.x, b.y);
-      }
+      for (int k8 = 0; k8 < CIN / 8; k8++)
+        tma_load_4d(halo + ((size_t)s * (CIN / 8) + k8) * SLAB, &xmap, &bar_load[s], k8 * 8, txi * TX - 1,
+                    tyi * TY - 1, z - 1);
     }
-  }
-  // epilogue: rows g, g+8 of the warp's 16 voxels, columns n*8 + 2t, 2t+1
-  const int g = lane >> 2, t4 = lane & 3;
-  const int y = y0 + warp;
-  if (y >= H) return;
+    ld_issued[s]++;
+  };
+  bool ok = true;
+  int tile = blockIdx.x;
+  if (tile < ntiles) issue_load(tile, 0);
+  for (int i = 0; tile < ntiles; tile += gridDim.x, i++) {
+    const int s = STAGES == 2 ? (i & 1) : 0;
+    const int next = tile + (int)gridDim.x;
+    if (STAGES == 2 && next < ntiles) issue_load(next, s ^ 1);
+    const bool lok = mbar_wait(&bar_load[s], ld_done[s] & 1, kWaitPolls);
+    ld_done[s]++;
+    if (!__syncthreads_and(lok)) {
+      ok = false;
+      break;
+    }
+    fence_after_sync();
+    const int acc = i & 1;
+    const uint32_t dt = tbase + (uint32_t)(acc * acc_cols(N));
+    if (tid == 0) {
+      const uint32_t a0 = hbase + (uint32_t)(s * (CIN / 8)) * SLAB;
+#pragma unroll 1
+      for (int tap = 0; tap < 27; tap++) {
+        const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
+        const uint32_t aoff = (uint32_t)(((dz * HY + dy) * HX + dx) * 16);
 #pragma unroll
-  for (int half = 0; half < 2; half++) {
-    const int x = x0 + g + half * 8;
-    if (x >= W) continue;
+        for (int q = 0; q < CIN / 16; q++) {
+          const uint64_t ad = smem_desc(a0 + (uint32_t)(2 * q) * SLAB + aoff, SLAB, SBO_A);
+          const uint64_t bd = smem_desc(wbase + (uint32_t)((tap * (CIN / 8) + 2 * q) * N * 16), N * 16, 128);
+          umma_bf16(dt, ad, bd, idesc, (tap | q) != 0);
+        }
+      }
+      mma_commit(&bar_mma[acc]);
+    }
+    mma_issued[acc]++;
+    const bool mok = mbar_wait(&bar_mma[acc], mma_done[acc] & 1, kWaitPolls);
+    mma_done[acc]++;
+    if (!__syncthreads_and(mok)) {
+      ok = false;
+      break;
+    }
+    fence_after_sync();
+    if (STAGES == 1 && next < ntiles) issue_load(next, 0);  // the halo buffer is free once the MMAs are done
+    // epilogue: warp w holds TMEM lanes 32w .. 32w+31 = tile rows m = 8 * my + mx
+    const int m = 32 * warp + lane, mx = m & 7, my = m >> 3;
+    const int txi = tile % tilesx, tyi = (tile / tilesx) % tilesy, z = tile / (tilesx * tilesy);
+    const int x = txi * TX + mx, y = tyi * TY + my;
+    const bool inside = x < W && y < H;
     const size_t vox = ((size_t)z * H + y) * W + x;
 #pragma unroll
-    for (int n = 0; n < COUT / 8; n++) {
-      const int co = n * 8 + 2 * t4;
-      float v0 = acc[n][half * 2 + 0], v1 = acc[n][half * 2 + 1];
-      if (bias) {
-        v0 += bias[co];
-        v1 += bias[co + 1];
+    for (int c = 0; c < N; c += 16) {
+      float v[16];
+      tmem_ld16(dt + ((uint32_t)(32 * warp) << 16) + (uint32_t)c, v);
+#pragma unroll
+      for (int q = 0; q < 16; q++) {
+        const int co = co0 + c + q;
+        if (bias && co < nbias) v[q] += bias[co];
+        if (RELU) v[q] = fmaxf(v[q], 0.f);
       }
-      if (RELU) {
-        v0 = fmaxf(v0, 0.f);
-        v1 = fmaxf(v1, 0.f);
-      }
+      if (!inside || c >= ywrite) continue;
       if (OUTF) {
-        float *Y = reinterpret_cast<float *>(Yv);
-        Y[vox * COUT + co] = v0;
-        Y[vox * COUT + co + 1] = v1;
+        float *Y = reinterpret_cast<float *>(Yv) + vox * ystride + co0 + c;
+        reinterpret_cast<float4 *>(Y)[0] = make_float4(v[0], v[1], v[2], v[3]);
+        reinterpret_cast<float4 *>(Y)[1] = make_float4(v[4], v[5], v[6], v[7]);
+        if (ywrite - c >= 16) {
+          reinterpret_cast<float4 *>(Y)[2] = make_float4(v[8], v[9], v[10], v[11]);
+          reinterpret_cast<float4 *>(Y)[3] = make_float4(v[12], v[13], v[14], v[15]);
+        }
       } else {
-        bf16 *Y = reinterpret_cast<bf16 *>(Yv);
-        *reinterpret_cast<__nv_bfloat162 *>(Y + vox * COUT + co) = __floats2bfloat162_rn(v0, v1);
+        bf16 *Y = reinterpret_cast<bf16 *>(Yv) + vox * ystride + co0 + c;
+        uint4 o[2];
+        __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(o);
+#pragma unroll
+        for (int q = 0; q < 8; q++) h[q] = __floats2bfloat162_rn(v[2 * q], v[2 * q + 1]);
+        reinterpret_cast<uint4 *>(Y)[0] = o[0];
+        reinterpret_cast<uint4 *>(Y)[1] = o[1];
       }
     }
+    fence_before_sync();
+    __syncthreads();
+  }
+  // anything still in flight (only after a timeout) is waited for, bounded
+  for (int q = 0; q < 2; q++) {
+    while (ld_done[q] < ld_issued[q]) {
+      mbar_wait(&bar_load[q], ld_done[q] & 1, kWaitPolls);
+      ld_done[q]++;
+    }
+    while (mma_done[q] < mma_issued[q]) {
+      mbar_wait(&bar_mma[q], mma_done[q] & 1, kWaitPolls);
+      mma_done[q]++;
+    }
+  }
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  if (warp == 0) tmem_dealloc(tbase, tmem_cols(N));
+  if (!ok && tid == 0) atomicExch(err, 1);
+}
+
+// Weights packed for k_conv3_tc: dst[tap][kin/8][ntot][8] bf16 from the FP32
+// master Wt[27][cin][cout].  Forward: K = input channels, N = output channels.
+// transpose (data gradient): K = the forward outputs, N = the forward inputs,
+// taps mirrored.  Padding channels are zero.
+__global__ void k_pack_tc(const float *__restrict__ Wt, bf16 *__restrict__ dst, int cin, int cout, int kin, int ntot,
+                          int transpose) {
+  const int total = 27 * kin * ntot;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+    const int j = e & 7;
+    const int n = (e >> 3) % ntot;
+    const int k8 = (e / (8 * ntot)) % (kin / 8);
+    const int tap = e / (8 * ntot * (kin / 8));
+    const int k = k8 * 8 + j;
+    float w = 0.f;
+    if (!transpose) {
+      if (k < cin && n < cout) w = Wt[((size_t)tap * cin + k) * cout + n];
+    } else {
+      if (k < cout && n < cin) w = Wt[((size_t)(26 - tap) * cin + n) * cout + k];
+    }
+    dst[e] = __float2bfloat16(w);
   }
 }
 
@@ -443,39 +570,6 @@ __global__ void k_mse(const float *__restrict__ y, const float *__restrict__ t, 
   if (threadIdx.x == 0) atomicAdd(loss, sh[0] / (double)nvox);
 }
 
-// Pack FP32 weights W[tap][ci][co] (logical sizes) into B fragments of the
-// forward conv (transpose=0) or of the data-gradient conv (transpose=1: uses
-// W[26-tap][co][ci], i.e. spatially flipped with in/out swapped).
-__global__ void k_pack(const float *__restrict__ Wt, uint2 *__restrict__ Wp, int cin, int cout, int kin, int kout,
-                       int transpose) {
-  // kin/kout: padded channel counts of the GEMM (K side / N side)
-  const int nfrag = 27 * (kin / 16) * (kout / 8) * 32;
-  for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nfrag; f += gridDim.x * blockDim.x) {
-    const int lane = f & 31;
-    int r = f >> 5;
-    const int n = r % (kout / 8);
-    r /= kout / 8;
-    const int kk = r % (kin / 16);
-    const int tap = r / (kin / 16);
-    const int g = lane >> 2, t4 = lane & 3;
-    float v[4];
-    for (int q = 0; q < 4; q++) {
-      const int k = kk * 16 + 2 * t4 + (q & 1) + (q >> 1) * 8;  // b0,b1: k=2t,2t+1 ; b2,b3: +8
-      const int nn = n * 8 + g;
-      float w = 0.f;
-      if (!transpose) {
-        if (k < cin && nn < cout) w = Wt[((size_t)tap * cin + k) * cout + nn];
-      } else {
-        // data gradient: K runs over the forward output channels, N over the inputs
-        if (k < cout && nn < cin) w = Wt[((size_t)(26 - tap) * cin + nn) * cout + k];
-      }
-      v[q] = w;
-    }
-    __nv_bfloat162 lo = __floats2bfloat162_rn(v[0], v[1]), hi = __floats2bfloat162_rn(v[2], v[3]);
-    Wp[f] = make_uint2(*reinterpret_cast<unsigned *>(&lo), *reinterpret_cast<unsigned *>(&hi));
-  }
-}
-
 // Adam step on FP32 master parameters.
 __global__ void k_adam(float *__restrict__ p, const float *__restrict__ g, float *__restrict__ m,
                        float *__restrict__ v, size_t n, float lr, float b1, float b2, float eps, float c1, float c2,
@@ -587,7 +681,8 @@ struct dsg_net {
   int W[4], H[4], D[4];             // interior sizes per level
   float *params = nullptr;          // FP32 master: per layer W[27][cin][cout] then bias[cout]
   float *grad = nullptr, *adam_m = nullptr, *adam_v = nullptr;
-  uint2 *packf[kLayers], *packb[kLayers];  // packed forward / data-gradient B fragments
+  bf16 *packt[kLayers], *packtb[kLayers];  // forward / data-gradient weights packed for k_conv3_tc
+  int *tc_err;                       // set by a tensor-core conv whose bounded wait ran out
   long long poff[kLayers];          // offset of each layer's weights in params
   // activations (bf16 channels-last)
   bf16 *x0;                          // input 16 ch, level 0
@@ -614,19 +709,69 @@ struct dsg_net {
 
 namespace {
 
-template <int CIN, int COUT, bool RELU, bool OUTF>
-cudaError_t conv_launch(const bf16 *X, const uint2 *Wp, const float *bias, void *Y, int W, int H, int D,
-                        cudaStream_t st) {
-  const size_t smem = 3 * (CTY + 2) * (CTX + 2) * CIN * sizeof(bf16);
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_conv3<CIN, COUT, RELU, OUTF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+// cuTensorMapEncodeTiled from the driver (no link-time dependency on libcuda).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<EncodeTiledFn>(f);
+  }();
+  return fn;
+}
+
+// TMA map of a channels-last bf16 activation [D][H][W][C] with the halo box of
+// k_conv3_tc: 8 channels x 10 x 18 x 3 voxels.
+cudaError_t halo_map(CUtensorMap *m, const bf16 *X, int C, int W, int H, int D) {
+  EncodeTiledFn fn = encode_tiled();
+  if (!fn) return cudaErrorNotSupported;
+  const cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)D};
+  const cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2};
+  const cuuint32_t box[4] = {8, (cuuint32_t)tc::HX, (cuuint32_t)tc::HY, (cuuint32_t)tc::HZ};
+  const cuuint32_t es[4] = {1, 1, 1, 1};
+  const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16 *>(X), dims, strides, box, es,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+// One tensor-core convolution: input X (CIN channels), weights Wt packed with
+// NT output channels, output channels co0 .. co0+N-1 of Y (ystride channels
+// per voxel, the first ywrite of them written).  Persistent grid: as many
+// CTAs as fit on the SMs (shared memory, TMEM), at most one per tile.
+template <int CIN, int N, int STAGES, bool RELU, bool OUTF>
+cudaError_t conv_tc(const bf16 *X, const bf16 *Wt, int NT, int co0, const float *bias, int nbias, void *Y, int ystride,
+                    int ywrite, int W, int H, int D, int *err, cudaStream_t st) {
+  constexpr size_t smem = tc::smem_bytes<CIN, N, STAGES>();
+  static_assert(smem <= 232448, "shared memory per CTA");
+  static int grid_cap = 0;
+  if (!grid_cap) {
+    cudaError_t e = cudaFuncSetAttribute(k_conv3_tc<CIN, N, STAGES, RELU, OUTF>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int dev = 0, sms = 0, occ = 0;
+    if (e == cudaSuccess) e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_conv3_tc<CIN, N, STAGES, RELU, OUTF>, tc::THREADS,
+                                                        smem);
     if (e != cudaSuccess) return e;
-    attr = true;
+    const int tmem_cap = 512 / tc::tmem_cols(N);
+    occ = occ < tmem_cap ? occ : tmem_cap;
+    grid_cap = sms * (occ > 0 ? occ : 1);
   }
-  const dim3 grid((unsigned)((W + CTX - 1) / CTX), (unsigned)((H + CTY - 1) / CTY), (unsigned)D);
-  DSG_COUNT k_conv3<CIN, COUT, RELU, OUTF><<<grid, 256, smem, st>>>(X, Wp, bias, Y, W, H, D);
+  CUtensorMap map;
+  cudaError_t e = halo_map(&map, X, CIN, W, H, D);
+  if (e != cudaSuccess) return e;
+  const int ntiles = ((W + tc::TX - 1) / tc::TX) * ((H + tc::TY - 1) / tc::TY) * D;
+  const int grid = ntiles < grid_cap ? ntiles : grid_cap;
+  DSG_COUNT k_conv3_tc<CIN, N, STAGES, RELU, OUTF><<<grid, tc::THREADS, smem, st>>>(
+      map, Wt, NT, co0, bias, nbias, Y, ystride, ywrite, W, H, D, err);
   return cudaGetLastError();
 }
 
@@ -645,34 +790,49 @@ cudaError_t wgrad_launch(const bf16 *X, const bf16 *G, float *dW, int W, int H, 
   return cudaGetLastError();
 }
 
-// forward conv of layer l; data-gradient conv uses the same kernels with the
-// channel roles swapped (packb).
+// forward conv of layer l (tensor cores); the 64 -> 64 layer runs as two
+// launches of 32 output channels each (its weights do not fit in one CTA's
+// shared memory next to the halo).
 cudaError_t conv_fwd(dsg_net *n, int l, const bf16 *X, void *Y, cudaStream_t st) {
   const int lv = kDefs[l].level;
   const int W = n->W[lv], H = n->H[lv], D = n->D[lv];
   const float *bias = n->params + n->poff[l] + 27LL * kDefs[l].cin * kDefs[l].cout;
+  const int nb = kDefs[l].cout;
+  const bf16 *Wt = n->packt[l];
+  int *err = n->tc_err;
   switch (l) {
-    case 0: return conv_launch<16, 16, true, false>(X, n->packf[0], bias, Y, W, H, D, st);
-    case 1: return conv_launch<16, 32, true, false>(X, n->packf[1], bias, Y, W, H, D, st);
-    case 2: return conv_launch<32, 64, true, false>(X, n->packf[2], bias, Y, W, H, D, st);
-    case 3: return conv_launch<64, 64, true, false>(X, n->packf[3], bias, Y, W, H, D, st);
-    case 4: return conv_launch<64, 32, true, false>(X, n->packf[4], bias, Y, W, H, D, st);
-    case 5: return conv_launch<32, 16, true, false>(X, n->packf[5], bias, Y, W, H, D, st);
-    default: return conv_launch<16, 8, false, true>(X, n->packf[6], bias, Y, W, H, D, st);
+    case 0: return conv_tc<16, 16, 2, true, false>(X, Wt, 16, 0, bias, nb, Y, 16, 16, W, H, D, err, st);
+    case 1: return conv_tc<16, 32, 2, true, false>(X, Wt, 32, 0, bias, nb, Y, 32, 32, W, H, D, err, st);
+    case 2: return conv_tc<32, 64, 2, true, false>(X, Wt, 64, 0, bias, nb, Y, 64, 64, W, H, D, err, st);
+    case 3: {
+      cudaError_t e = conv_tc<64, 32, 1, true, false>(X, Wt, 64, 0, bias, nb, Y, 64, 32, W, H, D, err, st);
+      if (e != cudaSuccess) return e;
+      return conv_tc<64, 32, 1, true, false>(X, Wt, 64, 32, bias, nb, Y, 64, 32, W, H, D, err, st);
+    }
+    case 4: return conv_tc<64, 32, 1, true, false>(X, Wt, 32, 0, bias, nb, Y, 32, 32, W, H, D, err, st);
+    case 5: return conv_tc<32, 16, 2, true, false>(X, Wt, 16, 0, bias, nb, Y, 16, 16, W, H, D, err, st);
+    default: return conv_tc<16, 16, 2, false, true>(X, Wt, 16, 0, bias, nb, Y, 8, 8, W, H, D, err, st);
   }
 }
 
-// data gradient of layer l: dX (bf16, cinp channels) from G (bf16, coutp channels)
+// data gradient of layer l: dX (bf16, cinp channels) from G (bf16, grad_ch(l)
+// channels) with the flipped, transposed weights
 cudaError_t conv_dgrad(dsg_net *n, int l, const bf16 *G, bf16 *dX, cudaStream_t st) {
   const int lv = kDefs[l].level;
   const int W = n->W[lv], H = n->H[lv], D = n->D[lv];
+  const bf16 *Wt = n->packtb[l];
+  int *err = n->tc_err;
   switch (l) {
-    case 1: return conv_launch<32, 16, false, false>(G, n->packb[1], nullptr, dX, W, H, D, st);
-    case 2: return conv_launch<64, 32, false, false>(G, n->packb[2], nullptr, dX, W, H, D, st);
-    case 3: return conv_launch<64, 64, false, false>(G, n->packb[3], nullptr, dX, W, H, D, st);
-    case 4: return conv_launch<32, 64, false, false>(G, n->packb[4], nullptr, dX, W, H, D, st);
-    case 5: return conv_launch<16, 32, false, false>(G, n->packb[5], nullptr, dX, W, H, D, st);
-    case 6: return conv_launch<16, 16, false, false>(G, n->packb[6], nullptr, dX, W, H, D, st);
+    case 1: return conv_tc<32, 16, 2, false, false>(G, Wt, 16, 0, nullptr, 0, dX, 16, 16, W, H, D, err, st);
+    case 2: return conv_tc<64, 32, 1, false, false>(G, Wt, 32, 0, nullptr, 0, dX, 32, 32, W, H, D, err, st);
+    case 3: {
+      cudaError_t e = conv_tc<64, 32, 1, false, false>(G, Wt, 64, 0, nullptr, 0, dX, 64, 32, W, H, D, err, st);
+      if (e != cudaSuccess) return e;
+      return conv_tc<64, 32, 1, false, false>(G, Wt, 64, 32, nullptr, 0, dX, 64, 32, W, H, D, err, st);
+    }
+    case 4: return conv_tc<32, 64, 2, false, false>(G, Wt, 64, 0, nullptr, 0, dX, 64, 64, W, H, D, err, st);
+    case 5: return conv_tc<16, 32, 2, false, false>(G, Wt, 32, 0, nullptr, 0, dX, 32, 32, W, H, D, err, st);
+    case 6: return conv_tc<16, 16, 2, false, false>(G, Wt, 16, 0, nullptr, 0, dX, 16, 16, W, H, D, err, st);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -717,20 +877,32 @@ int net_fail(dsg_net *n, cudaError_t e, const char *where) {
 
 size_t vox(const dsg_net *n, int lv) { return (size_t)n->W[lv] * n->H[lv] * n->D[lv]; }
 
+// Output channels of the forward tensor-core conv of layer l (padded to 16).
+inline int tc_nout(int l) { return kDefs[l].coutp < 16 ? 16 : kDefs[l].coutp; }
+
 int repack(dsg_net *n, cudaStream_t st) {
   for (int l = 0; l < kLayers; l++) {
     const LayerDef &L = kDefs[l];
     const float *Wt = n->params + n->poff[l];
-    int nf = 27 * (L.cinp / 16) * (L.coutp / 8) * 32;
-    DSG_COUNT k_pack<<<eblocks(nf), 256, 0, st>>>(Wt, n->packf[l], L.cin, L.cout, L.cinp, L.coutp, 0);
-    if (l > 0) {
-      // data gradient: K = forward outputs (padded to 16), N = forward inputs (padded to 8/16)
-      const int kin = L.coutp < 16 ? 16 : L.coutp, kout = L.cinp;
-      nf = 27 * (kin / 16) * (kout / 8) * 32;
-      DSG_COUNT k_pack<<<eblocks(nf), 256, 0, st>>>(Wt, n->packb[l], L.cin, L.cout, kin, kout, 1);
-    }
+    DSG_COUNT k_pack_tc<<<eblocks((size_t)27 * L.cinp * tc_nout(l)), 256, 0, st>>>(Wt, n->packt[l], L.cin, L.cout,
+                                                                                    L.cinp, tc_nout(l), 0);
+    if (l > 0)  // data gradient: K = the forward outputs (gradient channels), N = the forward inputs
+      DSG_COUNT k_pack_tc<<<eblocks((size_t)27 * grad_ch(l) * L.cinp), 256, 0, st>>>(Wt, n->packtb[l], L.cin, L.cout,
+                                                                                      grad_ch(l), L.cinp, 1);
   }
   NCK(n, cudaGetLastError());
+  return DSG_OK;
+}
+
+// A tensor-core conv whose bounded wait ran out leaves a flag; read (with a
+// synchronisation) by the entry points that synchronise anyway.
+int check_tc(dsg_net *n) {
+  int f = 0;
+  NCK(n, cudaMemcpy(&f, n->tc_err, sizeof f, cudaMemcpyDeviceToHost));
+  if (f) {
+    n->err = "tensor-core convolution: a bounded wait for a TMA copy or an MMA ran out";
+    return dsg::set_error(nullptr, DSG_E_CUDA, "%s", n->err.c_str());
+  }
   return DSG_OK;
 }
 
@@ -920,10 +1092,10 @@ int dsg_net_create(int W, int H, int D, uint64_t seed, dsg_net **out) {
   plan.push_back({(void **)&n->adam_v, up(DSG_NET_PARAMS * 4)});
   for (int l = 0; l < kLayers; l++) {
     const LayerDef &L = kDefs[l];
-    plan.push_back({(void **)&n->packf[l], up((size_t)27 * (L.cinp / 16) * (L.coutp / 8) * 32 * sizeof(uint2))});
-    const int kin = L.coutp < 16 ? 16 : L.coutp;
-    plan.push_back({(void **)&n->packb[l], up((size_t)27 * (kin / 16) * (L.cinp / 8) * 32 * sizeof(uint2))});
+    plan.push_back({(void **)&n->packt[l], up((size_t)27 * L.cinp * tc_nout(l) * sizeof(bf16))});
+    plan.push_back({(void **)&n->packtb[l], up((size_t)27 * grad_ch(l) * L.cinp * sizeof(bf16))});
   }
+  plan.push_back({(void **)&n->tc_err, 256});
   plan.push_back({(void **)&n->x0, up(v0 * 16 * 2)});
   plan.push_back({(void **)&n->e1, up(v0 * 16 * 2)});
   plan.push_back({(void **)&n->p1, up(v1 * 16 * 2)});
@@ -1025,7 +1197,7 @@ int dsg_net_forward_host(dsg_net *n, const float *x, float *y) {
   if (rc) return rc;
   DSG_COUNT k_output_ch0<<<eblocks(v0), 256>>>(n->yhost_f32, n->yout, v0);
   NCK(n, cudaMemcpy(y, n->yhost_f32, v0 * sizeof(float), cudaMemcpyDeviceToHost));
-  return DSG_OK;
+  return check_tc(n);
 }
 
 int dsg_net_grad_host(dsg_net *n, const float *x, const float *t, float *loss, float *grad) {
@@ -1042,7 +1214,7 @@ int dsg_net_grad_host(dsg_net *n, const float *x, const float *t, float *loss, f
   NCK(n, cudaMemcpy(&l, n->loss_dev, sizeof(double), cudaMemcpyDeviceToHost));
   *loss = (float)l;
   NCK(n, cudaMemcpy(grad, n->grad, DSG_NET_PARAMS * sizeof(float), cudaMemcpyDeviceToHost));
-  return DSG_OK;
+  return check_tc(n);
 }
 
 int dsg_net_train_step(dsg_net *n, float lr, float *loss) {
@@ -1064,7 +1236,7 @@ int dsg_net_train_step(dsg_net *n, float lr, float *loss) {
   NCK(n, cudaStreamSynchronize(st));
   if (loss) *loss = (float)*n->loss_host;
   n->have_target = false;
-  return DSG_OK;
+  return check_tc(n);
 }
 
 int64_t dsg_net_device_bytes(const dsg_net *n) { return n ? (int64_t)n->arena_bytes : 0; }
