@@ -102,29 +102,36 @@ constexpr int CTX = 16, CTY = 8;
 // inputs), the CTA uses output channels co0 .. co0+N-1; Y: [D][H][W][ystride]
 // (bf16, or float when OUTF, of which channels co0 .. co0+ywrite-1 are
 // written).  A CTA walks voxel tiles of 8 (x) x 16 (y) x 1 (z) = the 128 rows
-// of one MMA.  Per tile: TMA loads the 10 x 18 x 3 halo as CIN/8 slabs of 8
+// of one MMA.  Per tile TMA loads the 10 x 18 x 3 halo as CIN/8 slabs of 8
 // channels, which is the no-swizzle K-major core-matrix layout (8 voxels along
 // x x 16 bytes per core matrix, the next tile row 160 bytes on, the next 8
-// channels one slab on); one thread issues 27 x CIN/16 MMAs (M=128, N, K=16)
-// into a TMEM accumulator, each tap a shifted window of the same halo; the
-// four warps read their 32 TMEM lanes (= voxels) back, add the bias, apply
-// the ReLU and store.  With two halo stages the TMA of the next tile overlaps
-// the MMAs and epilogue of the current one; two TMEM accumulators alternate.
-// Every wait is bounded: on a timeout the CTA records it in *err, waits (again
-// bounded) for its copies and MMAs in flight, frees its TMEM and returns.
+// channels one slab on), and 27 x CIN/16 MMAs (M=128, N, K=16) accumulate
+// into TMEM, each tap a shifted window of the same halo.
+//
+// Warp roles (192 threads): warp 4 (one thread) issues the TMA loads into a
+// ring of STAGES halo buffers, warp 5 (one thread) issues the MMAs into two
+// alternating TMEM accumulators, warps 0-3 read their 32 TMEM lanes (= voxels)
+// back, add the bias, apply the ReLU and store.  mbarriers hand the buffers
+// over: full[s] (TMA bytes landed), empty[s] (the MMAs reading stage s are
+// done), tfull[a] (accumulator a complete), tempty[a] (its 128 values read).
+// The weights arrive once by bulk copies.  Every wait is bounded in time: on
+// a timeout the CTA raises a shared abort flag that ends every role's loop,
+// waits (again bounded) for its own copies and MMAs in flight, frees its TMEM
+// and records the failure in *err.
 namespace tc {
 constexpr int TX = 8, TY = 16, HX = TX + 2, HY = TY + 2, HZ = 3;
 constexpr uint32_t SLAB = 8704;        // 3 x 18 x 10 voxels x 16 bytes = 8640, padded to 128 bytes
 constexpr uint32_t SLAB_BYTES = 8640;  // bytes a slab's TMA box delivers
 constexpr uint32_t SBO_A = HX * 16;    // next tile row: 8 more M rows
-constexpr int THREADS = 128;
-constexpr uint32_t kWaitPolls = 1u << 26;
+constexpr int EPI_WARPS = 4, PRODUCER_WARP = 4, MMA_WARP = 5;
+constexpr int THREADS = 32 * (EPI_WARPS + 2);
+constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s bound of every wait
 
 __host__ __device__ constexpr int acc_cols(int n) { return n < 32 ? 32 : n; }
 __host__ __device__ constexpr int tmem_cols(int n) { return 2 * acc_cols(n) <= 64 ? 64 : 2 * acc_cols(n); }
 template <int CIN, int N, int STAGES>
 __host__ __device__ constexpr size_t smem_bytes() {
-  return 1024 + (size_t)STAGES * (CIN / 8) * SLAB + (size_t)27 * CIN * N * 2 + 128;
+  return 1024 + (size_t)STAGES * (CIN / 8) * SLAB + (size_t)27 * CIN * N * 2 + 256;
 }
 }  // namespace tc
 
@@ -136,147 +143,161 @@ __global__ void __launch_bounds__(tc::THREADS) k_conv3_tc(const __grid_constant_
                                                           int H, int D, int *__restrict__ err) {
   using namespace tc;
   using namespace dsg::tc05;
-  static_assert(N % 16 == 0 && N <= 256 && CIN % 16 == 0, "MMA shape");
+  static_assert(N % 16 == 0 && N <= 256 && CIN % 16 == 0 && STAGES >= 1 && STAGES <= 4, "MMA shape");
+  constexpr uint32_t WBYTES = 27u * CIN * N * 2;
   extern __shared__ unsigned char smem_raw[];
   unsigned char *sm = reinterpret_cast<unsigned char *>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   unsigned char *halo = sm;
   unsigned char *wts = sm + (size_t)STAGES * (CIN / 8) * SLAB;
-  uint64_t *bar_load = reinterpret_cast<uint64_t *>(wts + (size_t)27 * CIN * N * 2);  // [2]
-  uint64_t *bar_mma = bar_load + 2;                                                   // [2]
-  uint32_t *tslot = reinterpret_cast<uint32_t *>(bar_mma + 2);
+  uint64_t *full = reinterpret_cast<uint64_t *>(wts + WBYTES);
+  uint64_t *empty = full + STAGES, *tfull = empty + STAGES, *tempty = tfull + 2, *wbar = tempty + 2,
+           *fin = wbar + 1;
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(fin + 1);
+  volatile int *abort = reinterpret_cast<volatile int *>(tslot + 1);
+  __shared__ float s_bias[N];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int tilesx = (W + TX - 1) / TX, tilesy = (H + TY - 1) / TY;
   const int ntiles = tilesx * tilesy * D;
-  // weights of output channels co0 .. co0+N-1, [27][CIN/8][N][8]
-  for (int e = tid; e < 27 * (CIN / 8) * N; e += THREADS) {
-    const int n = e % N, tk = e / N;
-    reinterpret_cast<uint4 *>(wts)[e] = reinterpret_cast<const uint4 *>(Wt)[(size_t)tk * NT + co0 + n];
-  }
+  const int mine = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+  for (int q = tid; q < N; q += THREADS) s_bias[q] = (bias && co0 + q < nbias) ? bias[co0 + q] : 0.f;
   if (tid == 0) {
-    mbar_init(&bar_load[0], 1);
-    mbar_init(&bar_load[1], 1);
-    mbar_init(&bar_mma[0], 1);
-    mbar_init(&bar_mma[1], 1);
+    for (int s = 0; s < STAGES; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int a = 0; a < 2; a++) {
+      mbar_init(&tfull[a], 1);
+      mbar_init(&tempty[a], 32 * EPI_WARPS);
+    }
+    mbar_init(wbar, 1);
+    mbar_init(fin, 1);
+    *abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
     tmem_alloc(tslot, tmem_cols(N));
     tmem_relinquish();
   }
-  fence_proxy_async();  // the weights, written by plain stores, are read by the tensor cores
   fence_before_sync();
   __syncthreads();
   fence_after_sync();
   const uint32_t tbase = *tslot;
-  const uint32_t hbase = smem_addr(halo), wbase = smem_addr(wts);
-  constexpr uint32_t idesc = idesc_bf16(128, N);
-  // issue and completion counts of the barriers (uniform over the CTA)
-  uint32_t ld_issued[2] = {0, 0}, ld_done[2] = {0, 0}, mma_issued[2] = {0, 0}, mma_done[2] = {0, 0};
-  auto issue_load = [&](int tile, int s) {
-    if (tid == 0) {
-      const int txi = tile % tilesx, tyi = (tile / tilesx) % tilesy, z = tile / (tilesx * tilesy);
-      mbar_expect_tx(&bar_load[s], (CIN / 8) * SLAB_BYTES);
-#pragma unroll
-      for (int k8 = 0; k8 < CIN / 8; k8++)
-        tma_load_4d(halo + ((size_t)s * (CIN / 8) + k8) * SLAB, &xmap, &bar_load[s], k8 * 8, txi * TX - 1,
-                    tyi * TY - 1, z - 1);
-    }
-    ld_issued[s]++;
-  };
-  bool ok = true;
-  int tile = blockIdx.x;
-  if (tile < ntiles) issue_load(tile, 0);
-  for (int i = 0; tile < ntiles; tile += gridDim.x, i++) {
-    const int s = STAGES == 2 ? (i & 1) : 0;
-    const int next = tile + (int)gridDim.x;
-    if (STAGES == 2 && next < ntiles) issue_load(next, s ^ 1);
-    const bool lok = mbar_wait(&bar_load[s], ld_done[s] & 1, kWaitPolls);
-    ld_done[s]++;
-    if (!__syncthreads_and(lok)) {
-      ok = false;
-      break;
-    }
-    fence_after_sync();
-    const int acc = i & 1;
-    const uint32_t dt = tbase + (uint32_t)(acc * acc_cols(N));
-    if (tid == 0) {
-      const uint32_t a0 = hbase + (uint32_t)(s * (CIN / 8)) * SLAB;
-#pragma unroll 1
-      for (int tap = 0; tap < 27; tap++) {
-        const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
-        const uint32_t aoff = (uint32_t)(((dz * HY + dy) * HX + dx) * 16);
-#pragma unroll
-        for (int q = 0; q < CIN / 16; q++) {
-          const uint64_t ad = smem_desc(a0 + (uint32_t)(2 * q) * SLAB + aoff, SLAB, SBO_A);
-          const uint64_t bd = smem_desc(wbase + (uint32_t)((tap * (CIN / 8) + 2 * q) * N * 16), N * 16, 128);
-          umma_bf16(dt, ad, bd, idesc, (tap | q) != 0);
-        }
+
+  if (warp == PRODUCER_WARP) {
+    if (lane == 0) {
+      // weights of output channels co0 .. co0+N-1 as [27][CIN/8][N][8]
+      mbar_expect_tx(wbar, WBYTES);
+      if (NT == N) {
+        for (int tap = 0; tap < 27; tap++)
+          bulk_g2s(wts + (size_t)tap * CIN * N * 2, Wt + (size_t)tap * CIN * NT, CIN * N * 2, wbar);
+      } else {
+        for (int tk = 0; tk < 27 * (CIN / 8); tk++)
+          bulk_g2s(wts + (size_t)tk * N * 16, Wt + ((size_t)tk * NT + co0) * 8, N * 16, wbar);
       }
-      mma_commit(&bar_mma[acc]);
+      int nload = 0;
+      for (int i = 0; i < mine; i++) {
+        const int s = i % STAGES, k = i / STAGES;
+        if (k > 0 && !mbar_wait_ns(&empty[s], (k - 1) & 1, kWaitNs, abort)) break;
+        const int tile = (int)blockIdx.x + i * (int)gridDim.x;
+        const int txi = tile % tilesx, tyi = (tile / tilesx) % tilesy, z = tile / (tilesx * tilesy);
+        mbar_expect_tx(&full[s], (CIN / 8) * SLAB_BYTES);
+#pragma unroll
+        for (int k8 = 0; k8 < CIN / 8; k8++)
+          tma_load_4d(halo + ((size_t)s * (CIN / 8) + k8) * SLAB, &xmap, &full[s], k8 * 8, txi * TX - 1,
+                      tyi * TY - 1, z - 1);
+        nload = i + 1;
+      }
+      // copies in flight (after an abort only): the last load of each stage
+      for (int s = 0; s < STAGES && s < nload; s++) {
+        const int last = s + ((nload - 1 - s) / STAGES) * STAGES;
+        mbar_wait_ns(&full[s], (last / STAGES) & 1, kWaitNs, nullptr);
+      }
+      mbar_wait_ns(wbar, 0, kWaitNs, nullptr);
     }
-    mma_issued[acc]++;
-    const bool mok = mbar_wait(&bar_mma[acc], mma_done[acc] & 1, kWaitPolls);
-    mma_done[acc]++;
-    if (!__syncthreads_and(mok)) {
-      ok = false;
-      break;
+  } else if (warp == MMA_WARP) {
+    if (lane == 0) {
+      constexpr uint32_t idesc = idesc_bf16(128, N);
+      const uint64_t bdesc0 = smem_desc(smem_addr(wts), N * 16, 128);
+      bool ok = mbar_wait_ns(wbar, 0, kWaitNs, abort);
+      for (int i = 0; ok && i < mine; i++) {
+        const int s = i % STAGES, k = i / STAGES, acc = i & 1, j = i >> 1;
+        if (!mbar_wait_ns(&full[s], k & 1, kWaitNs, abort)) break;
+        if (j > 0 && !mbar_wait_ns(&tempty[acc], (j - 1) & 1, kWaitNs, abort)) break;
+        fence_after_sync();
+        const uint64_t adesc0 = smem_desc(smem_addr(halo) + (uint32_t)(s * (CIN / 8)) * SLAB, SLAB, SBO_A);
+        const uint32_t dt = tbase + (uint32_t)(acc * acc_cols(N));
+        // descriptors hold address / 16 in their low 14 bits: a shared-memory
+        // offset is added to them as offset / 16 (no carry below 256 KB)
+#pragma unroll
+        for (int tap = 0; tap < 27; tap++) {
+          const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
+#pragma unroll
+          for (int q = 0; q < CIN / 16; q++) {
+            const uint32_t aoff = (uint32_t)(((dz * HY + dy) * HX + dx) * 16) + (uint32_t)(2 * q) * SLAB;
+            const uint32_t boff = (uint32_t)((tap * (CIN / 8) + 2 * q) * N * 16);
+            umma_bf16(dt, adesc0 + (aoff >> 4), bdesc0 + (boff >> 4), idesc, (tap | q) != 0);
+          }
+        }
+        mma_commit(&empty[s]);
+        mma_commit(&tfull[acc]);
+      }
+      mma_commit(fin);  // arrives once every MMA issued above has completed
+      mbar_wait_ns(fin, 0, kWaitNs, nullptr);
     }
-    fence_after_sync();
-    if (STAGES == 1 && next < ntiles) issue_load(next, 0);  // the halo buffer is free once the MMAs are done
+  } else {
     // epilogue: warp w holds TMEM lanes 32w .. 32w+31 = tile rows m = 8 * my + mx
     const int m = 32 * warp + lane, mx = m & 7, my = m >> 3;
-    const int txi = tile % tilesx, tyi = (tile / tilesx) % tilesy, z = tile / (tilesx * tilesy);
-    const int x = txi * TX + mx, y = tyi * TY + my;
-    const bool inside = x < W && y < H;
-    const size_t vox = ((size_t)z * H + y) * W + x;
+    for (int i = 0; i < mine; i++) {
+      const int acc = i & 1, j = i >> 1;
+      const bool ok = mbar_wait_ns(&tfull[acc], j & 1, kWaitNs, abort);
+      if (!__all_sync(0xffffffffu, ok)) break;
+      fence_after_sync();
+      const uint32_t dt = tbase + ((uint32_t)(32 * warp) << 16) + (uint32_t)(acc * acc_cols(N));
+      uint32_t r[N / 16][16];
 #pragma unroll
-    for (int c = 0; c < N; c += 16) {
-      float v[16];
-      tmem_ld16(dt + ((uint32_t)(32 * warp) << 16) + (uint32_t)c, v);
+      for (int c = 0; c < N / 16; c++) tmem_ld16_async(dt + (uint32_t)(16 * c), r[c]);
 #pragma unroll
-      for (int q = 0; q < 16; q++) {
-        const int co = co0 + c + q;
-        if (bias && co < nbias) v[q] += bias[co];
-        if (RELU) v[q] = fmaxf(v[q], 0.f);
-      }
-      if (!inside || c >= ywrite) continue;
-      if (OUTF) {
-        float *Y = reinterpret_cast<float *>(Yv) + vox * ystride + co0 + c;
-        reinterpret_cast<float4 *>(Y)[0] = make_float4(v[0], v[1], v[2], v[3]);
-        reinterpret_cast<float4 *>(Y)[1] = make_float4(v[4], v[5], v[6], v[7]);
-        if (ywrite - c >= 16) {
-          reinterpret_cast<float4 *>(Y)[2] = make_float4(v[8], v[9], v[10], v[11]);
-          reinterpret_cast<float4 *>(Y)[3] = make_float4(v[12], v[13], v[14], v[15]);
+      for (int c = 0; c < N / 16; c++) tmem_wait_ld16(r[c]);
+      fence_before_sync();
+      mbar_arrive(&tempty[acc]);
+      const int tile = (int)blockIdx.x + i * (int)gridDim.x;
+      const int txi = tile % tilesx, tyi = (tile / tilesx) % tilesy, z = tile / (tilesx * tilesy);
+      const int x = txi * TX + mx, y = tyi * TY + my;
+      const size_t vox = ((size_t)z * H + y) * W + x;
+#pragma unroll
+      for (int c = 0; c < N / 16; c++) {
+        if (x >= W || y >= H || 16 * c >= ywrite) break;
+        float v[16];
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+          v[q] = __uint_as_float(r[c][q]) + s_bias[16 * c + q];
+          if (RELU) v[q] = fmaxf(v[q], 0.f);
         }
-      } else {
-        bf16 *Y = reinterpret_cast<bf16 *>(Yv) + vox * ystride + co0 + c;
-        uint4 o[2];
-        __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(o);
+        if (OUTF) {
+          float *Y = reinterpret_cast<float *>(Yv) + vox * ystride + co0 + 16 * c;
+          reinterpret_cast<float4 *>(Y)[0] = make_float4(v[0], v[1], v[2], v[3]);
+          reinterpret_cast<float4 *>(Y)[1] = make_float4(v[4], v[5], v[6], v[7]);
+          if (ywrite - 16 * c >= 16) {
+            reinterpret_cast<float4 *>(Y)[2] = make_float4(v[8], v[9], v[10], v[11]);
+            reinterpret_cast<float4 *>(Y)[3] = make_float4(v[12], v[13], v[14], v[15]);
+          }
+        } else {
+          bf16 *Y = reinterpret_cast<bf16 *>(Yv) + vox * ystride + co0 + 16 * c;
+          uint4 o[2];
+          __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(o);
 #pragma unroll
-        for (int q = 0; q < 8; q++) h[q] = __floats2bfloat162_rn(v[2 * q], v[2 * q + 1]);
-        reinterpret_cast<uint4 *>(Y)[0] = o[0];
-        reinterpret_cast<uint4 *>(Y)[1] = o[1];
+          for (int q = 0; q < 8; q++) h[q] = __floats2bfloat162_rn(v[2 * q], v[2 * q + 1]);
+          reinterpret_cast<uint4 *>(Y)[0] = o[0];
+          reinterpret_cast<uint4 *>(Y)[1] = o[1];
+        }
       }
-    }
-    fence_before_sync();
-    __syncthreads();
-  }
-  // anything still in flight (only after a timeout) is waited for, bounded
-  for (int q = 0; q < 2; q++) {
-    while (ld_done[q] < ld_issued[q]) {
-      mbar_wait(&bar_load[q], ld_done[q] & 1, kWaitPolls);
-      ld_done[q]++;
-    }
-    while (mma_done[q] < mma_issued[q]) {
-      mbar_wait(&bar_mma[q], mma_done[q] & 1, kWaitPolls);
-      mma_done[q]++;
     }
   }
   fence_before_sync();
   __syncthreads();
   fence_after_sync();
   if (warp == 0) tmem_dealloc(tbase, tmem_cols(N));
-  if (!ok && tid == 0) atomicExch(err, 1);
+  if (tid == 0 && *abort) atomicExch(err, 1);
 }
 
 // Weights packed for k_conv3_tc: dst[tap][kin/8][ntot][8] bf16 from the FP32
@@ -754,15 +775,23 @@ cudaError_t conv_tc(const bf16 *X, const bf16 *Wt, int NT, int co0, const float 
   if (!grid_cap) {
     cudaError_t e = cudaFuncSetAttribute(k_conv3_tc<CIN, N, STAGES, RELU, OUTF>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    int dev = 0, sms = 0, occ = 0;
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_conv3_tc<CIN, N, STAGES, RELU, OUTF>,
+                               cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+    int dev = 0, sms = 0, smem_sm = 0;
+    cudaFuncAttributes fa;
     if (e == cudaSuccess) e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e == cudaSuccess)
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_conv3_tc<CIN, N, STAGES, RELU, OUTF>, tc::THREADS,
-                                                        smem);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_conv3_tc<CIN, N, STAGES, RELU, OUTF>);
     if (e != cudaSuccess) return e;
-    const int tmem_cap = 512 / tc::tmem_cols(N);
-    occ = occ < tmem_cap ? occ : tmem_cap;
+    // resident CTAs per SM: shared memory (1 KB reserved per CTA), TMEM
+    // columns, registers, threads
+    int occ = smem_sm / (int)(smem + fa.sharedSizeBytes + 1024);
+    occ = occ < 512 / tc::tmem_cols(N) ? occ : 512 / tc::tmem_cols(N);
+    const int regs = fa.numRegs > 0 ? fa.numRegs : 64;
+    occ = occ < 65536 / (regs * tc::THREADS) ? occ : 65536 / (regs * tc::THREADS);
+    occ = occ < 2048 / tc::THREADS ? occ : 2048 / tc::THREADS;
     grid_cap = sms * (occ > 0 ? occ : 1);
   }
   CUtensorMap map;
