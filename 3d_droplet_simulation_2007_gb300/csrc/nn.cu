@@ -98,148 +98,198 @@ constexpr int CTX = 16, CTY = 8;
 
 // ---- convolution forward / data gradient on tcgen05 ------------------------------
 // X: [D][H][W][CIN] bf16 (read through the TMA map xmap), Wt: packed weights
-// [27][CIN/8][NT][8] bf16 (tap, 8-channel input block, output channel, 8
-// inputs), the CTA uses output channels co0 .. co0+N-1; Y: [D][H][W][ystride]
-// (bf16, or float when OUTF, of which channels co0 .. co0+ywrite-1 are
-// written).  A CTA walks voxel tiles of 8 (x) x 16 (y) x 1 (z) = the 128 rows
-// of one MMA.  Per tile TMA loads the 10 x 18 x 3 halo as CIN/8 slabs of 8
-// channels, which is the no-swizzle K-major core-matrix layout (8 voxels along
-// x x 16 bytes per core matrix, the next tile row 160 bytes on, the next 8
-// channels one slab on), and 27 x CIN/16 MMAs (M=128, N, K=16) accumulate
-// into TMEM, each tap a shifted window of the same halo.
+// [9][CIN/8][3][NT][8] bf16 (in-plane tap dy*3+dx, 8-channel input block,
+// tap row dz, output channel, 8 inputs); the CTA uses output channels
+// co0 .. co0+COUT-1; Y: [D][H][W][ystride] (bf16, or float when OUTF, of which
+// channels co0 .. co0+ywrite-1 are written).
+//
+// A work unit is an 8 (x) x 16 (y) voxel tile -- the 128 rows M of one MMA --
+// over a chunk of L output planes z0 .. z0+L-1, marched in z: the input
+// planes z0-1 .. z0+L arrive one at a time by TMA (the 10 x 18 halo as CIN/8
+// slabs of 8 channels, which is the no-swizzle K-major core-matrix layout:
+// 8 voxels along x x 16 bytes per core matrix, the next tile row 160 bytes
+// on, the next 8 channels one slab on), and each input plane is multiplied
+// once by the weights of all three tap rows dz: per in-plane tap (dy, dx) and
+// 16 input channels one MMA with N = 3 x COUT, whose three column groups are
+// the accumulators of output planes z'+1, z', z'-1.  Those accumulators sit
+// side by side in TMEM with the plane index descending, so each MMA lands on
+// the right three planes; at the chunk ends and the domain faces the MMA is
+// narrowed to the groups of planes inside the chunk.  An output plane is
+// complete after its last input plane; the epilogue then reads it, sets its
+// columns back to zero (every MMA accumulates), adds the bias, applies the
+// ReLU and stores it.  Per input plane the tensor cores read each A tile once
+// for 3 x COUT outputs, and the halo is re-read (L + 2) / L times instead of
+// 27 / 9.
 //
 // Warp roles (192 threads): warp 4 (one thread) issues the TMA loads into a
-// ring of STAGES halo buffers, warp 5 (one thread) issues the MMAs into two
-// alternating TMEM accumulators, warps 0-3 read their 32 TMEM lanes (= voxels)
-// back, add the bias, apply the ReLU and store.  mbarriers hand the buffers
-// over: full[s] (TMA bytes landed), empty[s] (the MMAs reading stage s are
-// done), tfull[a] (accumulator a complete), tempty[a] (its 128 values read).
+// ring of STAGES plane buffers, warp 5 (one thread) issues the MMAs into two
+// TMEM chunk buffers, warps 0-3 own TMEM lanes 32w .. 32w+31 (= voxels) and
+// run the epilogue.  mbarriers hand the buffers over: full[s] (plane bytes
+// landed), empty[s] (the MMAs reading stage s are done), pdone[b][p] (plane p
+// of chunk buffer b complete), tempty[b] (chunk buffer b read and zeroed).
 // The weights arrive once by bulk copies.  Every wait is bounded in time: on
 // a timeout the CTA raises a shared abort flag that ends every role's loop,
 // waits (again bounded) for its own copies and MMAs in flight, frees its TMEM
 // and records the failure in *err.
 namespace tc {
-constexpr int TX = 8, TY = 16, HX = TX + 2, HY = TY + 2, HZ = 3;
-constexpr uint32_t SLAB = 8704;        // 3 x 18 x 10 voxels x 16 bytes = 8640, padded to 128 bytes
-constexpr uint32_t SLAB_BYTES = 8640;  // bytes a slab's TMA box delivers
-constexpr uint32_t SBO_A = HX * 16;    // next tile row: 8 more M rows
+constexpr int TX = 8, TY = 16, HX = TX + 2, HY = TY + 2;
+constexpr uint32_t PL = 2944;        // 18 x 10 voxels x 16 bytes = 2880, padded to 128 bytes
+constexpr uint32_t PL_BYTES = 2880;  // bytes one slab's TMA box delivers
+constexpr uint32_t SBO_A = HX * 16;  // next tile row: 8 more M rows
 constexpr int EPI_WARPS = 4, PRODUCER_WARP = 4, MMA_WARP = 5;
 constexpr int THREADS = 32 * (EPI_WARPS + 2);
 constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s bound of every wait
 
-__host__ __device__ constexpr int acc_cols(int n) { return n < 32 ? 32 : n; }
-__host__ __device__ constexpr int tmem_cols(int n) { return 2 * acc_cols(n) <= 64 ? 64 : 2 * acc_cols(n); }
-template <int CIN, int N, int STAGES>
+// TMEM columns of two chunk buffers of LMAX planes x COUT channels
+__host__ __device__ constexpr int tmem_cols(int cout, int lmax) {
+  return 2 * lmax * cout <= 32 ? 32 : 2 * lmax * cout <= 64 ? 64 : 2 * lmax * cout <= 128 ? 128
+                                   : 2 * lmax * cout <= 256 ? 256 : 512;
+}
+template <int CIN, int COUT, int STAGES>
 __host__ __device__ constexpr size_t smem_bytes() {
-  return 1024 + (size_t)STAGES * (CIN / 8) * SLAB + (size_t)27 * CIN * N * 2 + 256;
+  return 1024 + (size_t)STAGES * (CIN / 8) * PL + (size_t)27 * CIN * COUT * 2 + 512;
 }
 }  // namespace tc
 
-template <int CIN, int N, int STAGES, bool RELU, bool OUTF>
+template <int CIN, int COUT, int STAGES, int LMAX, bool RELU, bool OUTF>
 __global__ void __launch_bounds__(tc::THREADS) k_conv3_tc(const __grid_constant__ CUtensorMap xmap,
                                                           const bf16 *__restrict__ Wt, int NT, int co0,
                                                           const float *__restrict__ bias, int nbias,
                                                           void *__restrict__ Yv, int ystride, int ywrite, int W,
-                                                          int H, int D, int *__restrict__ err) {
+                                                          int H, int D, int L, int *__restrict__ err) {
   using namespace tc;
   using namespace dsg::tc05;
-  static_assert(N % 16 == 0 && N <= 256 && CIN % 16 == 0 && STAGES >= 1 && STAGES <= 4, "MMA shape");
-  constexpr uint32_t WBYTES = 27u * CIN * N * 2;
+  static_assert(COUT % 16 == 0 && 3 * COUT <= 256 && CIN % 16 == 0 && STAGES >= 2 && STAGES <= 8, "MMA shape");
+  static_assert(2 * LMAX * COUT <= 512 && LMAX <= 16, "TMEM chunk buffers");
+  constexpr uint32_t WBYTES = 27u * CIN * COUT * 2;
+  constexpr uint32_t BROW = 3 * COUT * 16;  // bytes of one (tap, 8-channel block) of B
+  constexpr int TCOLS = tmem_cols(COUT, LMAX);
   extern __shared__ unsigned char smem_raw[];
   unsigned char *sm = reinterpret_cast<unsigned char *>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   unsigned char *halo = sm;
-  unsigned char *wts = sm + (size_t)STAGES * (CIN / 8) * SLAB;
+  unsigned char *wts = sm + (size_t)STAGES * (CIN / 8) * PL;
   uint64_t *full = reinterpret_cast<uint64_t *>(wts + WBYTES);
-  uint64_t *empty = full + STAGES, *tfull = empty + STAGES, *tempty = tfull + 2, *wbar = tempty + 2,
+  uint64_t *empty = full + STAGES, *tempty = empty + STAGES, *pdone = tempty + 2, *wbar = pdone + 2 * LMAX,
            *fin = wbar + 1;
   uint32_t *tslot = reinterpret_cast<uint32_t *>(fin + 1);
   volatile int *abort = reinterpret_cast<volatile int *>(tslot + 1);
-  __shared__ float s_bias[N];
+  __shared__ float s_bias[COUT];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int tilesx = (W + TX - 1) / TX, tilesy = (H + TY - 1) / TY;
-  const int ntiles = tilesx * tilesy * D;
-  const int mine = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
-  for (int q = tid; q < N; q += THREADS) s_bias[q] = (bias && co0 + q < nbias) ? bias[co0 + q] : 0.f;
+  const int tilesx = (W + TX - 1) / TX, tilesy = (H + TY - 1) / TY, tiles = tilesx * tilesy;
+  const int nunits = tiles * ((D + L - 1) / L);
+  const int mine = (int)blockIdx.x < nunits ? (nunits - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+  for (int q = tid; q < COUT; q += THREADS) s_bias[q] = (bias && co0 + q < nbias) ? bias[co0 + q] : 0.f;
   if (tid == 0) {
     for (int s = 0; s < STAGES; s++) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    for (int a = 0; a < 2; a++) {
-      mbar_init(&tfull[a], 1);
-      mbar_init(&tempty[a], 32 * EPI_WARPS);
-    }
+    mbar_init(&tempty[0], 32 * EPI_WARPS);
+    mbar_init(&tempty[1], 32 * EPI_WARPS);
+    for (int q = 0; q < 2 * LMAX; q++) mbar_init(&pdone[q], 1);
     mbar_init(wbar, 1);
     mbar_init(fin, 1);
     *abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
-    tmem_alloc(tslot, tmem_cols(N));
+    tmem_alloc(tslot, TCOLS);
     tmem_relinquish();
   }
   fence_before_sync();
   __syncthreads();
   fence_after_sync();
   const uint32_t tbase = *tslot;
+  // unit u: tile (txi, tyi) of chunk zc; its input planes zlo .. zhi
+  auto unit = [&](int i, int &txi, int &tyi, int &z0, int &lc, int &zlo, int &zhi) {
+    const int u = (int)blockIdx.x + i * (int)gridDim.x;
+    txi = u % tilesx;
+    tyi = (u / tilesx) % tilesy;
+    z0 = (u / tiles) * L;
+    lc = D - z0 < L ? D - z0 : L;
+    zlo = z0 > 0 ? z0 - 1 : 0;
+    zhi = z0 + lc < D ? z0 + lc : D - 1;
+  };
 
   if (warp == PRODUCER_WARP) {
     if (lane == 0) {
-      // weights of output channels co0 .. co0+N-1 as [27][CIN/8][N][8]
+      // weights of output channels co0 .. co0+COUT-1 as [9][CIN/8][3][COUT][8]
       mbar_expect_tx(wbar, WBYTES);
-      if (NT == N) {
-        for (int tap = 0; tap < 27; tap++)
-          bulk_g2s(wts + (size_t)tap * CIN * N * 2, Wt + (size_t)tap * CIN * NT, CIN * N * 2, wbar);
+      if (NT == COUT) {
+        bulk_g2s(wts, Wt, WBYTES, wbar);
       } else {
-        for (int tk = 0; tk < 27 * (CIN / 8); tk++)
-          bulk_g2s(wts + (size_t)tk * N * 16, Wt + ((size_t)tk * NT + co0) * 8, N * 16, wbar);
+        for (int r = 0; r < 27 * (CIN / 8); r++)
+          bulk_g2s(wts + (size_t)r * COUT * 16, Wt + ((size_t)r * NT + co0) * 8, COUT * 16, wbar);
       }
-      int nload = 0;
-      for (int i = 0; i < mine; i++) {
-        const int s = i % STAGES, k = i / STAGES;
-        if (k > 0 && !mbar_wait_ns(&empty[s], (k - 1) & 1, kWaitNs, abort)) break;
-        const int tile = (int)blockIdx.x + i * (int)gridDim.x;
-        const int txi = tile % tilesx, tyi = (tile / tilesx) % tilesy, z = tile / (tilesx * tilesy);
-        mbar_expect_tx(&full[s], (CIN / 8) * SLAB_BYTES);
+      int g = 0;
+      bool ok = true;
+      for (int i = 0; ok && i < mine; i++) {
+        int txi, tyi, z0, lc, zlo, zhi;
+        unit(i, txi, tyi, z0, lc, zlo, zhi);
+        for (int zp = zlo; zp <= zhi; zp++, g++) {
+          const int s = g % STAGES, k = g / STAGES;
+          if (k > 0 && !mbar_wait_ns(&empty[s], (k - 1) & 1, kWaitNs, abort)) {
+            ok = false;
+            break;
+          }
+          mbar_expect_tx(&full[s], (CIN / 8) * PL_BYTES);
 #pragma unroll
-        for (int k8 = 0; k8 < CIN / 8; k8++)
-          tma_load_4d(halo + ((size_t)s * (CIN / 8) + k8) * SLAB, &xmap, &full[s], k8 * 8, txi * TX - 1,
-                      tyi * TY - 1, z - 1);
-        nload = i + 1;
+          for (int k8 = 0; k8 < CIN / 8; k8++)
+            tma_load_4d(halo + ((size_t)s * (CIN / 8) + k8) * PL, &xmap, &full[s], k8 * 8, txi * TX - 1,
+                        tyi * TY - 1, zp);
+        }
       }
       // copies in flight (after an abort only): the last load of each stage
-      for (int s = 0; s < STAGES && s < nload; s++) {
-        const int last = s + ((nload - 1 - s) / STAGES) * STAGES;
+      for (int s = 0; s < STAGES && s < g; s++) {
+        const int last = s + ((g - 1 - s) / STAGES) * STAGES;
         mbar_wait_ns(&full[s], (last / STAGES) & 1, kWaitNs, nullptr);
       }
       mbar_wait_ns(wbar, 0, kWaitNs, nullptr);
     }
   } else if (warp == MMA_WARP) {
     if (lane == 0) {
-      constexpr uint32_t idesc = idesc_bf16(128, N);
-      const uint64_t bdesc0 = smem_desc(smem_addr(wts), N * 16, 128);
+      const uint64_t bdesc0 = smem_desc(smem_addr(wts), BROW, 128);
+      const uint32_t hbase = smem_addr(halo);
       bool ok = mbar_wait_ns(wbar, 0, kWaitNs, abort);
+      int g = 0;
       for (int i = 0; ok && i < mine; i++) {
-        const int s = i % STAGES, k = i / STAGES, acc = i & 1, j = i >> 1;
-        if (!mbar_wait_ns(&full[s], k & 1, kWaitNs, abort)) break;
-        if (j > 0 && !mbar_wait_ns(&tempty[acc], (j - 1) & 1, kWaitNs, abort)) break;
+        int txi, tyi, z0, lc, zlo, zhi;
+        unit(i, txi, tyi, z0, lc, zlo, zhi);
+        const int b = i & 1;
+        if (!mbar_wait_ns(&tempty[b], (i >> 1) & 1, kWaitNs, abort)) break;
         fence_after_sync();
-        const uint64_t adesc0 = smem_desc(smem_addr(halo) + (uint32_t)(s * (CIN / 8)) * SLAB, SLAB, SBO_A);
-        const uint32_t dt = tbase + (uint32_t)(acc * acc_cols(N));
-        // descriptors hold address / 16 in their low 14 bits: a shared-memory
-        // offset is added to them as offset / 16 (no carry below 256 KB)
-#pragma unroll
-        for (int tap = 0; tap < 27; tap++) {
-          const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
-#pragma unroll
-          for (int q = 0; q < CIN / 16; q++) {
-            const uint32_t aoff = (uint32_t)(((dz * HY + dy) * HX + dx) * 16) + (uint32_t)(2 * q) * SLAB;
-            const uint32_t boff = (uint32_t)((tap * (CIN / 8) + 2 * q) * N * 16);
-            umma_bf16(dt, adesc0 + (aoff >> 4), bdesc0 + (boff >> 4), idesc, (tap | q) != 0);
+        const uint32_t cbase = tbase + (uint32_t)(b * LMAX * COUT);
+        int next = 0;  // next plane of the chunk to report complete
+        for (int zp = zlo; zp <= zhi; zp++, g++) {
+          const int s = g % STAGES, k = g / STAGES;
+          if (!mbar_wait_ns(&full[s], k & 1, kWaitNs, abort)) {
+            ok = false;
+            break;
           }
+          // tap rows dz whose output plane zp + 1 - dz lies in the chunk
+          const int dlo = zp + 2 - z0 - lc > 0 ? zp + 2 - z0 - lc : 0;
+          const int dhi = zp + 1 - z0 < 2 ? zp + 1 - z0 : 2;
+          const uint32_t idesc = idesc_bf16(128, (dhi - dlo + 1) * COUT);
+          // plane z sits in slot lc - 1 - (z - z0): group dlo is plane zp + 1 - dlo
+          const uint32_t dt = cbase + (uint32_t)((lc - 1 - (zp + 1 - dlo - z0)) * COUT);
+          const uint64_t adesc0 = smem_desc(hbase + (uint32_t)(s * (CIN / 8)) * PL, PL, SBO_A);
+          const uint64_t bdesc1 = bdesc0 + ((uint32_t)(dlo * COUT * 16) >> 4);
+          // descriptors hold address / 16 in their low 14 bits: a shared-memory
+          // offset is added to them as offset / 16 (no carry below 256 KB)
+#pragma unroll
+          for (int t9 = 0; t9 < 9; t9++) {
+#pragma unroll
+            for (int q = 0; q < CIN / 16; q++) {
+              const uint32_t aoff = (uint32_t)(((t9 / 3) * HX + t9 % 3) * 16) + (uint32_t)(2 * q) * PL;
+              const uint32_t boff = (uint32_t)(t9 * (CIN / 8) + 2 * q) * BROW;
+              umma_bf16(dt, adesc0 + (aoff >> 4), bdesc1 + (boff >> 4), idesc, 1u);
+            }
+          }
+          mma_commit(&empty[s]);
+          // planes whose last input plane this was
+          const int upto = zp == zhi ? lc : (zp - z0 < lc ? zp - z0 : lc);
+          for (; next < upto; next++) mma_commit(&pdone[b * LMAX + next]);
         }
-        mma_commit(&empty[s]);
-        mma_commit(&tfull[acc]);
       }
       mma_commit(fin);  // arrives once every MMA issued above has completed
       mbar_wait_ns(fin, 0, kWaitNs, nullptr);
@@ -247,71 +297,101 @@ __global__ void __launch_bounds__(tc::THREADS) k_conv3_tc(const __grid_constant_
   } else {
     // epilogue: warp w holds TMEM lanes 32w .. 32w+31 = tile rows m = 8 * my + mx
     const int m = 32 * warp + lane, mx = m & 7, my = m >> 3;
-    for (int i = 0; i < mine; i++) {
-      const int acc = i & 1, j = i >> 1;
-      const bool ok = mbar_wait_ns(&tfull[acc], j & 1, kWaitNs, abort);
-      if (!__all_sync(0xffffffffu, ok)) break;
-      fence_after_sync();
-      const uint32_t dt = tbase + ((uint32_t)(32 * warp) << 16) + (uint32_t)(acc * acc_cols(N));
-      uint32_t r[N / 16][16];
+    const uint32_t lanes = (uint32_t)(32 * warp) << 16;
+    uint32_t zero[16];
 #pragma unroll
-      for (int c = 0; c < N / 16; c++) tmem_ld16_async(dt + (uint32_t)(16 * c), r[c]);
-#pragma unroll
-      for (int c = 0; c < N / 16; c++) tmem_wait_ld16(r[c]);
-      fence_before_sync();
-      mbar_arrive(&tempty[acc]);
-      const int tile = (int)blockIdx.x + i * (int)gridDim.x;
-      const int txi = tile % tilesx, tyi = (tile / tilesx) % tilesy, z = tile / (tilesx * tilesy);
+    for (int q = 0; q < 16; q++) zero[q] = 0u;
+    // both chunk buffers start at zero
+    for (int c = 0; c < 2 * LMAX * COUT; c += 16) tmem_st16(tbase + lanes + (uint32_t)c, zero);
+    tmem_wait_st();
+    fence_before_sync();
+    mbar_arrive(&tempty[0]);
+    mbar_arrive(&tempty[1]);
+    uint32_t par0 = 0u, par1 = 0u;  // phase parity of each pdone barrier of buffer 0 / 1, one bit per plane
+    bool ok = true;
+    for (int i = 0; ok && i < mine; i++) {
+      int txi, tyi, z0, lc, zlo, zhi;
+      unit(i, txi, tyi, z0, lc, zlo, zhi);
+      const int b = i & 1;
+      const uint32_t cbase = tbase + lanes + (uint32_t)(b * LMAX * COUT);
       const int x = txi * TX + mx, y = tyi * TY + my;
-      const size_t vox = ((size_t)z * H + y) * W + x;
-#pragma unroll
-      for (int c = 0; c < N / 16; c++) {
-        if (x >= W || y >= H || 16 * c >= ywrite) break;
-        float v[16];
-#pragma unroll
-        for (int q = 0; q < 16; q++) {
-          v[q] = __uint_as_float(r[c][q]) + s_bias[16 * c + q];
-          if (RELU) v[q] = fmaxf(v[q], 0.f);
+      const bool inside = x < W && y < H;
+      for (int p = 0; p < lc; p++) {
+        const uint32_t par = b ? par1 : par0;
+        const bool got = mbar_wait_ns(&pdone[b * LMAX + p], (par >> p) & 1u, kWaitNs, abort);
+        if (b) par1 ^= 1u << p;
+        else par0 ^= 1u << p;
+        if (!__all_sync(0xffffffffu, got)) {
+          ok = false;
+          break;
         }
-        if (OUTF) {
-          float *Y = reinterpret_cast<float *>(Yv) + vox * ystride + co0 + 16 * c;
-          reinterpret_cast<float4 *>(Y)[0] = make_float4(v[0], v[1], v[2], v[3]);
-          reinterpret_cast<float4 *>(Y)[1] = make_float4(v[4], v[5], v[6], v[7]);
-          if (ywrite - 16 * c >= 16) {
-            reinterpret_cast<float4 *>(Y)[2] = make_float4(v[8], v[9], v[10], v[11]);
-            reinterpret_cast<float4 *>(Y)[3] = make_float4(v[12], v[13], v[14], v[15]);
-          }
-        } else {
-          bf16 *Y = reinterpret_cast<bf16 *>(Yv) + vox * ystride + co0 + 16 * c;
-          uint4 o[2];
-          __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(o);
+        fence_after_sync();
+        const uint32_t dt = cbase + (uint32_t)((lc - 1 - p) * COUT);
+        uint32_t r[COUT / 16][16];
 #pragma unroll
-          for (int q = 0; q < 8; q++) h[q] = __floats2bfloat162_rn(v[2 * q], v[2 * q + 1]);
-          reinterpret_cast<uint4 *>(Y)[0] = o[0];
-          reinterpret_cast<uint4 *>(Y)[1] = o[1];
+        for (int c = 0; c < COUT / 16; c++) tmem_ld16_async(dt + (uint32_t)(16 * c), r[c]);
+#pragma unroll
+        for (int c = 0; c < COUT / 16; c++) tmem_wait_ld16(r[c]);
+#pragma unroll
+        for (int c = 0; c < COUT / 16; c++) tmem_st16(dt + (uint32_t)(16 * c), zero);
+        const size_t vox = ((size_t)(z0 + p) * H + y) * W + x;
+#pragma unroll
+        for (int c = 0; c < COUT / 16; c++) {
+          if (!inside || 16 * c >= ywrite) break;
+          float v[16];
+#pragma unroll
+          for (int q = 0; q < 16; q++) {
+            v[q] = __uint_as_float(r[c][q]) + s_bias[16 * c + q];
+            if (RELU) v[q] = fmaxf(v[q], 0.f);
+          }
+          if (OUTF) {
+            float *Y = reinterpret_cast<float *>(Yv) + vox * ystride + co0 + 16 * c;
+            reinterpret_cast<float4 *>(Y)[0] = make_float4(v[0], v[1], v[2], v[3]);
+            reinterpret_cast<float4 *>(Y)[1] = make_float4(v[4], v[5], v[6], v[7]);
+            if (ywrite - 16 * c >= 16) {
+              reinterpret_cast<float4 *>(Y)[2] = make_float4(v[8], v[9], v[10], v[11]);
+              reinterpret_cast<float4 *>(Y)[3] = make_float4(v[12], v[13], v[14], v[15]);
+            }
+          } else {
+            bf16 *Y = reinterpret_cast<bf16 *>(Yv) + vox * ystride + co0 + 16 * c;
+            uint4 o[2];
+            __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(o);
+#pragma unroll
+            for (int q = 0; q < 8; q++) h[q] = __floats2bfloat162_rn(v[2 * q], v[2 * q + 1]);
+            reinterpret_cast<uint4 *>(Y)[0] = o[0];
+            reinterpret_cast<uint4 *>(Y)[1] = o[1];
+          }
         }
       }
+      if (!ok) break;
+      tmem_wait_st();
+      fence_before_sync();
+      mbar_arrive(&tempty[b]);
     }
   }
   fence_before_sync();
   __syncthreads();
   fence_after_sync();
-  if (warp == 0) tmem_dealloc(tbase, tmem_cols(N));
+  if (warp == 0) tmem_dealloc(tbase, TCOLS);
   if (tid == 0 && *abort) atomicExch(err, 1);
 }
 
-// Weights packed for k_conv3_tc: dst[tap][kin/8][ntot][8] bf16 from the FP32
-// master Wt[27][cin][cout].  Forward: K = input channels, N = output channels.
-// transpose (data gradient): K = the forward outputs, N = the forward inputs,
-// taps mirrored.  Padding channels are zero.
+// Weights packed for k_conv3_tc: dst[t9][kin/8][3][ntot][8] bf16 (in-plane tap
+// t9 = dy*3+dx, 8-channel input block, tap row dz, output channel, 8 inputs)
+// from the FP32 master Wt[27][cin][cout] (tap = dz*9 + t9).  Forward: K =
+// input channels, N = output channels.  transpose (data gradient): K = the
+// forward outputs, N = the forward inputs, taps mirrored.  Padding channels
+// are zero.
 __global__ void k_pack_tc(const float *__restrict__ Wt, bf16 *__restrict__ dst, int cin, int cout, int kin, int ntot,
                           int transpose) {
   const int total = 27 * kin * ntot;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
     const int j = e & 7;
     const int n = (e >> 3) % ntot;
-    const int k8 = (e / (8 * ntot)) % (kin / 8);
-    const int tap = e / (8 * ntot * (kin / 8));
+    const int dz = (e / (8 * ntot)) % 3;
+    const int k8 = (e / (24 * ntot)) % (kin / 8);
+    const int t9 = e / (24 * ntot * (kin / 8));
+    const int tap = dz * 9 + t9;
     const int k = k8 * 8 + j;
     float w = 0.f;
     if (!transpose) {
@@ -748,13 +828,13 @@ EncodeTiledFn encode_tiled() {
 }
 
 // TMA map of a channels-last bf16 activation [D][H][W][C] with the halo box of
-// k_conv3_tc: 8 channels x 10 x 18 x 3 voxels.
+// k_conv3_tc: 8 channels x 10 x 18 voxels of one plane.
 cudaError_t halo_map(CUtensorMap *m, const bf16 *X, int C, int W, int H, int D) {
   EncodeTiledFn fn = encode_tiled();
   if (!fn) return cudaErrorNotSupported;
   const cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)D};
   const cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2};
-  const cuuint32_t box[4] = {8, (cuuint32_t)tc::HX, (cuuint32_t)tc::HY, (cuuint32_t)tc::HZ};
+  const cuuint32_t box[4] = {8, (cuuint32_t)tc::HX, (cuuint32_t)tc::HY, 1};
   const cuuint32_t es[4] = {1, 1, 1, 1};
   const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16 *>(X), dims, strides, box, es,
                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -763,32 +843,35 @@ cudaError_t halo_map(CUtensorMap *m, const bf16 *X, int C, int W, int H, int D) 
 }
 
 // One tensor-core convolution: input X (CIN channels), weights Wt packed with
-// NT output channels, output channels co0 .. co0+N-1 of Y (ystride channels
-// per voxel, the first ywrite of them written).  Persistent grid: as many
-// CTAs as fit on the SMs (shared memory, TMEM), at most one per tile.
-template <int CIN, int N, int STAGES, bool RELU, bool OUTF>
+// NT output channels, output channels co0 .. co0+COUT-1 of Y (ystride
+// channels per voxel, the first ywrite of them written).  Persistent grid: as
+// many CTAs as fit on the SMs (shared memory, TMEM columns, registers), at
+// most one per work unit; the chunk length L (<= LMAX planes) is the largest
+// that still gives every CTA a unit.
+template <int CIN, int COUT, int STAGES, int LMAX, bool RELU, bool OUTF>
 cudaError_t conv_tc(const bf16 *X, const bf16 *Wt, int NT, int co0, const float *bias, int nbias, void *Y, int ystride,
                     int ywrite, int W, int H, int D, int *err, cudaStream_t st) {
-  constexpr size_t smem = tc::smem_bytes<CIN, N, STAGES>();
+  constexpr size_t smem = tc::smem_bytes<CIN, COUT, STAGES>();
   static_assert(smem <= 232448, "shared memory per CTA");
+  auto kern = k_conv3_tc<CIN, COUT, STAGES, LMAX, RELU, OUTF>;
   static int grid_cap = 0;
   if (!grid_cap) {
-    cudaError_t e = cudaFuncSetAttribute(k_conv3_tc<CIN, N, STAGES, RELU, OUTF>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_conv3_tc<CIN, N, STAGES, RELU, OUTF>,
-                               cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+      e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               (int)cudaSharedmemCarveoutMaxShared);
     int dev = 0, sms = 0, smem_sm = 0;
     cudaFuncAttributes fa;
     if (e == cudaSuccess) e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_conv3_tc<CIN, N, STAGES, RELU, OUTF>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, kern);
     if (e != cudaSuccess) return e;
     // resident CTAs per SM: shared memory (1 KB reserved per CTA), TMEM
     // columns, registers, threads
+    constexpr int tcap = 512 / tc::tmem_cols(COUT, LMAX);
     int occ = smem_sm / (int)(smem + fa.sharedSizeBytes + 1024);
-    occ = occ < 512 / tc::tmem_cols(N) ? occ : 512 / tc::tmem_cols(N);
+    occ = occ < tcap ? occ : tcap;
     const int regs = fa.numRegs > 0 ? fa.numRegs : 64;
     occ = occ < 65536 / (regs * tc::THREADS) ? occ : 65536 / (regs * tc::THREADS);
     occ = occ < 2048 / tc::THREADS ? occ : 2048 / tc::THREADS;
@@ -797,10 +880,13 @@ cudaError_t conv_tc(const bf16 *X, const bf16 *Wt, int NT, int co0, const float 
   CUtensorMap map;
   cudaError_t e = halo_map(&map, X, CIN, W, H, D);
   if (e != cudaSuccess) return e;
-  const int ntiles = ((W + tc::TX - 1) / tc::TX) * ((H + tc::TY - 1) / tc::TY) * D;
-  const int grid = ntiles < grid_cap ? ntiles : grid_cap;
-  DSG_COUNT k_conv3_tc<CIN, N, STAGES, RELU, OUTF><<<grid, tc::THREADS, smem, st>>>(
-      map, Wt, NT, co0, bias, nbias, Y, ystride, ywrite, W, H, D, err);
+  const int tiles = ((W + tc::TX - 1) / tc::TX) * ((H + tc::TY - 1) / tc::TY);
+  const long long span = (long long)tiles * D / grid_cap;
+  const int L = span < 1 ? 1 : (span > LMAX ? LMAX : (int)span);
+  const int nunits = tiles * ((D + L - 1) / L);
+  const int grid = nunits < grid_cap ? nunits : grid_cap;
+  DSG_COUNT kern<<<grid, tc::THREADS, smem, st>>>(map, Wt, NT, co0, bias, nbias, Y, ystride, ywrite, W, H, D, L,
+                                                  err);
   return cudaGetLastError();
 }
 
@@ -830,17 +916,17 @@ cudaError_t conv_fwd(dsg_net *n, int l, const bf16 *X, void *Y, cudaStream_t st)
   const bf16 *Wt = n->packt[l];
   int *err = n->tc_err;
   switch (l) {
-    case 0: return conv_tc<16, 16, 2, true, false>(X, Wt, 16, 0, bias, nb, Y, 16, 16, W, H, D, err, st);
-    case 1: return conv_tc<16, 32, 2, true, false>(X, Wt, 32, 0, bias, nb, Y, 32, 32, W, H, D, err, st);
-    case 2: return conv_tc<32, 64, 2, true, false>(X, Wt, 64, 0, bias, nb, Y, 64, 64, W, H, D, err, st);
+    case 0: return conv_tc<16, 16, 4, 8, true, false>(X, Wt, 16, 0, bias, nb, Y, 16, 16, W, H, D, err, st);
+    case 1: return conv_tc<16, 32, 4, 4, true, false>(X, Wt, 32, 0, bias, nb, Y, 32, 32, W, H, D, err, st);
+    case 2: return conv_tc<32, 64, 4, 4, true, false>(X, Wt, 64, 0, bias, nb, Y, 64, 64, W, H, D, err, st);
     case 3: {
-      cudaError_t e = conv_tc<64, 32, 1, true, false>(X, Wt, 64, 0, bias, nb, Y, 64, 32, W, H, D, err, st);
+      cudaError_t e = conv_tc<64, 32, 3, 8, true, false>(X, Wt, 64, 0, bias, nb, Y, 64, 32, W, H, D, err, st);
       if (e != cudaSuccess) return e;
-      return conv_tc<64, 32, 1, true, false>(X, Wt, 64, 32, bias, nb, Y, 64, 32, W, H, D, err, st);
+      return conv_tc<64, 32, 3, 8, true, false>(X, Wt, 64, 32, bias, nb, Y, 64, 32, W, H, D, err, st);
     }
-    case 4: return conv_tc<64, 32, 1, true, false>(X, Wt, 32, 0, bias, nb, Y, 32, 32, W, H, D, err, st);
-    case 5: return conv_tc<32, 16, 2, true, false>(X, Wt, 16, 0, bias, nb, Y, 16, 16, W, H, D, err, st);
-    default: return conv_tc<16, 16, 2, false, true>(X, Wt, 16, 0, bias, nb, Y, 8, 8, W, H, D, err, st);
+    case 4: return conv_tc<64, 32, 3, 8, true, false>(X, Wt, 32, 0, bias, nb, Y, 32, 32, W, H, D, err, st);
+    case 5: return conv_tc<32, 16, 4, 8, true, false>(X, Wt, 16, 0, bias, nb, Y, 16, 16, W, H, D, err, st);
+    default: return conv_tc<16, 16, 4, 8, false, true>(X, Wt, 16, 0, bias, nb, Y, 8, 8, W, H, D, err, st);
   }
 }
 
@@ -852,16 +938,16 @@ cudaError_t conv_dgrad(dsg_net *n, int l, const bf16 *G, bf16 *dX, cudaStream_t 
   const bf16 *Wt = n->packtb[l];
   int *err = n->tc_err;
   switch (l) {
-    case 1: return conv_tc<32, 16, 2, false, false>(G, Wt, 16, 0, nullptr, 0, dX, 16, 16, W, H, D, err, st);
-    case 2: return conv_tc<64, 32, 1, false, false>(G, Wt, 32, 0, nullptr, 0, dX, 32, 32, W, H, D, err, st);
+    case 1: return conv_tc<32, 16, 4, 8, false, false>(G, Wt, 16, 0, nullptr, 0, dX, 16, 16, W, H, D, err, st);
+    case 2: return conv_tc<64, 32, 3, 8, false, false>(G, Wt, 32, 0, nullptr, 0, dX, 32, 32, W, H, D, err, st);
     case 3: {
-      cudaError_t e = conv_tc<64, 32, 1, false, false>(G, Wt, 64, 0, nullptr, 0, dX, 64, 32, W, H, D, err, st);
+      cudaError_t e = conv_tc<64, 32, 3, 8, false, false>(G, Wt, 64, 0, nullptr, 0, dX, 64, 32, W, H, D, err, st);
       if (e != cudaSuccess) return e;
-      return conv_tc<64, 32, 1, false, false>(G, Wt, 64, 32, nullptr, 0, dX, 64, 32, W, H, D, err, st);
+      return conv_tc<64, 32, 3, 8, false, false>(G, Wt, 64, 32, nullptr, 0, dX, 64, 32, W, H, D, err, st);
     }
-    case 4: return conv_tc<32, 64, 2, false, false>(G, Wt, 64, 0, nullptr, 0, dX, 64, 64, W, H, D, err, st);
-    case 5: return conv_tc<16, 32, 2, false, false>(G, Wt, 32, 0, nullptr, 0, dX, 32, 32, W, H, D, err, st);
-    case 6: return conv_tc<16, 16, 2, false, false>(G, Wt, 16, 0, nullptr, 0, dX, 16, 16, W, H, D, err, st);
+    case 4: return conv_tc<32, 64, 4, 4, false, false>(G, Wt, 64, 0, nullptr, 0, dX, 64, 64, W, H, D, err, st);
+    case 5: return conv_tc<16, 32, 4, 4, false, false>(G, Wt, 32, 0, nullptr, 0, dX, 32, 32, W, H, D, err, st);
+    case 6: return conv_tc<16, 16, 4, 8, false, false>(G, Wt, 16, 0, nullptr, 0, dX, 16, 16, W, H, D, err, st);
     default: return cudaErrorInvalidValue;
   }
 }
