@@ -85,7 +85,7 @@ class DsgMgStats(C.Structure):
     """struct dsg_mg_stats."""
     _fields_ = [("mode", C.c_int), ("vcycles", C.c_int), ("fine_sweeps", C.c_int),
                 ("relres_init", C.c_double), ("relres", C.c_double), ("converged", C.c_int),
-                ("fallback", C.c_int), ("epsdiv", C.c_double), ("relres_prev", C.c_double),
+                ("fallback", C.c_int), ("epsdiv", C.c_double), ("relres_base", C.c_double),
                 ("relres_net", C.c_double)]
 
     def as_dict(self):

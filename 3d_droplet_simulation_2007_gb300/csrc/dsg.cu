@@ -439,17 +439,20 @@ int fmg32(dsg_ctx *ctx) {
   return DSG_OK;
 }
 
-// After a solve: store (input features, solved correction) as the attached
-// network's training pair when recording is on.
+// After a solve: the attached network's training pair when recording is on
+// (its input was taken from this solve's start, its target is the solved
+// pressure's correction of that start).
 int record_pair(dsg_ctx *ctx) {
   if (!ctx->net || !ctx->net_record) return DSG_OK;
-  double **F = ctx->lv[ctx->ng];
-  int rc = dsg::nn::net_features(ctx->net, F[0], F[3], ctx->f[DSG_F_PPREV], ctx->f[DSG_F_PPREV2], F[1], F[4],
-                                 F[5], F[6], ctx->fine(),
-                                 ctx->s.lengthsize, ctx->stream);
-  if (rc) return rc;
-  dsg::nn::net_set_target(ctx->net, true, ctx->stream);
-  return DSG_OK;
+  return dsg::nn::net_target(ctx->net, ctx->lv[ctx->ng][1], ctx->fine(), ctx->stream);
+}
+
+// FP32 V-cycles the mixed solve expects to need from relative residual r at
+// the measured reduction per cycle (the count its outer loop would run).
+int cycles_needed(const dsg_ctx *ctx, double r) {
+  if (r < ctx->cfg.tol) return 0;
+  const int n = (int)ceil(log(ctx->cfg.tol / r) / log(ctx->rho_est) + 0.1);
+  return n < 1 ? 1 : n;
 }
 
 int mixed_solve(dsg_ctx *ctx, dsg_mg_stats *s) {
@@ -505,42 +508,10 @@ int mixed_solve(dsg_ctx *ctx, dsg_mg_stats *s) {
   };
   int rc;
   double r;
-  if (ctx->cfg.mode == DSG_MODE_LEARNED) {
-    // Guarded learned start: the previous-step pressure and the network's
-    // guess are both judged by their FP64 defect; the network's guess is kept
-    // only if it has the smaller relative residual.
-    if (!ctx->net) return dsg::set_error(ctx, DSG_E_STATE, "learned mode without an attached network");
-    double **F = ctx->lv[ng];
-    double *p = F[1], *pprev = ctx->f[DSG_F_PPREV], *pprev2 = ctx->f[DSG_F_PPREV2];
-    const size_t bytes = ctx->fine().count() * sizeof(double);
-    rc = coef_hierarchy32(ctx);
-    if (rc) return rc;
-    DSG_CK(ctx, cudaMemcpyAsync(p, pprev, bytes, cudaMemcpyDeviceToDevice, st));
-    double r_prev, r_net;
-    rc = defect_host(ctx, &r_prev);
-    if (rc) return rc;
-    rc = dsg::nn::net_features(ctx->net, F[0], F[3], pprev, pprev2, nullptr, F[4], F[5], F[6], ctx->fine(),
-                               ctx->s.lengthsize, st);
-    if (rc) return rc;
-    rc = dsg::nn::net_guess(ctx->net, p, pprev2, ctx->fine(), st);
-    if (rc) return rc;
-    DSG_CK(ctx, dsg::bc_scalar(p, ctx->fine(), st));
-    rc = defect_host(ctx, &r_net);
-    if (rc) return rc;
-    if (r_net < r_prev) {
-      r = r_net;
-      s->fallback = 0;
-    } else {
-      DSG_CK(ctx, cudaMemcpyAsync(p, pprev, bytes, cudaMemcpyDeviceToDevice, st));
-      rc = defect_host(ctx, &r);
-      if (rc) return rc;
-      s->fallback = 1;
-    }
-    ctx->last_relres_prev = r_prev;
-    ctx->last_relres_net = r_net;
-    s->relres_prev = r_prev;
-    s->relres_net = r_net;
-  } else if (ctx->cfg.warm_start == 1 || ctx->cfg.warm_start == 2) {
+  const bool learned = ctx->cfg.mode == DSG_MODE_LEARNED;
+  if (learned && !ctx->net) return dsg::set_error(ctx, DSG_E_STATE, "learned mode without an attached network");
+  if (ctx->net) dsg::nn::net_begin_solve(ctx->net);
+  if (!learned && (ctx->cfg.warm_start == 1 || ctx->cfg.warm_start == 2)) {
     // previous-step pressure (1) or zero (2) as the initial guess
     rc = coef_hierarchy32(ctx);
     if (rc) return rc;
@@ -557,6 +528,47 @@ int mixed_solve(dsg_ctx *ctx, dsg_mg_stats *s) {
     if (rc) return rc;
     rc = defect_read(ctx, &r);
     if (rc) return rc;
+    double **F = ctx->lv[ng];
+    // the network's input: when it runs this solve, or to record a training pair
+    if (ctx->net && ((learned && ctx->net_rest == 0) || ctx->net_record)) {
+      const FineSplit fs = fine_split(ctx);
+      rc = dsg::nn::net_features(ctx->net, F[0], F[3], F[1], ctx->f[DSG_F_PPREV], fs.r, ctx->red_out, ctx->fine(),
+                                 ctx->s.lengthsize, st);
+      if (rc) return rc;
+    }
+    if (learned) {
+      // Guarded learned start.  The method without the network is this FP32
+      // full-multigrid start; the network predicts its correction, scaled to
+      // the least FP64 defect (one minimal-residual step, whose defect is known
+      // from four sums before p changes).  The correction is kept only if it
+      // cuts the V-cycles the solve expects to need; after a rejection the
+      // network rests for 1, 2, 4 .. 32 solves (reset by an acceptance).
+      s->relres_base = r;
+      s->relres_net = -1.0;
+      s->fallback = 1;
+      if (ctx->net_rest > 0) {
+        ctx->net_rest--;
+      } else {
+        double pred = 0.0, alpha = 0.0;
+        rc = dsg::nn::net_correction(ctx->net, F[4], F[5], F[6], ctx->fine(), &pred, &alpha, st);
+        if (rc) return rc;
+        s->relres_net = pred;
+        if (cycles_needed(ctx, pred) < cycles_needed(ctx, r)) {
+          rc = dsg::nn::net_apply(ctx->net, F[1], alpha, ctx->fine(), st);
+          if (rc) return rc;
+          DSG_CK(ctx, dsg::bc_scalar(F[1], ctx->fine(), st));
+          rc = defect_host(ctx, &r);
+          if (rc) return rc;
+          s->fallback = 0;
+          ctx->net_backoff = 1;
+        } else {
+          ctx->net_rest = ctx->net_backoff;
+          ctx->net_backoff = ctx->net_backoff < 32 ? 2 * ctx->net_backoff : 32;
+        }
+      }
+      ctx->last_relres_base = s->relres_base;
+      ctx->last_relres_net = s->relres_net;
+    }
   }
   s->relres_init = r;
   int n = 0;
@@ -1126,9 +1138,6 @@ int dsg::solvelpres_post(dsg_ctx *ctx, int t, dsg_mg_stats *ms_in, int mg_rc, ds
   int rc;
   if ((rc = sync_point(ctx, SP_MG))) return rc;
   DSG_CK(ctx, phase_mark(ctx, 5));
-  if (ctx->net)
-    DSG_CK(ctx, cudaMemcpyAsync(ctx->f[DSG_F_PPREV2], ctx->f[DSG_F_PPREV], d.count() * sizeof(double),
-                                cudaMemcpyDeviceToDevice, st));
   DSG_CK(ctx, cudaMemcpyAsync(ctx->f[DSG_F_PPREV], w1, d.count() * sizeof(double), cudaMemcpyDeviceToDevice, st));
   DSG_CK(ctx, dsg::project(u, v, w, w1, a, b, c, d, st));
   DSG_CK(ctx, dsg::bc_v(u, v, w, ctx->red_partials, d, s.xvel2, st));

@@ -215,13 +215,22 @@ cudaError_t init_drop(double *cc, double *u, double *v, double *w, Dims d, doubl
 struct dsg_net;
 namespace dsg {
 namespace nn {
-// nn.cu: features of the current pressure system into the network input (and
-// the training target when p is given); p = p_prev + network correction.
-int net_features(dsg_net *n, const double *cc, const double *rhs, const double *p1, const double *p2,
-                 const double *p, const double *a, const double *b, const double *c, Dims d, double lengthsize,
-                 cudaStream_t st);
-int net_guess(dsg_net *n, double *p, const double *p2, Dims d, cudaStream_t st);
-void net_set_target(dsg_net *n, bool v, cudaStream_t st);
+// nn.cu: the network at the start of a pressure solve.  net_features: input
+// channels from the start pressure p (the FP32 full-multigrid guess), its
+// defect (r32: the FP32 colour-split copy the defect pass leaves; red = {sum
+// r^2, sum rhs^2} in FP64), cc, rhs and the previous pressure; keeps p as the
+// base of the training target.  net_correction: forward pass
+// and the minimal-residual step along the network's correction e of p: the
+// best alpha and the relative defect of p + alpha e (synchronises the
+// stream).  net_apply: p += alpha e.  net_target: after the solve, the
+// training pair (p_solved - p_start, in the network's units).
+int net_features(dsg_net *n, const double *cc, const double *rhs, const double *p, const double *pprev,
+                 const float *const r32[2], const double *red, Dims d, double lengthsize, cudaStream_t st);
+int net_correction(dsg_net *n, const double *a, const double *b, const double *c, Dims d, double *relres_pred,
+                   double *alpha, cudaStream_t st);
+int net_apply(dsg_net *n, double *p, double alpha, Dims d, cudaStream_t st);
+int net_target(dsg_net *n, const double *p, Dims d, cudaStream_t st);
+void net_begin_solve(dsg_net *n);
 }  // namespace nn
 }  // namespace dsg
 
@@ -275,8 +284,10 @@ struct dsg_ctx {
   GraphRec *cap = nullptr;            // graph under capture
   dsg_net *net = nullptr;             // learned initial guess (DSG_MODE_LEARNED)
   int net_record = 0;                 // store a training pair after every solve
-  double last_relres_prev = -1.0;     // learned mode: relres of the previous pressure
-  double last_relres_net = -1.0;      // learned mode: relres of the network's guess
+  double last_relres_base = -1.0;     // learned mode: relres of the FP32 full-multigrid start
+  double last_relres_net = -1.0;      // learned mode: predicted relres of the corrected start
+  int net_rest = 0;                   // learned mode: solves left without the network
+  int net_backoff = 1;                // learned mode: rest after the next rejection (1, 2, 4 .. 32)
   std::vector<cudaEvent_t> phase_ev;  // phase markers of dsg_step (event pool)
   std::vector<int> phase_id;          // phase that starts at each marker, -1 = end
   size_t phase_used = 0;

@@ -687,18 +687,54 @@ __global__ void k_adam(float *__restrict__ p, const float *__restrict__ g, float
   }
 }
 
-// Network input from the solver fields (interior cells, channels-last, 16 padded
-// channels): c0 = volume fraction, c1 = rhs / s_r, c2 = (rhs - L p1) / s_r,
-// c3 = p1 / s_p, c4 = p2 / s_p, where p1, p2 are the pressures of the last two
-// steps, s_r = RMS(rhs) and s_p = RMS(p1) (sums[0], sums[1] in device memory).
-// With p given (training snapshots) also writes the FP32 target (p - p2) / s_p.
-// The pressure alternates in sign from step to step (the off-diagonal stresses
-// carry over with a sign flip, main.f:3291-3300), so p2 is the closer base.
-__global__ void k_features(bf16 *__restrict__ Xin, float *__restrict__ target, const double *__restrict__ cc,
-                           const double *__restrict__ rhs, const double *__restrict__ p1,
-                           const double *__restrict__ p2, const double *__restrict__ p,
-                           const double *__restrict__ a, const double *__restrict__ b,
-                           const double *__restrict__ c, const double *__restrict__ sums, Dims d, double h2i) {
+// ---- the network at the start of a pressure solve --------------------------------
+// The start p is the FP32 full-multigrid guess; r = rhs - L p is its FP64
+// defect as the solver's defect pass leaves it: rounded to FP32 in the
+// colour-split layout of the finest FP32 level (r_ev / r_od, cell (i, j, k)
+// in the half with parity (i + j + k) & 1 at index sp.at((i - 2) / 2, j, k)),
+// with red = {sum r^2, sum rhs^2} over the interior in FP64.
+// Slots of the network's sums (sums_dev): [0] sum p^2, [1] the correction
+// scale h^2 RMS(r), [2..4] sums of the minimal-residual step, [5] sum rhs^2,
+// [6] RMS(r); from [10] on, as floats: 1 / RMS(r), 1 / RMS(rhs), 1 / RMS(p).
+constexpr int kScaleF = 20;  // float index of the reciprocal scales
+
+// Index into one colour half of the finest FP32 level (the layout of the
+// mixed solve: hx = (nx - 2) / 2 cells per row, rows of the interior).
+struct Split {
+  int hx, ny2, nz2;
+  __device__ __forceinline__ size_t at(int m, int j, int k) const {
+    return (size_t)m + (size_t)hx * ((size_t)(j - 2) + (size_t)ny2 * (size_t)(k - 2));
+  }
+};
+
+__device__ __forceinline__ float split_at(const float *__restrict__ r_ev, const float *__restrict__ r_od, Split sp,
+                                          int i, int j, int k) {
+  return (((i + j + k) & 1) ? r_od : r_ev)[sp.at((i - 2) >> 1, j, k)];
+}
+
+// The scales of one solve's start (one thread).
+__global__ void k_scales(double *__restrict__ sums, const double *__restrict__ red, double n_int, double h2) {
+  if (threadIdx.x != 0) return;
+  const double s_r = sqrt(red[0] / n_int) + 1e-300;
+  const double s_b = sqrt(red[1] / n_int) + 1e-300;
+  const double s_p = sqrt(sums[0] / n_int) + 1e-300;
+  sums[1] = h2 * s_r;
+  sums[5] = red[1];
+  sums[6] = s_r;
+  float *f = reinterpret_cast<float *>(sums);
+  f[kScaleF] = (float)(1.0 / s_r);
+  f[kScaleF + 1] = (float)(1.0 / s_b);
+  f[kScaleF + 2] = (float)(1.0 / s_p);
+}
+
+// Input channels: cc, rhs / RMS(rhs), r / RMS(r), p / RMS(p), pprev / RMS(p);
+// pbase keeps p in FP32 as the base of the training target.  The network
+// predicts the correction of p in units of h^2 RMS(r) (the correction scales
+// with the defect).
+__global__ void k_features(bf16 *__restrict__ Xin, float *__restrict__ pbase, const float *__restrict__ r_ev,
+                           const float *__restrict__ r_od, Split sp, const double *__restrict__ cc,
+                           const double *__restrict__ rhs, const double *__restrict__ p,
+                           const double *__restrict__ pprev, const double *__restrict__ sums, Dims d) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
@@ -706,48 +742,84 @@ __global__ void k_features(bf16 *__restrict__ Xin, float *__restrict__ target, c
   if (x >= W || y >= H) return;
   const int i = x + 2, j = y + 2, k = z + 2;
   const size_t q = d.ix(i, j, k);
-  const size_t sy = d.sy(), sz = d.sz();
-  const double n_int = (double)W * H * (d.nz - 2);
-  const double sr = sqrt(sums[0] / n_int) + 1e-300;
-  const double sp = sqrt(sums[1] / n_int) + 1e-300;
-  const double uc = p1[q];
-  const double xp = (i + 1 == d.nx) ? 0.0 : p1[q + 1];
-  const double xm = (i - 1 == 1) ? uc : p1[q - 1];
-  const double yp = (j + 1 == d.ny) ? uc : p1[q + sy];
-  const double ym = (j - 1 == 1) ? uc : p1[q - sy];
-  const double zp = (k + 1 == d.nz) ? uc : p1[q + sz];
-  const double zm = (k - 1 == 1) ? uc : p1[q - sz];
-  const double r = -h2i * (a[q] * (xp - uc) + a[q - 1] * (xm - uc) + b[q] * (yp - uc) + b[q - sy] * (ym - uc) +
-                           c[q] * (zp - uc) + c[q - sz] * (zm - uc)) +
-                   rhs[q];
+  const float *f = reinterpret_cast<const float *>(sums);
+  const float ir = f[kScaleF], ib = f[kScaleF + 1], ip = f[kScaleF + 2];
+  const float pc = (float)p[q];
   const size_t v = ((size_t)z * H + y) * W + x;
-  bf16 *o = Xin + v * 16;
-  o[0] = __float2bfloat16((float)cc[q]);
-  o[1] = __float2bfloat16((float)(rhs[q] / sr));
-  o[2] = __float2bfloat16((float)(r / sr));
-  o[3] = __float2bfloat16((float)(uc / sp));
-  o[4] = __float2bfloat16((float)(p2[q] / sp));
-#pragma unroll
-  for (int ch = 5; ch < 16; ch++) o[ch] = __float2bfloat16(0.f);
-  if (target) target[v] = (float)((p[q] - p2[q]) / sp);
+  uint4 o[2] = {make_uint4(0u, 0u, 0u, 0u), make_uint4(0u, 0u, 0u, 0u)};
+  __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(o);
+  h[0] = __floats2bfloat162_rn((float)cc[q], (float)rhs[q] * ib);
+  h[1] = __floats2bfloat162_rn(split_at(r_ev, r_od, sp, i, j, k) * ir, pc * ip);
+  h[2] = __floats2bfloat162_rn((float)pprev[q] * ip, 0.f);
+  uint4 *dst = reinterpret_cast<uint4 *>(Xin + v * 16);
+  dst[0] = o[0];
+  dst[1] = o[1];
+  pbase[v] = pc;
 }
 
-// p = p2 + s_p q over the interior (q = network output, channel 0 of 8).
-__global__ void k_apply_guess(double *__restrict__ p, const double *__restrict__ p2, const float *__restrict__ qout,
-                              const double *__restrict__ sums, Dims d) {
+// Training target after the solve: (p - pbase) / scale over the interior.
+__global__ void k_target(float *__restrict__ target, const double *__restrict__ p, const float *__restrict__ pbase,
+                         const double *__restrict__ sums, Dims d) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
   const int W = d.nx - 2, H = d.ny - 2;
   if (x >= W || y >= H) return;
-  const double sp = sqrt(sums[1] / ((double)W * H * (d.nz - 2))) + 1e-300;
-  const size_t q = d.ix(x + 2, y + 2, z + 2);
   const size_t v = ((size_t)z * H + y) * W + x;
-  p[q] = p2[q] + sp * (double)qout[v * 8];
+  target[v] = (float)((p[d.ix(x + 2, y + 2, z + 2)] - (double)pbase[v]) / sums[1]);
 }
 
-// *sums += sum of f^2 over the interior (block partials, one atomic per block).
-__global__ void k_sumsq(const double *__restrict__ f, double *__restrict__ sums, Dims d) {
+// Block partials of the minimal-residual step along the network's correction
+// e = h^2 RMS(r) q (q = channel 0 of the output): L e = RMS(r) l with
+// l = sum over the six faces of coefficient x (q_neighbour - q) under the
+// solver's operator and boundary rules (main.f resid), evaluated in FP32.
+// partials[3B..3B+2] = sums of r r, r l, l l over the block's cells; the
+// defect of p + alpha e is r - alpha RMS(r) l.
+__global__ void k_line_partials(double *__restrict__ partials, const float *__restrict__ r_ev,
+                                const float *__restrict__ r_od, Split sp, const double *__restrict__ a,
+                                const double *__restrict__ b, const double *__restrict__ c,
+                                const float *__restrict__ qout, Dims d) {
+  const int W = d.nx - 2, H = d.ny - 2;
+  const size_t n = (size_t)W * H * (d.nz - 2);
+  const size_t sy = d.sy(), sz = d.sz();
+  const size_t vy = (size_t)W, vz = (size_t)W * H;
+  float rr = 0.f, rl = 0.f, ll = 0.f;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    const unsigned ni = (unsigned)W, nj = (unsigned)H, t32 = (unsigned)t;  // < 2^32 cells
+    const unsigned rem = t32 / ni, kk = rem / nj;
+    const int i = (int)(t32 - rem * ni) + 2;
+    const int j = (int)(rem - kk * nj) + 2, k = (int)kk + 2;
+    const size_t q = d.ix(i, j, k);
+    const float r = split_at(r_ev, r_od, sp, i, j, k);
+    const float *qv = qout + t * 8;
+    const float ec = qv[0];
+    const float ex = (i + 1 == d.nx) ? 0.f : qv[8];
+    const float exm = (i - 1 == 1) ? ec : qv[-8];
+    const float ey = (j + 1 == d.ny) ? ec : qv[8 * vy];
+    const float eym = (j - 1 == 1) ? ec : qv[-(ptrdiff_t)(8 * vy)];
+    const float ez = (k + 1 == d.nz) ? ec : qv[8 * vz];
+    const float ezm = (k - 1 == 1) ? ec : qv[-(ptrdiff_t)(8 * vz)];
+    const float l = (float)a[q] * (ex - ec) + (float)a[q - 1] * (exm - ec) + (float)b[q] * (ey - ec) +
+                    (float)b[q - sy] * (eym - ec) + (float)c[q] * (ez - ec) + (float)c[q - sz] * (ezm - ec);
+    rr += r * r;
+    rl += r * l;
+    ll += l * l;
+  }
+  __shared__ double sh[3][256];
+  sh[0][threadIdx.x] = rr;
+  sh[1][threadIdx.x] = rl;
+  sh[2][threadIdx.x] = ll;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (threadIdx.x < s)
+      for (int m = 0; m < 3; m++) sh[m][threadIdx.x] += sh[m][threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x < 3) partials[3 * blockIdx.x + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+// Block partials of sum f^2 over the interior (partials[B]).
+__global__ void k_sumsq_partials(double *__restrict__ partials, const double *__restrict__ f, Dims d) {
   __shared__ double sh[256];
   const size_t n = (size_t)(d.nx - 2) * (d.ny - 2) * (d.nz - 2);
   double s = 0.0;
@@ -765,7 +837,36 @@ __global__ void k_sumsq(const double *__restrict__ f, double *__restrict__ sums,
     if (threadIdx.x < k) sh[threadIdx.x] += sh[threadIdx.x + k];
     __syncthreads();
   }
-  if (threadIdx.x == 0) atomicAdd(sums, sh[0]);
+  if (threadIdx.x == 0) partials[blockIdx.x] = sh[0];
+}
+
+// out[m] = sum over nb blocks of partials[w * B + m], m < w (one block, fixed order).
+__global__ void k_fold(double *__restrict__ out, const double *__restrict__ partials, int nb, int w) {
+  __shared__ double sh[256];
+  for (int m = 0; m < w; m++) {
+    double s = 0.0;
+    for (int q = threadIdx.x; q < nb; q += blockDim.x) s += partials[(size_t)q * w + m];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int k = 128; k > 0; k >>= 1) {
+      if (threadIdx.x < k) sh[threadIdx.x] += sh[threadIdx.x + k];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[m] = sh[0];
+    __syncthreads();
+  }
+}
+
+// p += alpha h^2 RMS(r) q over the interior.
+__global__ void k_apply_corr(double *__restrict__ p, const float *__restrict__ qout,
+                             const double *__restrict__ sums, double alpha, Dims d) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  const int W = d.nx - 2, H = d.ny - 2;
+  if (x >= W || y >= H) return;
+  const size_t v = ((size_t)z * H + y) * W + x;
+  p[d.ix(x + 2, y + 2, z + 2)] += alpha * sums[1] * (double)qout[v * 8];
 }
 
 inline int eblocks(size_t n) { return (int)((n + 255) / 256 < 8192 ? (n + 255) / 256 : 8192); }
@@ -798,8 +899,13 @@ struct dsg_net {
   float *tmp;                       // FP32 gradient of a decoder output
   float *wscratch;                  // bias (64) + padded weight gradient of one layer
   float *xin_f32, *yhost_f32;       // staging of the host-array entry points
-  double *loss_dev, *sums_dev;      // loss; sums of rhs^2 and p1^2 of the current system
-  double *loss_host;
+  double *loss_dev;                 // loss
+  double *sums_dev;                 // scales and sums of the current solve's start (see k_scales)
+  double *partials;                 // block partials of the reductions (kRedBlocks x 4)
+  float *pbase;                     // start pressure of the current solve (FP32, interior)
+  double *loss_host, *line_host;    // pinned mirrors
+  const float *r32[2] = {nullptr, nullptr};  // FP32 split defect of the current solve's start
+  bool have_features = false;       // x0 / pbase / scale hold the current solve's start
   long long step = 0;               // Adam steps taken
   bool have_target = false;         // a training pair is recorded
   cudaStream_t stream = 0;          // stream of the attached context (training)
@@ -1140,37 +1246,68 @@ namespace nn {
 
 // Solver hooks (used by dsg.cu): features of the current pressure system into
 // the network input; optional training target from the solved pressure.
-int net_features(dsg_net *n, const double *cc, const double *rhs, const double *p1, const double *p2,
-                 const double *p, const double *a, const double *b, const double *c, Dims d, double lengthsize,
-                 cudaStream_t st) {
+int net_features(dsg_net *n, const double *cc, const double *rhs, const double *p, const double *pprev,
+                 const float *const r32[2], const double *red, Dims d, double lengthsize, cudaStream_t st) {
   if (n->W[0] != d.nx - 2 || n->H[0] != d.ny - 2 || n->D[0] != d.nz - 2)
     return dsg::set_error(nullptr, DSG_E_ARG, "network sized %dx%dx%d, grid interior %dx%dx%d", n->W[0], n->H[0],
                           n->D[0], d.nx - 2, d.ny - 2, d.nz - 2);
   const double h1 = lengthsize / (d.nx - 2);
-  NCK(n, cudaMemsetAsync(n->sums_dev, 0, 2 * sizeof(double), st));
-  DSG_COUNT k_sumsq<<<1216, 256, 0, st>>>(rhs, n->sums_dev, d);
-  DSG_COUNT k_sumsq<<<1216, 256, 0, st>>>(p1, n->sums_dev + 1, d);
+  const Split sp{(d.nx - 2) >> 1, d.ny - 2, d.nz - 2};
+  DSG_COUNT k_sumsq_partials<<<kRedBlocks, 256, 0, st>>>(n->partials, p, d);
+  DSG_COUNT k_fold<<<1, 256, 0, st>>>(n->sums_dev, n->partials, kRedBlocks, 1);
+  DSG_COUNT k_scales<<<1, 32, 0, st>>>(n->sums_dev, red, (double)(d.nx - 2) * (d.ny - 2) * (d.nz - 2), h1 * h1);
   const dim3 blk(32, 8), grid((unsigned)((d.nx - 2 + 31) / 32), (unsigned)((d.ny - 2 + 7) / 8), (unsigned)(d.nz - 2));
-  DSG_COUNT k_features<<<grid, blk, 0, st>>>(n->x0, p ? n->target : nullptr, cc, rhs, p1, p2, p, a, b, c,
-                                             n->sums_dev, d, 1.0 / (h1 * h1));
+  DSG_COUNT k_features<<<grid, blk, 0, st>>>(n->x0, n->pbase, r32[0], r32[1], sp, cc, rhs, p, pprev, n->sums_dev, d);
   NCK(n, cudaGetLastError());
+  n->r32[0] = r32[0];
+  n->r32[1] = r32[1];
+  n->have_features = true;
   return DSG_OK;
 }
 
-// p = p2 + s_p net(x) on the interior (features must be current).
-int net_guess(dsg_net *n, double *p, const double *p2, Dims d, cudaStream_t st) {
+int net_target(dsg_net *n, const double *p, Dims d, cudaStream_t st) {
+  if (!n->have_features) return DSG_OK;
+  const dim3 blk(32, 8), grid((unsigned)((d.nx - 2 + 31) / 32), (unsigned)((d.ny - 2 + 7) / 8), (unsigned)(d.nz - 2));
+  DSG_COUNT k_target<<<grid, blk, 0, st>>>(n->target, p, n->pbase, n->sums_dev, d);
+  NCK(n, cudaGetLastError());
+  n->have_target = true;
+  n->stream = st;
+  return DSG_OK;
+}
+
+int net_correction(dsg_net *n, const double *a, const double *b, const double *c, Dims d, double *relres_pred,
+                   double *alpha, cudaStream_t st) {
+  if (!n->have_features) return dsg::set_error(nullptr, DSG_E_STATE, "network features not computed");
   int rc = forward(n, st);
   if (rc) return rc;
+  const Split sp{(d.nx - 2) >> 1, d.ny - 2, d.nz - 2};
+  DSG_COUNT k_line_partials<<<kRedBlocks, 256, 0, st>>>(n->partials, n->r32[0], n->r32[1], sp, a, b, c, n->yout, d);
+  DSG_COUNT k_fold<<<1, 256, 0, st>>>(n->sums_dev + 2, n->partials, kRedBlocks, 3);
+  NCK(n, cudaMemcpyAsync(n->line_host, n->sums_dev, 8 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  NCK(n, cudaStreamSynchronize(st));
+  rc = check_tc(n);
+  if (rc) return rc;
+  const double *h = n->line_host;
+  const double s_r = h[6], rr = h[2], rt = s_r * h[3], tt = s_r * s_r * h[4], bb = h[5];
+  if (!isfinite(rr) || !isfinite(rt) || !isfinite(tt) || !isfinite(bb))
+    return dsg::set_error(nullptr, DSG_E_NONFINITE, "non-finite network correction (%g, %g, %g)", rr, rt, tt);
+  // defect of p + alpha e: |r - alpha t|^2 = rr - 2 alpha rt + alpha^2 tt, least at alpha = rt / tt
+  *alpha = tt > 0.0 ? rt / tt : 0.0;
+  double left = tt > 0.0 ? rr - rt * rt / tt : rr;
+  if (left < 0.0) left = 0.0;
+  *relres_pred = bb > 0.0 ? sqrt(left) / sqrt(bb) : sqrt(left);
+  return DSG_OK;
+}
+
+int net_apply(dsg_net *n, double *p, double alpha, Dims d, cudaStream_t st) {
   const dim3 blk(32, 8), grid((unsigned)((d.nx - 2 + 31) / 32), (unsigned)((d.ny - 2 + 7) / 8), (unsigned)(d.nz - 2));
-  DSG_COUNT k_apply_guess<<<grid, blk, 0, st>>>(p, p2, n->yout, n->sums_dev, d);
+  DSG_COUNT k_apply_corr<<<grid, blk, 0, st>>>(p, n->yout, n->sums_dev, alpha, d);
   NCK(n, cudaGetLastError());
   return DSG_OK;
 }
 
-void net_set_target(dsg_net *n, bool v, cudaStream_t st) {
-  n->have_target = v;
-  n->stream = st;
-}
+void net_begin_solve(dsg_net *n) { n->have_features = false; }
+
 
 }  // namespace nn
 }  // namespace dsg
@@ -1238,11 +1375,14 @@ int dsg_net_create(int W, int H, int D, uint64_t seed, dsg_net **out) {
   plan.push_back({(void **)&n->yhost_f32, up(v0 * 4)});
   plan.push_back({(void **)&n->loss_dev, 256});
   plan.push_back({(void **)&n->sums_dev, 256});
+  plan.push_back({(void **)&n->partials, up((size_t)dsg::kRedBlocks * 4 * sizeof(double))});
+  plan.push_back({(void **)&n->pbase, up(v0 * 4)});
   size_t total = 0;
   for (auto &e : plan) total += e.second;
   cudaError_t e = cudaMalloc(&n->arena, total);
   if (e == cudaSuccess) e = cudaMemset(n->arena, 0, total);
   if (e == cudaSuccess) e = cudaMallocHost(&n->loss_host, sizeof(double));
+  if (e == cudaSuccess) e = cudaMallocHost(&n->line_host, 8 * sizeof(double));
   if (e != cudaSuccess) {
     int rc = net_fail(n, e, "dsg_net_create");
     dsg_net_destroy(n);
@@ -1285,6 +1425,7 @@ void dsg_net_destroy(dsg_net *n) {
   if (!n) return;
   if (n->arena) cudaFree(n->arena);
   if (n->loss_host) cudaFreeHost(n->loss_host);
+  if (n->line_host) cudaFreeHost(n->line_host);
   delete n;
 }
 

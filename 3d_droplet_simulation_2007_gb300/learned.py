@@ -1,20 +1,21 @@
 """The learned multigrid initial guess: host wrapper and training driver.
 
-A ``Net`` is the 3D convolutional U-Net of ``csrc/nn.cu`` (BF16 tensor-core
-kernels, FP32 accumulation) sized for one interior grid.  ``train`` runs the
-solver itself on droplets of random diameter (1-3 mm) and impact speed
-(0.5-4 m/s), records after every pressure solve the pair (features of the
-system, solved pressure) and takes one Adam step on it: the network learns
-from the solver's own snapshots, on the fly.  Training runs at 128^3 and is
-then continued at the grid the network will serve (the parameters carry over
-between grid sizes: the network is convolutional).
+A ``Net`` is the 3D convolutional U-Net of ``csrc/nn.cu`` (BF16 tcgen05
+tensor-core kernels, FP32 accumulation) sized for one interior grid.  The
+method without it starts every mixed-precision pressure solve from the FP32
+full-multigrid (FMG) guess p0; the network predicts the correction of p0 --
+from the volume fraction (density), the divergence right-hand side, the FP64
+defect of p0, p0 itself and the previous-step pressure -- and in
+``MODE_LEARNED`` the solver adds it, scaled to the least FP64 defect, only
+when that cuts the V-cycles it expects to need (otherwise it keeps p0 and
+rests the network for 1, 2, 4 .. 32 solves).
 
-The pressure of this scheme alternates in sign from step to step (the
-off-diagonal stresses carry over between steps with a sign flip,
-main.f:3291-3300), so the network sees the last two pressures p1, p2 and
-predicts the correction of p2.  In ``MODE_LEARNED`` the solver keeps the
-network's guess only if its FP64 residual is below that of the previous-step
-pressure p1, the guess it falls back to.
+``train`` runs the solver itself on droplets of random diameter (1-3 mm) and
+impact speed (0.5-4 m/s), records after every pressure solve the pair
+(features at the start, solved pressure minus p0) and takes one Adam step on
+it: the network learns from the solver's own snapshots, on the fly.  Training
+runs at 128^3 and is then continued at the grid the network will serve (the
+parameters carry over between grid sizes: the network is convolutional).
 """
 import ctypes as C
 import os
@@ -160,7 +161,7 @@ def evaluate(inp, net=None, steps=8, warmup=2):
     residuals, guard fallbacks and ms per step."""
     import time
     from .solver import Solver
-    keys = ("vcycles", "relres_init", "fallback", "relres_net", "relres_prev")
+    keys = ("vcycles", "relres_init", "fallback", "relres_net", "relres_base")
     out = {k: [] for k in keys}
     with Solver(inp) as s:
         if net is not None:
@@ -181,8 +182,9 @@ def evaluate(inp, net=None, steps=8, warmup=2):
 
 
 def compare_starts(n, net, steps=8, warmup=20, speed=3.0, diameter=2e-3, seed=0):
-    """V-cycles and time per step at n^3 from the FP32 full-multigrid start,
-    from the previous-step pressure, and from the guarded learned guess."""
+    """V-cycles and time per step at n^3 from the FP32 full-multigrid start
+    (the method without the network), from the previous-step pressure, and
+    from the guarded learned correction of the full-multigrid start."""
     base = droplet(n, steps=1000, impact_speed=speed, diameter=diameter, noise_si=1e-4, mode=MODE_TOL_MIXED,
                    tol=1e-8, npre=4, npost=4, ntop=4, seed=seed)
     return {"fmg_start": evaluate(base, steps=steps, warmup=warmup),

@@ -53,7 +53,7 @@ enum {
   DSG_F_S11 = 11, DSG_F_S22 = 12, DSG_F_S33 = 13, DSG_F_S12 = 14, DSG_F_S13 = 15, DSG_F_S23 = 16,
   DSG_F_RHON = 17, DSG_F_MUN = 18,
   DSG_F_PPREV = 19, /* previous-step pressure (build addition: the reference keeps none) */
-  DSG_F_PPREV2 = 20, /* pressure of two steps back (kept while a network is attached) */
+  DSG_F_PPREV2 = 20, /* spare fine array (not written by the step) */
   DSG_F_KTUR = 21,  /* k-epsilon state (iturb = 3), COMMON /turbulence/ input.h:36-42 */
   DSG_F_EPS = 22,
   DSG_F_MUT = 23,
@@ -132,10 +132,11 @@ typedef struct dsg_mg_stats {
   double relres_init; /* relative residual of the initial guess (FMG or learned) */
   double relres;      /* final relative residual (-1 in ref_exact mode) */
   int converged;      /* 1 if relres < tol (tol modes) */
-  int fallback;       /* 1 if the learned guess was rejected for the previous-step pressure */
+  int fallback;       /* learned mode: 1 if the solve started from the FP32 full-multigrid guess alone
+                         (the network's correction was rejected, or the network rested) */
   double epsdiv;      /* h*max|div| of the adaptivity check, -1 if not run this step */
-  double relres_prev; /* learned mode: relres of the previous-step pressure as a guess */
-  double relres_net;  /* learned mode: relres of the network's guess */
+  double relres_base; /* learned mode: relres of the FP32 full-multigrid start (the method without it) */
+  double relres_net;  /* learned mode: relres of that start with the network's correction, -1 if not run */
 } dsg_mg_stats;
 
 typedef struct dsg_ctx dsg_ctx;
@@ -224,13 +225,13 @@ int64_t dsg_launch_count(void);
 
 /* ---- learned initial guess (no reference counterpart) ----------------------
  * A 3D convolutional U-Net (4 levels, 16/32/64/64 channels, 3x3x3 kernels,
- * 251649 parameters, BF16 weights/activations, FP32 accumulation, tensor-core
- * implicit-GEMM kernels) predicting the pressure from DSG_NET_INPUTS channels:
- * the volume fraction (density), the divergence right-hand side, the defect
- * of the previous pressure p1 under the current operator, p1 and the pressure
- * of two steps back p2.  Its output is the correction of p2 in units of
- * RMS(p1).  A network is sized for one interior grid W x H x D (each a
- * multiple of 8). */
+ * 251649 parameters, BF16 weights/activations, FP32 accumulation, tcgen05
+ * tensor-core implicit-GEMM kernels) predicting the correction of the FP32
+ * full-multigrid start p0 of a pressure solve from DSG_NET_INPUTS channels:
+ * the volume fraction (density), the divergence right-hand side, the FP64
+ * defect of p0, p0 and the previous-step pressure.  Its output is in units of
+ * h^2 RMS(defect of p0).  A network is sized for one interior grid W x H x D
+ * (each a multiple of 8). */
 #define DSG_NET_INPUTS 5
 typedef struct dsg_net dsg_net;
 int64_t dsg_net_param_count(void);
@@ -248,9 +249,12 @@ int dsg_net_grad_host(dsg_net *net, const float *x, const float *t, float *loss,
 /* one Adam step on the training pair recorded by the attached context */
 int dsg_net_train_step(dsg_net *net, float lr, float *loss);
 /* Attach a network to a context (NULL detaches).  record=1: after every
- * pressure solve the context stores (input, solved correction) as the net's
- * training pair.  DSG_MODE_LEARNED uses the attached network for its initial
- * guess. */
+ * mixed-precision pressure solve the context stores (input at the start,
+ * solved pressure minus the start) as the net's training pair.
+ * DSG_MODE_LEARNED adds the network's correction to the full-multigrid start,
+ * scaled to the least FP64 defect, when that cuts the V-cycles the solve
+ * expects to need; otherwise it starts from the full-multigrid guess alone
+ * and rests the network for 1, 2, 4 .. 32 solves. */
 int dsg_attach_net(dsg_ctx *ctx, dsg_net *net, int record);
 
 /* ---- array-level kernels (device pointers, reference argument lists) ----
