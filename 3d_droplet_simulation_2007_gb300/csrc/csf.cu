@@ -119,9 +119,45 @@ __global__ void k_bct_z(double *__restrict__ s33, double *__restrict__ s13, doub
   s23[d.ix(i, j, d.nz)] = 0.0;
 }
 
+// The off-diagonal part of bc_tensor alone: the constant faces of S12, S13,
+// S23 that k_bct_x/y/z write (the same cells and values).
+__global__ void k_bct_off_x(double *__restrict__ s12, double *__restrict__ s13, Dims d) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 2;
+  const int k = blockIdx.y * blockDim.y + threadIdx.y + 2;
+  if (j > d.ny - 1 || k > d.nz - 1) return;
+  s12[d.ix(d.nx, j, k)] = 0.0;
+  s13[d.ix(d.nx, j, k)] = 0.0;
+}
+
+__global__ void k_bct_off_y(double *__restrict__ s12, double *__restrict__ s23, Dims d) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int k = blockIdx.y * blockDim.y + threadIdx.y + 2;
+  if (i > d.nx || k > d.nz - 1) return;
+  s12[d.ix(i, d.ny, k)] = 0.0;
+  s23[d.ix(i, d.ny, k)] = 0.0;
+}
+
+__global__ void k_bct_off_z(double *__restrict__ s13, double *__restrict__ s23, Dims d) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (i > d.nx || j > d.ny) return;
+  s13[d.ix(i, j, 2)] = 0.0;
+  s13[d.ix(i, j, d.nz)] = 0.0;
+  s23[d.ix(i, j, 2)] = 0.0;
+  s23[d.ix(i, j, d.nz)] = 0.0;
+}
+
 const dim3 kBlk(32, 4, 1);
 
 }  // namespace
+
+cudaError_t bc_tensor_offdiag(double *s12, double *s13, double *s23, Dims d, cudaStream_t st) {
+  const dim3 b2(32, 8);
+  DSG_COUNT k_bct_off_x<<<dim3((d.ny + 31) / 32, (d.nz + 7) / 8), b2, 0, st>>>(s12, s13, d);
+  DSG_COUNT k_bct_off_y<<<dim3((d.nx + 31) / 32, (d.nz + 7) / 8), b2, 0, st>>>(s12, s23, d);
+  DSG_COUNT k_bct_off_z<<<dim3((d.nx + 31) / 32, (d.ny + 7) / 8), b2, 0, st>>>(s13, s23, d);
+  return cudaGetLastError();
+}
 
 cudaError_t bc_tensor(double *const S[6], Dims d, cudaStream_t st) {
   // S = {S11, S22, S33, S12, S13, S23}

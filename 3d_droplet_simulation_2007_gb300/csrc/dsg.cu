@@ -1227,6 +1227,8 @@ namespace {
 // bc_tensor zeroes ghost faces of S12, S13, S23; with sigma = 0 all six are
 // zeroed), so they arrive before it; a, b, c and the previous pressures are
 // first touched in the pressure phase.
+bool late_offdiag(const dsg_ctx *ctx) { return ctx->cfg.surfacet == 2 && ctx->s.sigma != 0.0; }
+
 int first_touch(const dsg_ctx *ctx, int f) {
   int order[3];
   sweep_order(ctx->s.tswap + 1 > 3 ? 1 : ctx->s.tswap + 1, order);
@@ -1236,8 +1238,13 @@ int first_touch(const dsg_ctx *ctx, int f) {
         if (order[q] == f - DSG_F_U + 1) return SP_SWEEP1 + q;
       return SP_SWEEP1;
     case DSG_F_S11: case DSG_F_S22: case DSG_F_S33:
-    case DSG_F_S12: case DSG_F_S13: case DSG_F_S23:
       return SP_CFL;
+    case DSG_F_S12: case DSG_F_S13: case DSG_F_S23:
+      // csf (surfacet 2, sigma != 0) only writes their constant bc_tensor
+      // faces, which xfer_hook writes again after a late upload; the
+      // momentum phase reads them first.  Otherwise csf or SGIP may write
+      // their interiors: before it.
+      return late_offdiag(ctx) ? SP_CSF : SP_CFL;
     case DSG_F_A: case DSG_F_B: case DSG_F_C: case DSG_F_PPREV: case DSG_F_PPREV2:
       return SP_CSF;
     default:
@@ -1278,6 +1285,8 @@ struct HostXfer {
   const int *in_fields, *out_fields;
   double *const *out_host;
   bool need[dsg_ctx::kSyncPoints];
+  bool offdiag_late;  // S12/S13/S23 arrive at SP_CSF: their csf faces are written again
+  int last_in;        // last sync point with uploads (-1: none)
 };
 
 // At a sync point: the library's stream waits for the inputs the following
@@ -1286,12 +1295,18 @@ struct HostXfer {
 int xfer_hook(dsg_ctx *ctx, int point, void *arg) {
   const HostXfer &x = *static_cast<const HostXfer *>(arg);
   if (x.need[point]) DSG_CK(ctx, cudaStreamWaitEvent(ctx->stream, ctx->xfer_in_ev[point], 0));
+  if (point == SP_CSF && x.offdiag_late)
+    DSG_CK(ctx, dsg::bc_tensor_offdiag(ctx->f[DSG_F_S12], ctx->f[DSG_F_S13], ctx->f[DSG_F_S23], ctx->fine(),
+                                       ctx->stream));
   bool any = false;
   for (int q = 0; q < x.n_out; q++) any = any || last_write(x.out_fields[q]) == point;
   if (!any) return DSG_OK;
   const size_t bytes = ctx->fine().count() * sizeof(double);
   DSG_CK(ctx, cudaEventRecord(ctx->xfer_out_ev[point], ctx->stream));
   DSG_CK(ctx, cudaStreamWaitEvent(ctx->xfer_out, ctx->xfer_out_ev[point], 0));
+  // the uploads gate the step and the downloads only its end: the link is
+  // left to the uploads until they are all in
+  if (x.last_in >= 0) DSG_CK(ctx, cudaStreamWaitEvent(ctx->xfer_out, ctx->xfer_in_ev[x.last_in], 0));
   for (int q = 0; q < x.n_out; q++)
     if (last_write(x.out_fields[q]) == point)
       DSG_CK(ctx, cudaMemcpyAsync(x.out_host[q], ctx->f[x.out_fields[q]], bytes, cudaMemcpyDeviceToHost,
@@ -1322,7 +1337,7 @@ int dsg_step_host(dsg_ctx *ctx, int t, dsg_mg_stats *stats, int n_in, const int 
   int rc = xfer_resources(ctx);
   if (rc) return rc;
   const size_t bytes = ctx->fine().count() * sizeof(double);
-  HostXfer x{n_in, n_out, in_fields, out_fields, out_host, {}};
+  HostXfer x{n_in, n_out, in_fields, out_fields, out_host, {}, false, -1};
   // the uploads start after the work already queued on the library's stream,
   // in the order the step needs them, one event after each sync point's group
   DSG_CK(ctx, cudaEventRecord(ctx->xfer_start, ctx->stream));
@@ -1333,8 +1348,13 @@ int dsg_step_host(dsg_ctx *ctx, int t, dsg_mg_stats *stats, int n_in, const int 
       if (first_touch(ctx, in_fields[q]) == p) {
         DSG_CK(ctx, cudaMemcpyAsync(ctx->f[in_fields[q]], in_host[q], bytes, cudaMemcpyHostToDevice, ctx->xfer_in));
         x.need[p] = true;
+        const int f = in_fields[q];
+        if (p == SP_CSF && (f == DSG_F_S12 || f == DSG_F_S13 || f == DSG_F_S23)) x.offdiag_late = true;
       }
-    if (x.need[p]) DSG_CK(ctx, cudaEventRecord(ctx->xfer_in_ev[p], ctx->xfer_in));
+    if (x.need[p]) {
+      DSG_CK(ctx, cudaEventRecord(ctx->xfer_in_ev[p], ctx->xfer_in));
+      x.last_in = p;
+    }
   }
   ctx->sync_hook = xfer_hook;
   ctx->sync_arg = &x;

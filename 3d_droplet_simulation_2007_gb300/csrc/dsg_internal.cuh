@@ -131,6 +131,9 @@ cudaError_t swp(const double *us, double *cc, double *vof1, double *vof2, double
 cudaError_t calcrho(double *rhon, double *mun, const double *cc, Dims d, double rho1, double rho2,
                     double mu1, double mu2, cudaStream_t st);
 // csf.cu (S = {S11,S22,S33,S12,S13,S23})
+// The S12/S13/S23 writes of bc_tensor alone (constant faces), for an upload of
+// those fields that lands after csf.
+cudaError_t bc_tensor_offdiag(double *s12, double *s13, double *s23, Dims d, cudaStream_t st);
 cudaError_t bc_tensor(double *const S[6], Dims d, cudaStream_t st);
 cudaError_t csf(const double *ccc, double *w11, double *w22, double *w33, double *ccf, double *const S[6],
                 Dims d, double tau, double sigma, double h, cudaStream_t st);

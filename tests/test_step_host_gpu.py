@@ -3,8 +3,10 @@ copies overlapped with the step's phases, computes the same bits as
 upload + dsg_step + download.
 
 Each input's device copy is overwritten with zeros before the call, and the
-host arrays hold values the step itself overwrites (nonzero ghost faces on the
-stress components, which csf's bc_tensor zeroes; random face coefficients and
+host arrays hold values the step itself overwrites (nonzero ghost faces and
+first interior z-plane on the off-diagonal stresses, which csf's bc_tensor
+zeroes: with surface tension on they arrive after csf and the step writes
+those faces again; random face coefficients and
 previous pressure, which the pressure phase rebuilds), so an input that
 arrived after the first phase touching it would change the result.
 """
@@ -37,6 +39,8 @@ def _perturbed(name, arr, rng):
             a[sl[0], :, :] = 7.0
             a[:, sl[0], :] = 7.0
             a[:, :, sl[0]] = 7.0
+        if name in ("s13", "s23"):
+            a[:, :, 1] = 7.0  # the first interior z-plane, which bc_tensor also zeroes
     elif name in ("a", "b", "c", "pprev"):
         a[...] = rng.uniform(1.0, 2.0, a.shape)
     return np.ascontiguousarray(a.ravel(order="F"))
