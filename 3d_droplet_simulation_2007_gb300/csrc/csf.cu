@@ -89,84 +89,99 @@ __global__ void k_csf_force(double *__restrict__ s11, double *__restrict__ s22, 
   s33[q] = sigh * (fq - fz) * kq;
 }
 
-// bc_tensor, three ordered steps.
-__global__ void k_bct_x(double *__restrict__ s11, double *__restrict__ s12, double *__restrict__ s13, Dims d) {
+// bc_tensor, three ordered steps (every cell two steps write gets the same
+// constant from both, so the steps also split into ranges of planes: the x
+// and y faces of planes kx0 .. kx1-1, the z planes 1, 2 and nz where they
+// lie in kz0 .. kz1-1).
+__global__ void k_bct_x(double *__restrict__ s11, double *__restrict__ s12, double *__restrict__ s13, Dims d, int kx0,
+                        int kx1) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 2;
-  const int k = blockIdx.y * blockDim.y + threadIdx.y + 2;
-  if (j > d.ny - 1 || k > d.nz - 1) return;
+  const int k = blockIdx.y * blockDim.y + threadIdx.y + kx0;
+  if (j > d.ny - 1 || k >= kx1) return;
   s11[d.ix(1, j, k)] = 0.0;
   s12[d.ix(d.nx, j, k)] = 0.0;
   s13[d.ix(d.nx, j, k)] = 0.0;
 }
 
-__global__ void k_bct_y(double *__restrict__ s22, double *__restrict__ s12, double *__restrict__ s23, Dims d) {
+__global__ void k_bct_y(double *__restrict__ s22, double *__restrict__ s12, double *__restrict__ s23, Dims d, int kx0,
+                        int kx1) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  const int k = blockIdx.y * blockDim.y + threadIdx.y + 2;
-  if (i > d.nx || k > d.nz - 1) return;
+  const int k = blockIdx.y * blockDim.y + threadIdx.y + kx0;
+  if (i > d.nx || k >= kx1) return;
   s22[d.ix(i, 1, k)] = s22[d.ix(i, 2, k)];
   s12[d.ix(i, d.ny, k)] = 0.0;
   s23[d.ix(i, d.ny, k)] = 0.0;
 }
 
-__global__ void k_bct_z(double *__restrict__ s33, double *__restrict__ s13, double *__restrict__ s23, Dims d) {
+__global__ void k_bct_z(double *__restrict__ s33, double *__restrict__ s13, double *__restrict__ s23, Dims d, int kz0,
+                        int kz1) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (i > d.nx || j > d.ny) return;
-  s33[d.ix(i, j, 1)] = 0.0;
-  s13[d.ix(i, j, 2)] = 0.0;
-  s13[d.ix(i, j, d.nz)] = 0.0;
-  s23[d.ix(i, j, 2)] = 0.0;
-  s23[d.ix(i, j, d.nz)] = 0.0;
+  if (kz0 <= 1 && 1 < kz1) s33[d.ix(i, j, 1)] = 0.0;
+  if (kz0 <= 2 && 2 < kz1) s13[d.ix(i, j, 2)] = 0.0;
+  if (kz0 <= d.nz && d.nz < kz1) s13[d.ix(i, j, d.nz)] = 0.0;
+  if (kz0 <= 2 && 2 < kz1) s23[d.ix(i, j, 2)] = 0.0;
+  if (kz0 <= d.nz && d.nz < kz1) s23[d.ix(i, j, d.nz)] = 0.0;
 }
 
 // The off-diagonal part of bc_tensor alone: the constant faces of S12, S13,
 // S23 that k_bct_x/y/z write (the same cells and values).
-__global__ void k_bct_off_x(double *__restrict__ s12, double *__restrict__ s13, Dims d) {
+__global__ void k_bct_off_x(double *__restrict__ s12, double *__restrict__ s13, Dims d, int kx0, int kx1) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 2;
-  const int k = blockIdx.y * blockDim.y + threadIdx.y + 2;
-  if (j > d.ny - 1 || k > d.nz - 1) return;
+  const int k = blockIdx.y * blockDim.y + threadIdx.y + kx0;
+  if (j > d.ny - 1 || k >= kx1) return;
   s12[d.ix(d.nx, j, k)] = 0.0;
   s13[d.ix(d.nx, j, k)] = 0.0;
 }
 
-__global__ void k_bct_off_y(double *__restrict__ s12, double *__restrict__ s23, Dims d) {
+__global__ void k_bct_off_y(double *__restrict__ s12, double *__restrict__ s23, Dims d, int kx0, int kx1) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  const int k = blockIdx.y * blockDim.y + threadIdx.y + 2;
-  if (i > d.nx || k > d.nz - 1) return;
+  const int k = blockIdx.y * blockDim.y + threadIdx.y + kx0;
+  if (i > d.nx || k >= kx1) return;
   s12[d.ix(i, d.ny, k)] = 0.0;
   s23[d.ix(i, d.ny, k)] = 0.0;
 }
 
-__global__ void k_bct_off_z(double *__restrict__ s13, double *__restrict__ s23, Dims d) {
+__global__ void k_bct_off_z(double *__restrict__ s13, double *__restrict__ s23, Dims d, int kz0, int kz1) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (i > d.nx || j > d.ny) return;
-  s13[d.ix(i, j, 2)] = 0.0;
-  s13[d.ix(i, j, d.nz)] = 0.0;
-  s23[d.ix(i, j, 2)] = 0.0;
-  s23[d.ix(i, j, d.nz)] = 0.0;
+  if (kz0 <= 2 && 2 < kz1) s13[d.ix(i, j, 2)] = 0.0;
+  if (kz0 <= d.nz && d.nz < kz1) s13[d.ix(i, j, d.nz)] = 0.0;
+  if (kz0 <= 2 && 2 < kz1) s23[d.ix(i, j, 2)] = 0.0;
+  if (kz0 <= d.nz && d.nz < kz1) s23[d.ix(i, j, d.nz)] = 0.0;
 }
 
 const dim3 kBlk(32, 4, 1);
 
 }  // namespace
 
-cudaError_t bc_tensor_offdiag(double *s12, double *s13, double *s23, Dims d, cudaStream_t st) {
+// x and y faces of the interior planes among k0 .. k1-1, and the z planes in
+// that range (k0 = 1, k1 = nz + 1: everything).
+cudaError_t bc_tensor_offdiag(double *s12, double *s13, double *s23, Dims d, cudaStream_t st, int k0, int k1) {
   const dim3 b2(32, 8);
-  DSG_COUNT k_bct_off_x<<<dim3((d.ny + 31) / 32, (d.nz + 7) / 8), b2, 0, st>>>(s12, s13, d);
-  DSG_COUNT k_bct_off_y<<<dim3((d.nx + 31) / 32, (d.nz + 7) / 8), b2, 0, st>>>(s12, s23, d);
-  DSG_COUNT k_bct_off_z<<<dim3((d.nx + 31) / 32, (d.ny + 7) / 8), b2, 0, st>>>(s13, s23, d);
+  const int kx0 = k0 > 2 ? k0 : 2, kx1 = k1 < d.nz ? k1 : d.nz;
+  if (kx1 > kx0) {
+    DSG_COUNT k_bct_off_x<<<dim3((d.ny + 31) / 32, (kx1 - kx0 + 7) / 8), b2, 0, st>>>(s12, s13, d, kx0, kx1);
+    DSG_COUNT k_bct_off_y<<<dim3((d.nx + 31) / 32, (kx1 - kx0 + 7) / 8), b2, 0, st>>>(s12, s23, d, kx0, kx1);
+  }
+  DSG_COUNT k_bct_off_z<<<dim3((d.nx + 31) / 32, (d.ny + 7) / 8), b2, 0, st>>>(s13, s23, d, k0, k1);
   return cudaGetLastError();
 }
 
-cudaError_t bc_tensor(double *const S[6], Dims d, cudaStream_t st) {
+cudaError_t bc_tensor(double *const S[6], Dims d, cudaStream_t st, int k0, int k1) {
   // S = {S11, S22, S33, S12, S13, S23}
   const dim3 b2(32, 8);
-  DSG_COUNT k_bct_x<<<dim3((d.ny + 31) / 32, (d.nz + 7) / 8), b2, 0, st>>>(S[0], S[3], S[4], d);
-  DSG_COUNT k_bct_y<<<dim3((d.nx + 31) / 32, (d.nz + 7) / 8), b2, 0, st>>>(S[1], S[3], S[5], d);
-  DSG_COUNT k_bct_z<<<dim3((d.nx + 31) / 32, (d.ny + 7) / 8), b2, 0, st>>>(S[2], S[4], S[5], d);
+  const int kx0 = k0 > 2 ? k0 : 2, kx1 = k1 < d.nz ? k1 : d.nz;
+  if (kx1 > kx0) {
+    DSG_COUNT k_bct_x<<<dim3((d.ny + 31) / 32, (kx1 - kx0 + 7) / 8), b2, 0, st>>>(S[0], S[3], S[4], d, kx0, kx1);
+    DSG_COUNT k_bct_y<<<dim3((d.nx + 31) / 32, (kx1 - kx0 + 7) / 8), b2, 0, st>>>(S[1], S[3], S[5], d, kx0, kx1);
+  }
+  DSG_COUNT k_bct_z<<<dim3((d.nx + 31) / 32, (d.ny + 7) / 8), b2, 0, st>>>(S[2], S[4], S[5], d, k0, k1);
   return cudaGetLastError();
 }
+
 
 // csf with the reference's scratch aliasing: w11 = pressure array, w22 = fine
 // residual array, w33 = fine rhs array; ccf is the routine's local array.

@@ -827,6 +827,9 @@ void dsg_destroy(dsg_ctx *ctx) {
     if (ctx->xfer_in_ev[q]) cudaEventDestroy(ctx->xfer_in_ev[q]);
     if (ctx->xfer_out_ev[q]) cudaEventDestroy(ctx->xfer_out_ev[q]);
   }
+  for (int q = 0; q < dsg_ctx::kSChunks; q++) {
+    if (ctx->s_chunk_ev[q]) cudaEventDestroy(ctx->s_chunk_ev[q]);
+  }
   if (ctx->xfer_start) cudaEventDestroy(ctx->xfer_start);
   for (cudaEvent_t e : ctx->prof_ev) cudaEventDestroy(e);
   for (cudaEvent_t e : ctx->phase_ev) cudaEventDestroy(e);
@@ -1106,13 +1109,37 @@ int dsg::solvelpres_pre(dsg_ctx *ctx) {
   double r2 = 2.0 * tauh2 * mu2;
   const double stdgrav = s.g * (s.tau * s.tau) / s.h;
   const double horgrav = s.g1 * (s.tau * s.tau) / s.h;
+  const double rho_r2 = s.rho2, rho_r1 = 0.5 * (s.rho1 - s.rho2);
   DSG_CK(ctx, phase_mark(ctx, 3));
-  DSG_CK(ctx, dsg::stress(S.p, u, v, w, cc, d, r1, r2, r10, r20, st));
-  DSG_CK(ctx, dsg::bc_tensor(S.p, d, st));
-  r2 = s.rho2;
-  r1 = 0.5 * (s.rho1 - s.rho2);
-  DSG_CK(ctx, dsg::abcei(a, b, c, ei, cc, r1, r2, d, st));
-  DSG_CK(ctx, dsg::predictor(w1, w2, w3, u, v, w, a, b, c, S.p, d, horgrav, stdgrav, st));
+  if (ctx->s_chunks > 0) {
+    // S12/S13/S23 still arriving in chunks of planes (dsg_step_host): abcei
+    // (cc only) first; then per chunk, once its copies are in, the csf faces
+    // of those stresses written again, stress and bc_tensor on its planes,
+    // and the predictor on the previous chunk's planes (it reads the
+    // stresses of the planes either side).  The same cells get the same
+    // values as in the unsplit order.
+    DSG_CK(ctx, dsg::abcei(a, b, c, ei, cc, rho_r1, rho_r2, d, st));
+    const int *K = ctx->s_chunk_k, n = ctx->s_chunks;
+    auto lo = [&](int q) { return K[q] > 2 ? K[q] : 2; };
+    auto hi = [&](int q) { return K[q + 1] < d.nz ? K[q + 1] : d.nz; };
+    for (int q = 0; q < n; q++) {
+      DSG_CK(ctx, cudaStreamWaitEvent(st, ctx->s_chunk_ev[q], 0));
+      DSG_CK(ctx, dsg::bc_tensor_offdiag(S.p[3], S.p[4], S.p[5], d, st, K[q], K[q + 1]));
+      if (hi(q) > lo(q)) DSG_CK(ctx, dsg::stress(S.p, u, v, w, cc, d, r1, r2, r10, r20, st, lo(q), hi(q)));
+      DSG_CK(ctx, dsg::bc_tensor(S.p, d, st, K[q], K[q + 1]));
+      if (q > 0 && hi(q - 1) > lo(q - 1))
+        DSG_CK(ctx, dsg::predictor(w1, w2, w3, u, v, w, a, b, c, S.p, d, horgrav, stdgrav, st, lo(q - 1),
+                                   hi(q - 1)));
+    }
+    if (hi(n - 1) > lo(n - 1))
+      DSG_CK(ctx, dsg::predictor(w1, w2, w3, u, v, w, a, b, c, S.p, d, horgrav, stdgrav, st, lo(n - 1),
+                                 hi(n - 1)));
+  } else {
+    DSG_CK(ctx, dsg::stress(S.p, u, v, w, cc, d, r1, r2, r10, r20, st));
+    DSG_CK(ctx, dsg::bc_tensor(S.p, d, st));
+    DSG_CK(ctx, dsg::abcei(a, b, c, ei, cc, rho_r1, rho_r2, d, st));
+    DSG_CK(ctx, dsg::predictor(w1, w2, w3, u, v, w, a, b, c, S.p, d, horgrav, stdgrav, st));
+  }
   DSG_CK(ctx, dsg::bc_w(w1, w2, w3, u, v, w, ctx->red_partials, d, st));
   DSG_CK(ctx, dsg::convective(u, v, w, w1, w2, w3, d, s.tauh, ctx->cfg.convectype, st));
   DSG_CK(ctx, dsg::bc_v(u, v, w, ctx->red_partials, d, s.xvel2, st));
@@ -1274,6 +1301,8 @@ int xfer_resources(dsg_ctx *ctx) {
     DSG_CK(ctx, cudaEventCreateWithFlags(&ctx->xfer_in_ev[q], cudaEventDisableTiming));
     DSG_CK(ctx, cudaEventCreateWithFlags(&ctx->xfer_out_ev[q], cudaEventDisableTiming));
   }
+  for (int q = 0; q < dsg_ctx::kSChunks; q++)
+    DSG_CK(ctx, cudaEventCreateWithFlags(&ctx->s_chunk_ev[q], cudaEventDisableTiming));
   DSG_CK(ctx, cudaStreamCreateWithFlags(&ctx->xfer_out, cudaStreamNonBlocking));
   DSG_CK(ctx, cudaStreamCreateWithFlags(&ctx->xfer_in, cudaStreamNonBlocking));
   return DSG_OK;
@@ -1285,8 +1314,7 @@ struct HostXfer {
   const int *in_fields, *out_fields;
   double *const *out_host;
   bool need[dsg_ctx::kSyncPoints];
-  bool offdiag_late;  // S12/S13/S23 arrive at SP_CSF: their csf faces are written again
-  int last_in;        // last sync point with uploads (-1: none)
+  cudaEvent_t last_in;  // completion of the last upload (null: none)
 };
 
 // At a sync point: the library's stream waits for the inputs the following
@@ -1295,9 +1323,6 @@ struct HostXfer {
 int xfer_hook(dsg_ctx *ctx, int point, void *arg) {
   const HostXfer &x = *static_cast<const HostXfer *>(arg);
   if (x.need[point]) DSG_CK(ctx, cudaStreamWaitEvent(ctx->stream, ctx->xfer_in_ev[point], 0));
-  if (point == SP_CSF && x.offdiag_late)
-    DSG_CK(ctx, dsg::bc_tensor_offdiag(ctx->f[DSG_F_S12], ctx->f[DSG_F_S13], ctx->f[DSG_F_S23], ctx->fine(),
-                                       ctx->stream));
   bool any = false;
   for (int q = 0; q < x.n_out; q++) any = any || last_write(x.out_fields[q]) == point;
   if (!any) return DSG_OK;
@@ -1306,7 +1331,7 @@ int xfer_hook(dsg_ctx *ctx, int point, void *arg) {
   DSG_CK(ctx, cudaStreamWaitEvent(ctx->xfer_out, ctx->xfer_out_ev[point], 0));
   // the uploads gate the step and the downloads only its end: the link is
   // left to the uploads until they are all in
-  if (x.last_in >= 0) DSG_CK(ctx, cudaStreamWaitEvent(ctx->xfer_out, ctx->xfer_in_ev[x.last_in], 0));
+  if (x.last_in) DSG_CK(ctx, cudaStreamWaitEvent(ctx->xfer_out, x.last_in, 0));
   for (int q = 0; q < x.n_out; q++)
     if (last_write(x.out_fields[q]) == point)
       DSG_CK(ctx, cudaMemcpyAsync(x.out_host[q], ctx->f[x.out_fields[q]], bytes, cudaMemcpyDeviceToHost,
@@ -1337,23 +1362,43 @@ int dsg_step_host(dsg_ctx *ctx, int t, dsg_mg_stats *stats, int n_in, const int 
   int rc = xfer_resources(ctx);
   if (rc) return rc;
   const size_t bytes = ctx->fine().count() * sizeof(double);
-  HostXfer x{n_in, n_out, in_fields, out_fields, out_host, {}, false, -1};
+  HostXfer x{n_in, n_out, in_fields, out_fields, out_host, {}, nullptr};
   // the uploads start after the work already queued on the library's stream,
   // in the order the step needs them, one event after each sync point's group
   DSG_CK(ctx, cudaEventRecord(ctx->xfer_start, ctx->stream));
   DSG_CK(ctx, cudaStreamWaitEvent(ctx->xfer_in, ctx->xfer_start, 0));
   DSG_CK(ctx, cudaStreamWaitEvent(ctx->xfer_out, ctx->xfer_start, 0));
+  int late[3], n_late = 0;  // off-diagonal stresses that arrive after csf
   for (int p = 0; p < dsg_ctx::kSyncPoints; p++) {
     for (int q = 0; q < n_in; q++)
       if (first_touch(ctx, in_fields[q]) == p) {
-        DSG_CK(ctx, cudaMemcpyAsync(ctx->f[in_fields[q]], in_host[q], bytes, cudaMemcpyHostToDevice, ctx->xfer_in));
-        x.need[p] = true;
         const int f = in_fields[q];
-        if (p == SP_CSF && (f == DSG_F_S12 || f == DSG_F_S13 || f == DSG_F_S23)) x.offdiag_late = true;
+        if (p == SP_CSF && (f == DSG_F_S12 || f == DSG_F_S13 || f == DSG_F_S23)) {
+          if (n_late < 3) late[n_late++] = q;
+          continue;
+        }
+        DSG_CK(ctx, cudaMemcpyAsync(ctx->f[f], in_host[q], bytes, cudaMemcpyHostToDevice, ctx->xfer_in));
+        x.need[p] = true;
       }
     if (x.need[p]) {
       DSG_CK(ctx, cudaEventRecord(ctx->xfer_in_ev[p], ctx->xfer_in));
-      x.last_in = p;
+      x.last_in = ctx->xfer_in_ev[p];
+    }
+    if (p == SP_CSF && n_late > 0) {
+      // in chunks of planes, so that the momentum phase starts on the first
+      const size_t plane = (size_t)ctx->nx * ctx->ny;
+      const int nch = dsg_ctx::kSChunks;
+      for (int c = 0; c <= nch; c++) ctx->s_chunk_k[c] = 1 + (int)((long long)c * ctx->nz / nch);
+      for (int c = 0; c < nch; c++) {
+        const size_t off = (size_t)(ctx->s_chunk_k[c] - 1) * plane;
+        const size_t cnt = (size_t)(ctx->s_chunk_k[c + 1] - ctx->s_chunk_k[c]) * plane;
+        for (int m = 0; m < n_late; m++)
+          DSG_CK(ctx, cudaMemcpyAsync(ctx->f[in_fields[late[m]]] + off, in_host[late[m]] + off,
+                                      cnt * sizeof(double), cudaMemcpyHostToDevice, ctx->xfer_in));
+        DSG_CK(ctx, cudaEventRecord(ctx->s_chunk_ev[c], ctx->xfer_in));
+      }
+      ctx->s_chunks = nch;
+      x.last_in = ctx->s_chunk_ev[nch - 1];
     }
   }
   ctx->sync_hook = xfer_hook;
@@ -1361,6 +1406,7 @@ int dsg_step_host(dsg_ctx *ctx, int t, dsg_mg_stats *stats, int n_in, const int 
   rc = step_phases(ctx, t, stats);
   ctx->sync_hook = nullptr;
   ctx->sync_arg = nullptr;
+  ctx->s_chunks = 0;
   // no copy stays in flight into or out of the caller's buffers, also on errors
   const cudaError_t e1 = cudaStreamSynchronize(ctx->xfer_in);
   const cudaError_t e2 = cudaStreamSynchronize(ctx->xfer_out);

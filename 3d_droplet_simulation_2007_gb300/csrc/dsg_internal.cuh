@@ -133,19 +133,23 @@ cudaError_t calcrho(double *rhon, double *mun, const double *cc, Dims d, double 
 // csf.cu (S = {S11,S22,S33,S12,S13,S23})
 // The S12/S13/S23 writes of bc_tensor alone (constant faces), for an upload of
 // those fields that lands after csf.
-cudaError_t bc_tensor_offdiag(double *s12, double *s13, double *s23, Dims d, cudaStream_t st);
-cudaError_t bc_tensor(double *const S[6], Dims d, cudaStream_t st);
+// Both on planes k0 .. k1-1 (x and y faces of the interior planes among them,
+// the z planes 1, 2, nz in the range); the defaults cover every plane.
+cudaError_t bc_tensor_offdiag(double *s12, double *s13, double *s23, Dims d, cudaStream_t st, int k0 = 1,
+                              int k1 = 1 << 30);
+cudaError_t bc_tensor(double *const S[6], Dims d, cudaStream_t st, int k0 = 1, int k1 = 1 << 30);
 cudaError_t csf(const double *ccc, double *w11, double *w22, double *w33, double *ccf, double *const S[6],
                 Dims d, double tau, double sigma, double h, cudaStream_t st);
 // momentum.cu
 cudaError_t bc_v(double *u, double *v, double *w, double *partials, Dims d, double xvel2, cudaStream_t st);
 cudaError_t bc_w(double *w1, double *w2, double *w3, const double *u, const double *v, const double *w,
                  double *partials, Dims d, cudaStream_t st);
+// stress and predictor on the interior planes k0 .. k1-1 (k1 = 0: up to nz-1)
 cudaError_t stress(double *const S[6], const double *u, const double *v, const double *w, const double *cc,
-                   Dims d, double r1, double r2, double r10, double r20, cudaStream_t st);
+                   Dims d, double r1, double r2, double r10, double r20, cudaStream_t st, int k0 = 2, int k1 = 0);
 cudaError_t predictor(double *w1, double *w2, double *w3, const double *u, const double *v, const double *w,
                       const double *a, const double *b, const double *c, double *const S[6], Dims d,
-                      double horgrav, double stdgrav, cudaStream_t st);
+                      double horgrav, double stdgrav, cudaStream_t st, int k0 = 2, int k1 = 0);
 cudaError_t convective(double *u, double *v, double *w, const double *w1, const double *w2, const double *w3,
                        Dims d, double tauh, int convectype, cudaStream_t st);
 cudaError_t divergence(double *out, const double *u, const double *v, const double *w, Dims d, double hi2,
@@ -310,6 +314,14 @@ struct dsg_ctx {
   cudaEvent_t xfer_in_ev[kSyncPoints] = {};
   cudaEvent_t xfer_out_ev[kSyncPoints] = {};
   cudaEvent_t xfer_start = nullptr;
+  // off-diagonal stresses arriving after csf come in kSChunks ranges of
+  // planes (chunk c: planes s_chunk_k[c] .. s_chunk_k[c+1]-1, its copies
+  // complete at s_chunk_ev[c]); the momentum phase then works through them
+  // chunk by chunk.  s_chunks = 0: not in a host-buffer step, or not late.
+  static constexpr int kSChunks = 4;
+  cudaEvent_t s_chunk_ev[kSChunks] = {};
+  int s_chunk_k[kSChunks + 1] = {};
+  int s_chunks = 0;
   int (*sync_hook)(dsg_ctx *ctx, int point, void *arg) = nullptr;
   void *sync_arg = nullptr;
   dsg::Dims fine() const { return dsg::Dims{nx, ny, nz}; }

@@ -14,10 +14,10 @@ __global__ void k_stress(double *__restrict__ S11, double *__restrict__ S22, dou
                          double *__restrict__ S12, double *__restrict__ S13, double *__restrict__ S23,
                          const double *__restrict__ u, const double *__restrict__ v,
                          const double *__restrict__ w, const double *__restrict__ cc, Dims d, double r1,
-                         double r2, double r10, double r20) {
+                         double r2, double r10, double r20, int k0) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
-  const int k = blockIdx.z + 2;
+  const int k = blockIdx.z + k0;
   if (i > d.nx - 1 || j > d.ny - 1) return;
   const size_t q = d.ix(i, j, k);
   const size_t sy = d.sy(), sz = d.sz();
@@ -41,10 +41,10 @@ __global__ void k_predictor(double *__restrict__ w1, double *__restrict__ w2, do
                             const double *__restrict__ S11, const double *__restrict__ S22,
                             const double *__restrict__ S33, const double *__restrict__ S12,
                             const double *__restrict__ S13, const double *__restrict__ S23, Dims d,
-                            double horgrav, double stdgrav) {
+                            double horgrav, double stdgrav, int k0) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
-  const int k = blockIdx.z + 2;
+  const int k = blockIdx.z + k0;
   if (i > d.nx - 1 || j > d.ny - 1) return;
   const size_t q = d.ix(i, j, k);
   const size_t sy = d.sy(), sz = d.sz();
@@ -305,18 +305,26 @@ cudaError_t bc_w(double *w1, double *w2, double *w3, const double *u, const doub
   return cudaGetLastError();
 }
 
+// Interior planes k0 .. k1-1 (k1 = 0: all interior planes, 2 .. nz-1).
+inline dim3 plane_grid(const Dims &d, int k0, int k1) {
+  const dim3 g = interior_grid(d, kBlk);
+  return dim3(g.x, g.y, (unsigned)((k1 ? k1 : d.nz) - k0));
+}
+
 cudaError_t stress(double *const S[6], const double *u, const double *v, const double *w, const double *cc,
-                   Dims d, double r1, double r2, double r10, double r20, cudaStream_t st) {
-  DSG_COUNT k_stress<<<interior_grid(d, kBlk), kBlk, 0, st>>>(S[0], S[1], S[2], S[3], S[4], S[5], u, v, w, cc, d, r1,
-                                                    r2, r10, r20);
+                   Dims d, double r1, double r2, double r10, double r20, cudaStream_t st, int k0, int k1) {
+  if ((k1 ? k1 : d.nz) <= k0) return cudaSuccess;
+  DSG_COUNT k_stress<<<plane_grid(d, k0, k1), kBlk, 0, st>>>(S[0], S[1], S[2], S[3], S[4], S[5], u, v, w, cc, d, r1,
+                                                              r2, r10, r20, k0);
   return cudaGetLastError();
 }
 
 cudaError_t predictor(double *w1, double *w2, double *w3, const double *u, const double *v, const double *w,
                       const double *a, const double *b, const double *c, double *const S[6], Dims d,
-                      double horgrav, double stdgrav, cudaStream_t st) {
-  DSG_COUNT k_predictor<<<interior_grid(d, kBlk), kBlk, 0, st>>>(w1, w2, w3, u, v, w, a, b, c, S[0], S[1], S[2], S[3],
-                                                       S[4], S[5], d, horgrav, stdgrav);
+                      double horgrav, double stdgrav, cudaStream_t st, int k0, int k1) {
+  if ((k1 ? k1 : d.nz) <= k0) return cudaSuccess;
+  DSG_COUNT k_predictor<<<plane_grid(d, k0, k1), kBlk, 0, st>>>(w1, w2, w3, u, v, w, a, b, c, S[0], S[1], S[2],
+                                                                 S[3], S[4], S[5], d, horgrav, stdgrav, k0);
   return cudaGetLastError();
 }
 
