@@ -75,6 +75,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 reference point")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned warm-start point")
+    ap.add_argument("--no-ensemble", action="store_true",
+                    help="skip the 16-member ensemble point recorded beside the headline")
     ap.add_argument("--ensemble", type=int, default=0,
                     help="time the droplet-study ensemble of this many members instead (48-160^3 grids)")
     ap.add_argument("--workers", type=int, default=0, help="ensemble host threads (0: autotune)")
@@ -510,6 +512,21 @@ def run_gb300(args):
                "d2h_bytes_per_step": len(outs) * n_cells * 8}
     solver.close()
 
+    # a bounded droplet-study ensemble on the same GPU, recorded beside the
+    # headline (the full study is `bench.py --ensemble 64`)
+    ens = None
+    if not args.no_ensemble and ws == 1:
+        n_ens, k_ens = 16, 4
+        cfgs = dsg.ensemble.study_configs(n_ens, tol=args.tol)
+        m = measure_ensemble(dsg, dsg.load(), cfgs, k_ens, 2, 0, [4])
+        ens = {"value": n_ens * k_ens / m["el"], "unit": "member-steps/s", "members": n_ens, "steps": k_ens,
+               "workload": "%d droplets on wall, interior sides 48-160, Weber 50-800, mixed pressure to %.0e"
+                           % (n_ens, args.tol),
+               "cells_per_step": sum((c.nx - 2) * (c.ny - 2) * (c.nz - 2) for c in cfgs),
+               "workers": m["workers"], "ms_per_step": 1e3 * m["el"] / k_ens,
+               "timing": "host clock between synchronisations of all member streams",
+               "clocks": m["clocks"], "batched": batched_entry(n_ens, k_ens, m["batched"])}
+
     if rank == 0:
         roof = relax_roofline(prof, ms, args.n)
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -530,35 +547,24 @@ def run_gb300(args):
             line["plain_fp64"] = plain
         if learned:
             line["learned_warm_start"] = learned
+        if ens:
+            line["ensemble"] = ens
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
     return 0
 
 
-def run_ensemble(args):
-    """Member time steps per second of the droplet-study ensemble: members
-    of 48-160^3 cells, Weber 50-800, mixed-precision pressure to tol.  The
-    members run on their own streams from a pool of host threads; the timed
-    region is bracketed by a synchronisation of every member's stream and
-    measured with the host clock (the work spans many streams).  With N
-    ranks the members are sharded across the GPUs by cost (no data-path
-    collective); the time is the slowest rank's."""
-    import torch
-    ws, rank, local = dist_env()
-    torch.cuda.set_device(local)
-    dist = None
-    if ws > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    dsg = importlib.import_module(PKG)
-    lib = dsg.load()
-    cfgs = dsg.ensemble.study_configs(args.ensemble, tol=args.tol)
-    mine = dsg.ensemble.shard(cfgs, rank, ws)
-    cells = sum((c.nx - 2) * (c.ny - 2) * (c.nz - 2) for c in cfgs)
-    with dsg.Ensemble([cfgs[i] for i in mine], workers=max(args.workers, 1)) as e:
-        tuned = e.autotune(steps_per_trial=2) if args.workers <= 0 else None
-        for _ in range(args.warmup):
+def measure_ensemble(dsg, lib, cfgs, steps, warmup, workers, group_cands, dist=None):
+    """Time the members `cfgs` (this rank's share) as an ensemble: the worker
+    pool (worker count autotuned when `workers` <= 0), then, if
+    `group_cands` is not empty, the batched pressure solve with the fastest
+    group count among them (tail depth and tile shapes autotuned).  The
+    timed region is bracketed by a synchronisation of every member's stream
+    and measured with the host clock (the work spans many streams)."""
+    with dsg.Ensemble(cfgs, workers=max(workers, 1)) as e:
+        tuned = e.autotune(steps_per_trial=2) if workers <= 0 else None
+        for _ in range(warmup):
             e.step()
 
         def timed(k):
@@ -576,19 +582,18 @@ def run_ensemble(args):
                 dist.barrier()
             return el, lib.dsg_launch_count() - l0, stats
 
-        clocks = Clocks(local)
+        clocks = Clocks(torch_device_index())
         clocks.start()
-        el, launches, stats = timed(args.steps)
+        el, launches, stats = timed(steps)
         clk = clocks.stop()
-        workers = e.workers
+        out = {"el": el, "launches": launches, "stats": stats, "workers": e.workers, "tuned": tuned is not None,
+               "clocks": clk, "n": e.n}
         # the batched pressure solve, same members and workers, after the
-        # timed steps: group count tried over 1, 2, 4, 8 and 16 (or fixed),
-        # coarse-tail depth and tile shapes autotuned, then timed the same way
-        batched = None
-        if not args.no_batched:
-            cands = [args.groups] if args.groups > 0 else [g for g in (1, 2, 4, 8, 16) if g <= len(mine)]
+        # timed steps: the fastest group count, coarse-tail depth and tile
+        # shapes autotuned, then timed the same way
+        if group_cands:
             group_ms = {}
-            for g in cands:
+            for g in group_cands:
                 e.set_batched(g)
                 e.autotune_tiles(reps=3)
                 e.step()
@@ -600,18 +605,58 @@ def run_ensemble(args):
             e.set_batched(groups)
             tiles = e.autotune_tiles(reps=3)
             e.step()
-            bel, blaunch, _ = timed(args.steps)
-            batched = {"el": bel, "groups": groups, "tiles": tiles, "tail_nodes": e.batch_tail_nodes,
-                       "launches": blaunch, "group_ms": {k: round(v, 1) for k, v in group_ms.items()}}
+            bel, blaunch, _ = timed(steps)
+            out["batched"] = {"el": bel, "groups": groups, "tiles": tiles, "tail_nodes": e.batch_tail_nodes,
+                              "launches": blaunch, "group_ms": {k: round(v, 1) for k, v in group_ms.items()}}
             e.set_batched(0)
         e.set_workers(1)
-        el1, _, _ = timed(1)
-    if batched:
-        batched["el"] = max_over_ranks(batched["el"], dist, "cuda")
-    el = max_over_ranks(el, dist, "cuda")
-    el1 = max_over_ranks(el1, dist, "cuda")
+        out["el1"], _, _ = timed(1)
+    return out
+
+
+def torch_device_index():
+    import torch
+    return torch.cuda.current_device()
+
+
+def batched_entry(n_members, steps, b):
+    return {"value": n_members * steps / b["el"], "unit": "member-steps/s",
+            "ms_per_step": 1e3 * b["el"] / steps,
+            "solve": ("batched pressure solves: one launch per multigrid pass over each of %d cost-balanced "
+                      "groups (each worker steps whole groups), CUDA graphs, %d pass tile shapes autotuned, "
+                      "levels of at most %d nodes in each member's single-block tail"
+                      % (b["groups"], b["tiles"], b["tail_nodes"])),
+            "step_ms_per_group_count": b["group_ms"], "gpu_launches": b["launches"]}
+
+
+def run_ensemble(args):
+    """Member time steps per second of the droplet-study ensemble: members
+    of 48-160^3 cells, Weber 50-800, mixed-precision pressure to tol.  The
+    members run on their own streams from a pool of host threads.  With N
+    ranks the members are sharded across the GPUs by cost (no data-path
+    collective); the time is the slowest rank's."""
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dsg = importlib.import_module(PKG)
+    lib = dsg.load()
+    cfgs = dsg.ensemble.study_configs(args.ensemble, tol=args.tol)
+    mine = dsg.ensemble.shard(cfgs, rank, ws)
+    cells = sum((c.nx - 2) * (c.ny - 2) * (c.nz - 2) for c in cfgs)
+    cands = [] if args.no_batched else (
+        [args.groups] if args.groups > 0 else [g for g in (1, 2, 4, 8, 16) if g <= len(mine)])
+    m = measure_ensemble(dsg, lib, [cfgs[i] for i in mine], args.steps, args.warmup, args.workers, cands, dist)
+    if "batched" in m:
+        m["batched"]["el"] = max_over_ranks(m["batched"]["el"], dist, "cuda")
+    el = max_over_ranks(m["el"], dist, "cuda")
+    el1 = max_over_ranks(m["el1"], dist, "cuda")
     value = args.ensemble * args.steps / el
     if rank == 0:
+        stats = m["stats"]
         line = {"metric": "member time-steps/s, droplet-study ensemble", "value": value,
                 "unit": "member-steps/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True, "scaling": "strong",
@@ -619,23 +664,16 @@ def run_ensemble(args):
                 "config": {"workload": "%d droplets on wall, interior sides 48/64/96/128/160, Weber 50-800 "
                                        "log-uniform, D = 2 mm, mixed-precision pressure to %.0e"
                                        % (args.ensemble, args.tol),
-                           "cells_per_step": cells, "workers": workers, "autotuned": tuned is not None,
+                           "cells_per_step": cells, "workers": m["workers"], "autotuned": m["tuned"],
                            "pressure_solve": "one mixed-precision solve per member (CUDA graphs per member)",
                            "members_rank0": len(mine),
                            "parallelism": "members sharded by cost over %d GPU(s)" % ws,
                            "timing": "host clock between synchronisations of all member streams"},
                 "one_worker_value": args.ensemble / el1,
-                "vcycles_mean": float(sum(s["vcycles"] for st in stats for s in st) / max(1, len(stats) * e.n)),
-                "gpu_launches": launches, "clocks": clk}
-        if batched:
-            line["batched"] = {
-                "value": args.ensemble * args.steps / batched["el"], "unit": "member-steps/s",
-                "ms_per_step": 1e3 * batched["el"] / args.steps,
-                "solve": ("batched pressure solves: one launch per multigrid pass over each of %d cost-balanced "
-                          "groups (each worker steps whole groups), CUDA graphs, %d pass tile shapes autotuned, "
-                          "levels of at most %d nodes in each member's single-block tail"
-                          % (batched["groups"], batched["tiles"], batched["tail_nodes"])),
-                "step_ms_per_group_count": batched["group_ms"], "gpu_launches": batched["launches"]}
+                "vcycles_mean": float(sum(s["vcycles"] for st in stats for s in st) / max(1, len(stats) * m["n"])),
+                "gpu_launches": m["launches"], "clocks": m["clocks"]}
+        if "batched" in m:
+            line["batched"] = batched_entry(args.ensemble, args.steps, m["batched"])
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
