@@ -960,19 +960,20 @@ cudaError_t conv_tc(const bf16 *X, const bf16 *Wt, int NT, int co0, const float 
   constexpr size_t smem = tc::smem_bytes<CIN, COUT, STAGES>();
   static_assert(smem <= 232448, "shared memory per CTA");
   auto kern = k_conv3_tc<CIN, COUT, STAGES, LMAX, RELU, OUTF>;
-  static int grid_cap = 0;
-  if (!grid_cap) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
-                               (int)cudaSharedmemCarveoutMaxShared);
+  // resident CTAs on the device, computed once per instantiation (a
+  // function-local static: thread-safe initialisation); 0 after a failure
+  static const int grid_cap = [&]() -> int {
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+        cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess)
+      return 0;
     int dev = 0, sms = 0, smem_sm = 0;
     cudaFuncAttributes fa;
-    if (e == cudaSuccess) e = cudaGetDevice(&dev);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, kern);
-    if (e != cudaSuccess) return e;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess ||
+        cudaFuncGetAttributes(&fa, kern) != cudaSuccess)
+      return 0;
     // resident CTAs per SM: shared memory (1 KB reserved per CTA), TMEM
     // columns, registers, threads
     constexpr int tcap = 512 / tc::tmem_cols(COUT, LMAX);
@@ -981,8 +982,9 @@ cudaError_t conv_tc(const bf16 *X, const bf16 *Wt, int NT, int co0, const float 
     const int regs = fa.numRegs > 0 ? fa.numRegs : 64;
     occ = occ < 65536 / (regs * tc::THREADS) ? occ : 65536 / (regs * tc::THREADS);
     occ = occ < 2048 / tc::THREADS ? occ : 2048 / tc::THREADS;
-    grid_cap = sms * (occ > 0 ? occ : 1);
-  }
+    return sms * (occ > 0 ? occ : 1);
+  }();
+  if (!grid_cap) return cudaErrorInvalidConfiguration;
   CUtensorMap map;
   cudaError_t e = halo_map(&map, X, CIN, W, H, D);
   if (e != cudaSuccess) return e;
@@ -999,13 +1001,10 @@ cudaError_t conv_tc(const bf16 *X, const bf16 *Wt, int NT, int co0, const float 
 template <int CIN, int COUT>
 cudaError_t wgrad_launch(const bf16 *X, const bf16 *G, float *dW, int W, int H, int D, cudaStream_t st) {
   const size_t smem = ((size_t)(BZ + 2) * (CTY + 2) * (CTX + 2) * CIN + (size_t)BZ * CTY * CTX * COUT) * sizeof(bf16);
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e =
-        cudaFuncSetAttribute(k_conv3_wgrad<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  // set once per instantiation (a function-local static: thread-safe initialisation)
+  static const cudaError_t attr =
+      cudaFuncSetAttribute(k_conv3_wgrad<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (attr != cudaSuccess) return attr;
   const dim3 grid((unsigned)((W + CTX - 1) / CTX), (unsigned)((H + CTY - 1) / CTY), (unsigned)((D + BZ - 1) / BZ));
   DSG_COUNT k_conv3_wgrad<CIN, COUT><<<grid, 256, smem, st>>>(X, G, dW, W, H, D);
   return cudaGetLastError();
