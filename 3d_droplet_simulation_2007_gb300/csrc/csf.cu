@@ -185,14 +185,19 @@ cudaError_t bc_tensor(double *const S[6], Dims d, cudaStream_t st, int k0, int k
 
 // csf with the reference's scratch aliasing: w11 = pressure array, w22 = fine
 // residual array, w33 = fine rhs array; ccf is the routine's local array.
+// scratch = false (inside a whole step, where the pressure phase overwrites
+// all three before reading them): the filtered field goes straight to ccf
+// and S11..S33 are not copied into w11..w33; w11 still holds the curvature.
 cudaError_t csf(const double *ccc, double *w11, double *w22, double *w33, double *ccf, double *const S[6],
-                Dims d, double tau, double sigma, double h, cudaStream_t st) {
+                Dims d, double tau, double sigma, double h, cudaStream_t st, bool scratch) {
   const size_t bytes = d.count() * sizeof(double);
   // copy(ccf,ccc); filterc27(ccf,w22); copy(ccf,w22): filtering ccf == filtering ccc
-  cudaError_t e = filterc27(ccc, w22, d, st);
+  cudaError_t e = filterc27(ccc, scratch ? w22 : ccf, d, st);
   if (e != cudaSuccess) return e;
-  e = cudaMemcpyAsync(ccf, w22, bytes, cudaMemcpyDeviceToDevice, st);
-  if (e != cudaSuccess) return e;
+  if (scratch) {
+    e = cudaMemcpyAsync(ccf, w22, bytes, cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) return e;
+  }
   e = bc_out(ccf, d, st);
   if (e != cudaSuccess) return e;
   if (sigma == 0.0) {
@@ -207,9 +212,11 @@ cudaError_t csf(const double *ccc, double *w11, double *w22, double *w33, double
   e = bc_out(w11, d, st);
   if (e != cudaSuccess) return e;
   DSG_COUNT k_csf_force<<<interior_grid(d, kBlk), kBlk, 0, st>>>(S[0], S[1], S[2], ccf, w11, d, sigh);
-  if ((e = cudaMemcpyAsync(w11, S[0], bytes, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
-  if ((e = cudaMemcpyAsync(w22, S[1], bytes, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
-  if ((e = cudaMemcpyAsync(w33, S[2], bytes, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
+  if (scratch) {
+    if ((e = cudaMemcpyAsync(w11, S[0], bytes, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(w22, S[1], bytes, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(w33, S[2], bytes, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
+  }
   return bc_tensor(S, d, st);
 }
 

@@ -1030,7 +1030,14 @@ int dsg_checktime(dsg_ctx *ctx) {
   return DSG_OK;
 }
 
-int dsg_csf(dsg_ctx *ctx) {
+int dsg_csf(dsg_ctx *ctx) { return dsg::csf_phase(ctx, true); }
+
+}  // extern "C"
+
+// The surface-tension model of surfacet; scratch: csf's copies into the
+// pressure, residual and rhs arrays (the reference's aliasing), which a whole
+// step overwrites before reading.
+int dsg::csf_phase(dsg_ctx *ctx, bool scratch) {
   if (!ctx) return DSG_E_ARG;
   Tensor S(ctx);
   if (ctx->cfg.surfacet == 5 || ctx->cfg.surfacet == 6) {
@@ -1046,9 +1053,11 @@ int dsg_csf(dsg_ctx *ctx) {
     return DSG_OK;
   }
   DSG_CK(ctx, dsg::csf(ctx->f[DSG_F_CC], ctx->f[DSG_F_P], ctx->f[DSG_F_RES], ctx->f[DSG_F_RHS], ctx->ccf, S.p,
-                       ctx->fine(), ctx->s.tau, ctx->s.sigma, ctx->s.h, ctx->stream));
+                       ctx->fine(), ctx->s.tau, ctx->s.sigma, ctx->s.h, ctx->stream, scratch));
   return DSG_OK;
 }
+
+extern "C" {
 
 // CalcH3d (main.f:30 with hswitch = 1).  The reference STOPs when a cell
 // matches none of the polygon cases; here the step returns DSG_E_STATE.
@@ -1230,7 +1239,7 @@ int dsg::step_pre_solve(dsg_ctx *ctx, int t) {
   rc = dsg_checktime(ctx);
   if (rc || (rc = sync_point(ctx, SP_CFL))) return rc;
   DSG_CK(ctx, phase_mark(ctx, 2));
-  rc = dsg_csf(ctx);
+  rc = dsg::csf_phase(ctx, false);
   if (rc || (rc = sync_point(ctx, SP_CSF))) return rc;
   return dsg::solvelpres_pre(ctx);
 }

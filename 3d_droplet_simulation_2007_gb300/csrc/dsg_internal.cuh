@@ -139,7 +139,7 @@ cudaError_t bc_tensor_offdiag(double *s12, double *s13, double *s23, Dims d, cud
                               int k1 = 1 << 30);
 cudaError_t bc_tensor(double *const S[6], Dims d, cudaStream_t st, int k0 = 1, int k1 = 1 << 30);
 cudaError_t csf(const double *ccc, double *w11, double *w22, double *w33, double *ccf, double *const S[6],
-                Dims d, double tau, double sigma, double h, cudaStream_t st);
+                Dims d, double tau, double sigma, double h, cudaStream_t st, bool scratch = true);
 // momentum.cu
 cudaError_t bc_v(double *u, double *v, double *w, double *partials, Dims d, double xvel2, cudaStream_t st);
 cudaError_t bc_w(double *w1, double *w2, double *w3, const double *u, const double *v, const double *w,
@@ -239,6 +239,12 @@ int net_apply(dsg_net *n, double *p, double alpha, Dims d, cudaStream_t st);
 int net_target(dsg_net *n, const double *p, Dims d, cudaStream_t st);
 void net_begin_solve(dsg_net *n);
 }  // namespace nn
+}  // namespace dsg
+
+struct dsg_ctx;
+namespace dsg {
+// dsg.cu: the surface-tension phase (dsg_csf with scratch = true)
+int csf_phase(dsg_ctx *ctx, bool scratch);
 }  // namespace dsg
 
 // ---- context ---------------------------------------------------------------
