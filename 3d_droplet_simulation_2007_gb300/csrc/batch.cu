@@ -70,7 +70,14 @@ struct ARR { float *rhs_c, *u_c; const float *u, *rhs, *a, *b, *c; Dims df, dc; 
 struct AProSplit { float *ue, *uo; const float *uc; Dims df; Split sp; Dims dc; int add; };
 struct APro { float *uf; const float *uc; Dims df, dc; int add; };
 struct ACorrect { double *p; const float *ev, *od; Dims d; Split sp; int init; };
-struct ADefect { float *r_ev, *r_od; Split sp; double *partials; const double *p, *rhs, *a, *b, *c; Dims d; double h2i; };
+struct ADefect {
+  float *r_ev, *r_od;
+  Split sp;
+  double *partials;
+  const double *p, *rhs, *a, *b, *c, *diag;
+  Dims d;
+  double h2i;
+};
 struct AFold { const double *partials; double *out; };
 struct AZero { float *p; size_t n; };
 struct ATo32 { float *dst; const double *src; size_t n; };
@@ -185,7 +192,7 @@ __global__ void kb_correct64(BATCH_PARAMS(ACorrect)) {
 
 __global__ void kb_defect64(BATCH_PARAMS(ADefect)) {
   FOR_MEMBER_BLOCKS(ADefect) {
-    b_defect64(B, G, a.r_ev, a.r_od, a.sp, a.partials, a.p, a.rhs, a.a, a.b, a.c, a.d, a.h2i);
+    b_defect64(B, G, a.r_ev, a.r_od, a.sp, a.partials, a.p, a.rhs, a.a, a.b, a.c, a.diag, a.d, a.h2i);
   });
 }
 
@@ -550,7 +557,8 @@ struct Planner {
       tc.add((int)i, grid_of(K_CORRECT, d, kDefaultShape), 1, ACorrect{L[1], f.u[0], f.u[1], d, sp, init});
       const double h1 = c->s.lengthsize / (d.nx - 2);
       td.add((int)i, dim3(kRedBlocks), 1,
-             ADefect{f.r[0], f.r[1], sp, c->red_partials, L[1], L[3], L[4], L[5], L[6], d, 1.0 / (h1 * h1)});
+             ADefect{f.r[0], f.r[1], sp, c->red_partials, L[1], L[3], L[4], L[5], L[6], c->diag64, d,
+                     1.0 / (h1 * h1)});
       tf.add((int)i, dim3(1), 1, AFold{c->red_partials, norms_dev + 2 * i});
     }
     emit(out, K_CORRECT, tc, kDefaultShape, 0, 0, 0, 0, gate, -1);
@@ -955,7 +963,13 @@ int batch_solve(BatchSolve *b, const std::vector<int> &active, std::vector<dsg_m
   for (size_t i = 0; i < n; i++) {
     mg_rc[i] = DSG_OK;
     dsg_ctx *c = b->m[i];
-    cudaError_t e = cudaEventRecord(b->ev_member[i], c->stream);
+    cudaError_t e = cudaSuccess;
+    if (!c->diag_fresh) {  // coefficients not from this step's abcei: form the defect's diagonal
+      double **L = c->lv[c->ng];
+      e = dsg::diag_sum(c->diag64, L[4], L[5], L[6], c->fine(), c->stream);
+      c->diag_fresh = true;
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(b->ev_member[i], c->stream);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(b->st, b->ev_member[i], 0);
     if (e != cudaSuccess) return set_error(nullptr, DSG_E_CUDA, "batched solve: join: %s", cudaGetErrorString(e));
   }

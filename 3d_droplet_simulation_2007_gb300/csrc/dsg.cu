@@ -302,8 +302,8 @@ int vcycle32(dsg_ctx *ctx, int j) {
 int defect_launch(dsg_ctx *ctx) {
   double **L = ctx->lv[ctx->ng];
   FineSplit f = fine_split(ctx);
-  DSG_CK(ctx, dsg::defect64(f.r, ctx->red_out, ctx->red_partials, L[1], L[3], L[4], L[5], L[6], ctx->fine(),
-                            ctx->s.lengthsize, ctx->stream));
+  DSG_CK(ctx, dsg::defect64(f.r, ctx->red_out, ctx->red_partials, L[1], L[3], L[4], L[5], L[6], ctx->diag64,
+                            ctx->fine(), ctx->s.lengthsize, ctx->stream));
   DSG_CK(ctx, cudaMemcpyAsync(ctx->red_host, ctx->red_out, 2 * sizeof(double), cudaMemcpyDeviceToHost,
                               ctx->stream));
   return DSG_OK;
@@ -508,6 +508,11 @@ int mixed_solve(dsg_ctx *ctx, dsg_mg_stats *s) {
   };
   int rc;
   double r;
+  if (!ctx->diag_fresh) {  // coefficients not from this step's abcei: form the defect's diagonal
+    double **L = ctx->lv[ng];
+    DSG_CK(ctx, dsg::diag_sum(ctx->diag64, L[4], L[5], L[6], ctx->fine(), st));
+    ctx->diag_fresh = true;
+  }
   const bool learned = ctx->cfg.mode == DSG_MODE_LEARNED;
   if (learned && !ctx->net) return dsg::set_error(ctx, DSG_E_STATE, "learned mode without an attached network");
   if (ctx->net) dsg::nn::net_begin_solve(ctx->net);
@@ -605,6 +610,7 @@ int mixed_solve(dsg_ctx *ctx, dsg_mg_stats *s) {
 // an attached network, the context's record of the solve, the caller's
 // statistics, and DSG_E_NOT_CONVERGED when the cycle cap stopped it.
 int dsg::mixed_finish(dsg_ctx *ctx, dsg_mg_stats *s, dsg_mg_stats *stats) {
+  ctx->diag_fresh = false;  // the next solve forms it again unless abcei does
   int rc = record_pair(ctx);
   if (rc) return rc;
   ctx->s.last_vcycles = s->vcycles;
@@ -748,7 +754,7 @@ int dsg_create(const dsg_config *cfg, dsg_ctx **out) {
   for (int l = ng; l >= 1; l--)
     total += 6 * up((size_t)ctx->lnx[l] * ctx->lny[l] * ctx->lnz[l] * sizeof(float));
   const size_t fine = up((size_t)cfg->nx * cfg->ny * cfg->nz * sizeof(double));
-  const int nextra = DSG_NFIELDS - 8 + 1;  // fine fields beyond the level arrays + ccf
+  const int nextra = DSG_NFIELDS - 8 + 2;  // fine fields beyond the level arrays + ccf + diag64
   total += nextra * fine;
   total += up(dsg::kRedBlocks * 4 * sizeof(double)) + up(16 * sizeof(double)) + up(sizeof(unsigned long long)) +
            up(sizeof(unsigned));
@@ -777,6 +783,8 @@ int dsg_create(const dsg_config *cfg, dsg_ctx **out) {
     p += fine;
   }
   ctx->ccf = (double *)p;
+  p += fine;
+  ctx->diag64 = (double *)p;
   p += fine;
   ctx->red_partials = (double *)p;
   p += up(dsg::kRedBlocks * 4 * sizeof(double));
@@ -1127,7 +1135,8 @@ int dsg::solvelpres_pre(dsg_ctx *ctx) {
     // and the predictor on the previous chunk's planes (it reads the
     // stresses of the planes either side).  The same cells get the same
     // values as in the unsplit order.
-    DSG_CK(ctx, dsg::abcei(a, b, c, ei, cc, rho_r1, rho_r2, d, st));
+    DSG_CK(ctx, dsg::abcei(a, b, c, ei, cc, rho_r1, rho_r2, d, st, ctx->diag64));
+    ctx->diag_fresh = true;
     const int *K = ctx->s_chunk_k, n = ctx->s_chunks;
     auto lo = [&](int q) { return K[q] > 2 ? K[q] : 2; };
     auto hi = [&](int q) { return K[q + 1] < d.nz ? K[q + 1] : d.nz; };
@@ -1146,7 +1155,8 @@ int dsg::solvelpres_pre(dsg_ctx *ctx) {
   } else {
     DSG_CK(ctx, dsg::stress(S.p, u, v, w, cc, d, r1, r2, r10, r20, st));
     DSG_CK(ctx, dsg::bc_tensor(S.p, d, st));
-    DSG_CK(ctx, dsg::abcei(a, b, c, ei, cc, rho_r1, rho_r2, d, st));
+    DSG_CK(ctx, dsg::abcei(a, b, c, ei, cc, rho_r1, rho_r2, d, st, ctx->diag64));
+    ctx->diag_fresh = true;
     DSG_CK(ctx, dsg::predictor(w1, w2, w3, u, v, w, a, b, c, S.p, d, horgrav, stdgrav, st));
   }
   DSG_CK(ctx, dsg::bc_w(w1, w2, w3, u, v, w, ctx->red_partials, d, st));

@@ -107,7 +107,9 @@ cudaError_t addint(double *uf, const double *uc, double *res, Dims df, cudaStrea
 cudaError_t acfromac(double *a, double *b, double *c, double *ei, const double *a2, const double *b2,
                      const double *c2, Dims dc, cudaStream_t st);
 cudaError_t abcei(double *a, double *b, double *c, double *ei, const double *cc, double r1, double r2,
-                  Dims d, cudaStream_t st);
+                  Dims d, cudaStream_t st, double *diag = nullptr);
+// diag = the sum of the six face coefficients of every interior cell
+cudaError_t diag_sum(double *diag, const double *a, const double *b, const double *c, Dims d, cudaStream_t st);
 cudaError_t filterc27(const double *cc, double *cf, Dims d, cudaStream_t st);
 // relres partial sums: out[0] = sum r^2, out[1] = sum rhs^2 (device, 2 doubles)
 cudaError_t relres_sums(double *out, double *partials, double lengthsize, const double *u,
@@ -208,8 +210,8 @@ cudaError_t prolong32_split(float *const u[2], const float *uc, Dims df, int add
 cudaError_t restrict32_split(float *uc, float *const rhs[2], Dims dc, cudaStream_t st);
 cudaError_t split_from64(float *const dst[2], const double *src, Dims d, cudaStream_t st);
 cudaError_t defect64(float *const r32[2], double *out2, double *partials, const double *p, const double *rhs,
-                     const double *a, const double *b, const double *c, Dims d, double lengthsize,
-                     cudaStream_t st);
+                     const double *a, const double *b, const double *c, const double *diag, Dims d,
+                     double lengthsize, cudaStream_t st);
 cudaError_t correct64(double *p, float *const e[2], Dims d, int init, cudaStream_t st);
 cudaError_t to32(float *dst, const double *src, size_t n, cudaStream_t st);
 // init.cu
@@ -271,6 +273,8 @@ struct dsg_ctx {
                               // half) and A holds cc in FP32
   double *f[DSG_NFIELDS];     // fine fields; 0..7 alias lv[ng]
   double *ccf;                // csf filtered volume fraction (local array of csf)
+  double *diag64;             // sum of the six fine face coefficients (the mixed solve's defect)
+  bool diag_fresh = false;    // diag64 was formed from the current coefficients (this step's abcei)
   double *red_partials;       // reduction partials (kRedBlocks * 4 doubles)
   double *red_out;            // device reduction results (8 doubles)
   double *red_host;           // pinned host mirror of red_out

@@ -84,8 +84,9 @@ __global__ void k_acfromac32(float *__restrict__ a, float *__restrict__ b, float
 __global__ void k_defect64(float *__restrict__ r_ev, float *__restrict__ r_od, Split sp,
                            double *__restrict__ partials, const double *__restrict__ p,
                            const double *__restrict__ rhs, const double *__restrict__ a,
-                           const double *__restrict__ b, const double *__restrict__ c, Dims d, double h2i) {
-  b_defect64(blockIdx, gridDim, r_ev, r_od, sp, partials, p, rhs, a, b, c, d, h2i);
+                           const double *__restrict__ b, const double *__restrict__ c,
+                           const double *__restrict__ diag, Dims d, double h2i) {
+  b_defect64(blockIdx, gridDim, r_ev, r_od, sp, partials, p, rhs, a, b, c, diag, d, h2i);
 }
 
 __global__ void k_fold2(const double *__restrict__ partials, double *__restrict__ out) {
@@ -218,12 +219,13 @@ cudaError_t acfromac64to32(float *a, float *b, float *c, float *ei, const double
 }
 
 cudaError_t defect64(float *const r32[2], double *out2, double *partials, const double *p, const double *rhs,
-                     const double *a, const double *b, const double *c, Dims d, double lengthsize,
-                     cudaStream_t st) {
+                     const double *a, const double *b, const double *c, const double *diag, Dims d,
+                     double lengthsize, cudaStream_t st) {
   const double h1 = lengthsize / (d.nx - 2);
   const double h2i = 1.0 / (h1 * h1);
   const Split sp{(d.nx - 2) >> 1, d.ny - 2, d.nz - 2};
-  DSG_COUNT k_defect64<<<kRedBlocks, kRedThreads, 0, st>>>(r32[0], r32[1], sp, partials, p, rhs, a, b, c, d, h2i);
+  DSG_COUNT k_defect64<<<kRedBlocks, kRedThreads, 0, st>>>(r32[0], r32[1], sp, partials, p, rhs, a, b, c, diag, d,
+                                                           h2i);
   DSG_COUNT k_fold2<<<1, kRedThreads, 0, st>>>(partials, out2);
   return cudaGetLastError();
 }

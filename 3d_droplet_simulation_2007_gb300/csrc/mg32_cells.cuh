@@ -502,13 +502,18 @@ __device__ __forceinline__ void b_acfromac32(const uint3 B, const uint3 G, float
 }
 
 // ---- FP64 defect-correction kernels ----------------------------------------
-// r = rhs - L p in FP64 over the interior (the expression of resid,
-// main.f:3912-3925, with bc_scalar ghosts read virtually); writes (float)r as
-// the FP32 fine rhs and per-block partial sums of r^2 and rhs^2.
+// r = rhs - L p in FP64 over the interior (resid's operator, main.f:3912-3925,
+// with bc_scalar ghosts read virtually), in flux form: L p = h2i (sum of
+// a_f p_f - diag p) with p_f the neighbour (the cell itself behind a Neumann
+// face, 0 behind the Dirichlet one) and diag the sum of the six face
+// coefficients (stored by abcei), the same operator as sum a_f (p_f - p) in
+// 11 instead of 17 FP64 operations per cell.  Writes (float)r as the FP32
+// fine rhs and per-block partial sums of r^2 and rhs^2.
 __device__ __forceinline__ void b_defect64(const uint3 B, const uint3 G, float *__restrict__ r_ev, float *__restrict__ r_od, Split sp,
                            double *__restrict__ partials, const double *__restrict__ p,
                            const double *__restrict__ rhs, const double *__restrict__ a,
-                           const double *__restrict__ b, const double *__restrict__ c, Dims d, double h2i) {
+                           const double *__restrict__ b, const double *__restrict__ c,
+                           const double *__restrict__ diag, Dims d, double h2i) {
   const size_t n = (size_t)(d.nx - 2) * (d.ny - 2) * (d.nz - 2);
   const size_t sy = d.sy(), sz = d.sz();
   double rr = 0.0, bb = 0.0;
@@ -526,9 +531,14 @@ __device__ __forceinline__ void b_defect64(const uint3 B, const uint3 G, float *
     const double zp = (k + 1 == d.nz) ? uc : p[q + sz];
     const double zm = (k - 1 == 1) ? uc : p[q - sz];
     const double f = rhs[q];
-    const double r = -h2i * (a[q] * (xp - uc) + a[q - 1] * (xm - uc) + b[q] * (yp - uc) + b[q - sy] * (ym - uc) +
-                             c[q] * (zp - uc) + c[q - sz] * (zm - uc)) +
-                     f;
+    double lp = a[q] * xp;
+    lp = fma(a[q - 1], xm, lp);
+    lp = fma(b[q], yp, lp);
+    lp = fma(b[q - sy], ym, lp);
+    lp = fma(c[q], zp, lp);
+    lp = fma(c[q - sz], zm, lp);
+    lp = fma(-diag[q], uc, lp);
+    const double r = fma(-h2i, lp, f);
     (((i + j + k) & 1) ? r_od : r_ev)[sp.at((i - 2) >> 1, j, k)] = (float)r;
     rr += r * r;
     bb += f * f;

@@ -293,9 +293,12 @@ __global__ void k_bc_coef(double *__restrict__ a, double *__restrict__ b, double
   }
 }
 
-__global__ void k_ei(double *__restrict__ ei, const double *__restrict__ a, const double *__restrict__ b,
-                     const double *__restrict__ c, Dims d, double k_gas, double k_liq, double e_gas,
-                     double e_liq) {
+// ei = 1 / (sum of the six face coefficients); with diag non-null the sum
+// itself is stored there too (the diagonal of the operator, for the
+// mixed solve's flux-form defect).
+__global__ void k_ei(double *__restrict__ ei, double *__restrict__ diag, const double *__restrict__ a,
+                     const double *__restrict__ b, const double *__restrict__ c, Dims d, double k_gas,
+                     double k_liq, double e_gas, double e_liq, double d_gas, double d_liq) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
   const int k = blockIdx.z + 2;
@@ -305,10 +308,25 @@ __global__ void k_ei(double *__restrict__ ei, const double *__restrict__ a, cons
   // Six equal bulk faces: the precomputed 1/(k+k+k+k+k+k).
   if (same_bits(s0, s1) && same_bits(s0, s2) && same_bits(s0, s3) && same_bits(s0, s4) && same_bits(s0, s5) &&
       (same_bits(s0, k_gas) || same_bits(s0, k_liq))) {
-    ei[q] = same_bits(s0, k_gas) ? e_gas : e_liq;
+    const bool gas = same_bits(s0, k_gas);
+    ei[q] = gas ? e_gas : e_liq;
+    if (diag) diag[q] = gas ? d_gas : d_liq;
     return;
   }
-  ei[q] = 1.0 / (s0 + s1 + s2 + s3 + s4 + s5);
+  const double sum = s0 + s1 + s2 + s3 + s4 + s5;
+  ei[q] = 1.0 / sum;
+  if (diag) diag[q] = sum;
+}
+
+// diag = the sum of the six face coefficients of every interior cell.
+__global__ void k_diag(double *__restrict__ diag, const double *__restrict__ a, const double *__restrict__ b,
+                       const double *__restrict__ c, Dims d) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
+  const int k = blockIdx.z + 2;
+  if (i > d.nx - 1 || j > d.ny - 1) return;
+  const size_t q = d.ix(i, j, k);
+  diag[q] = a[q] + a[q - 1] + b[q] + b[q - d.sy()] + c[q] + c[q - d.sz()];
 }
 
 // ---- filterc27 (main.f:5473-5511), default-REAL weights -------------------
@@ -611,15 +629,22 @@ cudaError_t acfromac(double *a, double *b, double *c, double *ei, const double *
 }
 
 cudaError_t abcei(double *a, double *b, double *c, double *ei, const double *cc, double r1, double r2,
-                  Dims d, cudaStream_t st) {
+                  Dims d, cudaStream_t st, double *diag) {
   // bulk-face constants, same operation order as the kernels
   const double k_gas = 1.0 / (r1 * (0.0 + 0.0) + r2), k_liq = 1.0 / (r1 * (1.0 + 1.0) + r2);
-  const double e_gas = 1.0 / (k_gas + k_gas + k_gas + k_gas + k_gas + k_gas);
-  const double e_liq = 1.0 / (k_liq + k_liq + k_liq + k_liq + k_liq + k_liq);
+  const double d_gas = k_gas + k_gas + k_gas + k_gas + k_gas + k_gas;
+  const double d_liq = k_liq + k_liq + k_liq + k_liq + k_liq + k_liq;
+  const double e_gas = 1.0 / d_gas, e_liq = 1.0 / d_liq;
   DSG_COUNT k_abc<<<interior_grid(d, kBlk), kBlk, 0, st>>>(a, b, c, cc, r1, r2, k_gas, k_liq, d);
   const dim3 blk(32, 8);
   DSG_COUNT k_bc_coef<<<face_grid(d, blk), blk, 0, st>>>(a, b, c, cc, r1, r2, d);
-  DSG_COUNT k_ei<<<interior_grid(d, kBlk), kBlk, 0, st>>>(ei, a, b, c, d, k_gas, k_liq, e_gas, e_liq);
+  DSG_COUNT k_ei<<<interior_grid(d, kBlk), kBlk, 0, st>>>(ei, diag, a, b, c, d, k_gas, k_liq, e_gas, e_liq, d_gas,
+                                                         d_liq);
+  return cudaGetLastError();
+}
+
+cudaError_t diag_sum(double *diag, const double *a, const double *b, const double *c, Dims d, cudaStream_t st) {
+  DSG_COUNT k_diag<<<interior_grid(d, kBlk), kBlk, 0, st>>>(diag, a, b, c, d);
   return cudaGetLastError();
 }
 
