@@ -110,6 +110,9 @@ class InputData:
     # tolerance mode: 0 = FP64 multigrid in fused multiply-add form (within
     # ulps of the oracle), 1 = the reference's exact operation order
     fp64_exact: int = 0
+    # mixed modes: 1 = each FP32 V-cycle preconditions one GCR step (one
+    # previous direction kept), 0 = the V-cycles iterate on one correction
+    mg32_krylov: int = 0
 
     def as_dict(self):
         return asdict(self)

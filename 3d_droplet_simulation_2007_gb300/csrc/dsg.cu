@@ -476,14 +476,34 @@ int mixed_solve(dsg_ctx *ctx, dsg_mg_stats *s) {
   };
   // one outer iteration: `inner` FP32 V-cycles on the correction equation,
   // FP64 accumulation, FP64 defect and its norms
+  // With mg32_krylov each V-cycle instead starts from zero on the current FP32
+  // residual and its result z = M r is one GCR direction: the FP64 pressure
+  // takes the step that minimises the FP32 residual along z made orthogonal
+  // (in the operator's image) to the previous direction.
   auto iterate = [&]() -> int {
     FineSplit f = fine_split(ctx);
-    DSG_CK(ctx, cudaMemsetAsync(f.u[0], 0, fine_split_bytes(ctx), st));
+    if (!ctx->cfg.mg32_krylov) {
+      DSG_CK(ctx, cudaMemsetAsync(f.u[0], 0, fine_split_bytes(ctx), st));
+      for (int q = 0; q < inner; q++) {
+        int e = vcycle32(ctx, ng);
+        if (e) return e;
+      }
+      DSG_CK(ctx, dsg::correct64(ctx->lv[ng][1], f.u, ctx->fine(), 0, st));
+      return defect_launch(ctx);
+    }
+    float **L = ctx->lv32[ng];
+    const size_t half = fine_split_bytes(ctx) / (2 * sizeof(float));
+    const dsg::GcrBufs g{{L[B32], L[B32] + half}, {L[C32], L[C32] + half}, {L[EI32], L[EI32] + half},
+                         ctx->gcr_partials, ctx->gcr_partials + 4 * dsg::kRedBlocks, ctx->gcr_coef};
+    float r1, r2;
+    phase_coefs(ctx, &r1, &r2);
     for (int q = 0; q < inner; q++) {
+      DSG_CK(ctx, cudaMemsetAsync(f.u[0], 0, fine_split_bytes(ctx), st));
       int e = vcycle32(ctx, ng);
       if (e) return e;
+      DSG_CK(ctx, dsg::gcr_step(q == 0, q == inner - 1, g, ctx->lv[ng][1], f.u, f.r, L[A32], ctx->fine(),
+                                1.0f / level_h2(ctx, ng), r1, r2, st));
     }
-    DSG_CK(ctx, dsg::correct64(ctx->lv[ng][1], f.u, ctx->fine(), 0, st));
     return defect_launch(ctx);
   };
   // Run a phase as a replayed CUDA graph (captured once per sweep-count key),
@@ -757,7 +777,7 @@ int dsg_create(const dsg_config *cfg, dsg_ctx **out) {
   const int nextra = DSG_NFIELDS - 8 + 2;  // fine fields beyond the level arrays + ccf + diag64
   total += nextra * fine;
   total += up(dsg::kRedBlocks * 4 * sizeof(double)) + up(16 * sizeof(double)) + up(sizeof(unsigned long long)) +
-           up(sizeof(unsigned));
+           up(sizeof(unsigned)) + up(dsg::kRedBlocks * 6 * sizeof(double)) + up(16 * sizeof(double));
   cudaError_t e = cudaMalloc(&ctx->arena, total);
   if (e != cudaSuccess) {
     int rc = dsg::cuda_fail(ctx, e, "cudaMalloc(arena)");
@@ -793,6 +813,10 @@ int dsg_create(const dsg_config *cfg, dsg_ctx **out) {
   ctx->stop_flag = (unsigned long long *)p;
   p += up(sizeof(unsigned long long));
   ctx->iface_count = (unsigned *)p;
+  p += up(sizeof(unsigned));
+  ctx->gcr_partials = (double *)p;
+  p += up(dsg::kRedBlocks * 6 * sizeof(double));
+  ctx->gcr_coef = (double *)p;
   e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMallocHost(&ctx->red_host, 16 * sizeof(double));
   if (e == cudaSuccess) e = cudaMemsetAsync(ctx->arena, 0, total, ctx->own_stream);

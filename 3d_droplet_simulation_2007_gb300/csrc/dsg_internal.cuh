@@ -214,6 +214,15 @@ cudaError_t defect64(float *const r32[2], double *out2, double *partials, const 
                      double lengthsize, cudaStream_t st);
 cudaError_t correct64(double *p, float *const e[2], Dims d, int init, cudaStream_t st);
 cudaError_t to32(float *dst, const double *src, size_t n, cudaStream_t st);
+// One GCR iteration of the mixed solve on the finest level, after the V-cycle
+// that left z = M r in the split correction arrays: w = A z, the step
+// lengths, then (not last) d, q, r and p updated, or (last) p += alpha d.
+struct GcrBufs {
+  float *w[2], *d[2], *q[2];  // colour-split pairs
+  double *p1, *p2, *coef;     // block sums of the apply (4 per block) and update (2), step lengths
+};
+cudaError_t gcr_step(int first, int last, const GcrBufs &g, double *p, float *const z[2], float *const r[2],
+                     const float *cc, Dims d, float h2i, float r1, float r2, cudaStream_t st);
 // init.cu
 cudaError_t init_drop(double *cc, double *u, double *v, double *w, Dims d, double h, double x0, double y0,
                       double z0, double radius, double yvel1, double yvel2, double zvel1, double zvel2,
@@ -276,6 +285,8 @@ struct dsg_ctx {
   double *diag64;             // sum of the six fine face coefficients (the mixed solve's defect)
   bool diag_fresh = false;    // diag64 was formed from the current coefficients (this step's abcei)
   double *red_partials;       // reduction partials (kRedBlocks * 4 doubles)
+  double *gcr_partials;       // GCR block sums of the mixed solve (kRedBlocks * 6 doubles)
+  double *gcr_coef;           // GCR step lengths and sums (16 doubles)
   double *red_out;            // device reduction results (8 doubles)
   double *red_host;           // pinned host mirror of red_out
   unsigned long long *stop_flag;  // device: first cell where CalcH3d would STOP (code << 48 | index)

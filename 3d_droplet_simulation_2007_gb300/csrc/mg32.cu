@@ -112,6 +112,202 @@ const dim3 kBlk(32, 4, 1);
 
 inline int flat_blocks(size_t n) { return (int)((n + 255) / 256 < 8192 ? (n + 255) / 256 : 8192); }
 
+// ---- GCR over the FP32 V-cycle ----------------------------------------------
+//
+// The kernels below run over the finest level's colour-split index range
+// t = m + hx (j - 2 + ny2 (k - 2)), both colours per index, so that every
+// split array is read with unit stride and the FP64 pressure (natural layout)
+// in runs of two cells.  Sums are formed per thread in FP32, per block in
+// FP64 in a fixed order, and folded by one block: the results are
+// deterministic.
+
+// Index t's split coordinates.
+struct SplitIx {
+  int m, j, k;
+};
+__device__ __forceinline__ SplitIx split_ix(unsigned t, Split sp) {
+  const unsigned rem = t / (unsigned)sp.hx, kk = rem / (unsigned)sp.ny2;
+  return SplitIx{(int)(t - rem * (unsigned)sp.hx), (int)(rem - kk * (unsigned)sp.ny2) + 2, (int)kk + 2};
+}
+
+// NS FP64 sums of the block (thread 0 holds them afterwards) written to
+// out[NS * block + s].
+template <int NS>
+__device__ __forceinline__ void block_partials(double (&v)[NS], double *__restrict__ out) {
+  __shared__ double sh[NS][kRedThreads / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int s = 0; s < NS; s++) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[s] += __shfl_down_sync(0xffffffffu, v[s], o);
+    if (lane == 0) sh[s][wid] = v[s];
+  }
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int s = 0; s < NS; s++) {
+      double x = lane < kRedThreads / 32 ? sh[s][lane] : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+      if (lane == 0) out[NS * blockIdx.x + s] = x;
+    }
+  }
+}
+
+// w = A z (A z = lap(z) / h^2, the operator whose residual the V-cycle
+// restricts), stored when STORE, and the sums (w,w), (r,w), (w,q), (r,q) of
+// the current residual r and the previous direction's image q (not read on
+// the first iteration).
+template <bool FIRST, bool STORE>
+__global__ void __launch_bounds__(kRedThreads) k_gcr_apply(float *__restrict__ w_ev, float *__restrict__ w_od,
+                                                           double *__restrict__ partials,
+                                                           const float *__restrict__ z_ev,
+                                                           const float *__restrict__ z_od,
+                                                           const float *__restrict__ r_ev,
+                                                           const float *__restrict__ r_od,
+                                                           const float *__restrict__ q_ev,
+                                                           const float *__restrict__ q_od, const float *__restrict__ cc,
+                                                           Dims d, Split sp, float h2i, float r1, float r2) {
+  const unsigned n = (unsigned)sp.hx * (unsigned)sp.ny2 * (unsigned)sp.nz2;
+  float ww = 0.f, rw = 0.f, wq = 0.f, rq = 0.f;
+  for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const SplitIx x = split_ix(t, sp);
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+      const float w = h2i * lap32_split_cell(c ? z_od : z_ev, c ? z_ev : z_od, cc, d, sp, c, r1, r2, x.m, x.j, x.k, t);
+      if (STORE) (c ? w_od : w_ev)[t] = w;
+      const float r = (c ? r_od : r_ev)[t];
+      ww = fmaf(w, w, ww);
+      rw = fmaf(r, w, rw);
+      if (!FIRST) {
+        const float q = (c ? q_od : q_ev)[t];
+        wq = fmaf(w, q, wq);
+        rq = fmaf(r, q, rq);
+      }
+    }
+  }
+  double v[4] = {ww, rw, wq, rq};
+  block_partials<4>(v, partials);
+}
+
+// Step lengths from the sums: new direction d = z - beta d_prev with image
+// q = w - beta q_prev orthogonal to q_prev, and the step alpha that minimises
+// |r - alpha q|.  coef = {alpha, beta, (w,w), (r,w), (w,q), (r,q), (q,q) of
+// the previous direction}.  A breakdown (a non-finite or non-positive
+// denominator) gives alpha = beta = 0: no update, and the FP64 defect that
+// follows decides.
+template <bool FIRST>
+__global__ void __launch_bounds__(kRedThreads) k_gcr_fold(const double *__restrict__ p1,
+                                                          const double *__restrict__ p2, double *__restrict__ coef,
+                                                          int nb) {
+  double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int b = threadIdx.x; b < nb; b += kRedThreads) {
+#pragma unroll
+    for (int s = 0; s < 4; s++) v[s] += p1[4 * b + s];
+    if (!FIRST) v[4] += p2[2 * b];
+  }
+  __shared__ double tot[5];
+  __shared__ double sh[5][kRedThreads / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int s = 0; s < 5; s++) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[s] += __shfl_down_sync(0xffffffffu, v[s], o);
+    if (lane == 0) sh[s][wid] = v[s];
+  }
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int s = 0; s < 5; s++) {
+      double x = lane < kRedThreads / 32 ? sh[s][lane] : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+      if (lane == 0) tot[s] = x;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const double ww = tot[0], rw = tot[1], wq = tot[2], rq = tot[3], qq0 = tot[4];
+    double alpha, beta;
+    if (FIRST) {
+      beta = 0.0;
+      alpha = rw / ww;
+    } else {
+      beta = wq / qq0;
+      const double qq = ww - beta * wq;  // |w - beta q_prev|^2
+      alpha = (rw - beta * rq) / qq;
+      if (!(qq > 0.0) || !(qq0 > 0.0)) alpha = beta = 0.0;
+    }
+    if (!(ww > 0.0) || !isfinite(alpha) || !isfinite(beta)) alpha = beta = 0.0;
+    coef[0] = alpha;
+    coef[1] = beta;
+#pragma unroll
+    for (int s = 0; s < 5; s++) coef[2 + s] = tot[s];
+  }
+}
+
+// d = z - beta d, q = w - beta q (FIRST: d = z, q = w), r -= alpha q and the
+// FP64 pressure p += alpha d; sums (q,q) and (r,r) of the new q and r.
+template <bool FIRST>
+__global__ void __launch_bounds__(kRedThreads) k_gcr_update(double *__restrict__ p, float *__restrict__ d_ev,
+                                                            float *__restrict__ d_od, float *__restrict__ q_ev,
+                                                            float *__restrict__ q_od, float *__restrict__ r_ev,
+                                                            float *__restrict__ r_od, double *__restrict__ partials,
+                                                            const float *__restrict__ z_ev,
+                                                            const float *__restrict__ z_od,
+                                                            const float *__restrict__ w_ev,
+                                                            const float *__restrict__ w_od,
+                                                            const double *__restrict__ coef, Dims d, Split sp) {
+  const double alpha = coef[0];
+  const float alpha32 = (float)alpha, beta = (float)coef[1];
+  const unsigned n = (unsigned)sp.hx * (unsigned)sp.ny2 * (unsigned)sp.nz2;
+  float qq = 0.f, rr = 0.f;
+  for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const SplitIx x = split_ix(t, sp);
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+      float *dc = c ? d_od : d_ev, *qc = c ? q_od : q_ev, *rc = c ? r_od : r_ev;
+      const float z = (c ? z_od : z_ev)[t], w = (c ? w_od : w_ev)[t];
+      const float dn = FIRST ? z : fmaf(-beta, dc[t], z);
+      const float qn = FIRST ? w : fmaf(-beta, qc[t], w);
+      const float rn = fmaf(-alpha32, qn, rc[t]);
+      dc[t] = dn;
+      qc[t] = qn;
+      rc[t] = rn;
+      const int i = 2 + 2 * x.m + ((x.j + x.k + c) & 1);
+      const unsigned q = ix32(d, i, x.j, x.k);
+      p[q] = fma(alpha, (double)dn, p[q]);
+      qq = fmaf(qn, qn, qq);
+      rr = fmaf(rn, rn, rr);
+    }
+  }
+  double v[2] = {qq, rr};
+  block_partials<2>(v, partials);
+}
+
+// Last iteration: p += alpha (z - beta d) (FIRST: p += alpha z).
+template <bool FIRST>
+__global__ void __launch_bounds__(kRedThreads) k_gcr_final(double *__restrict__ p, const float *__restrict__ z_ev,
+                                                           const float *__restrict__ z_od,
+                                                           const float *__restrict__ d_ev,
+                                                           const float *__restrict__ d_od,
+                                                           const double *__restrict__ coef, Dims d, Split sp) {
+  const double alpha = coef[0];
+  const float beta = (float)coef[1];
+  const unsigned n = (unsigned)sp.hx * (unsigned)sp.ny2 * (unsigned)sp.nz2;
+  for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const SplitIx x = split_ix(t, sp);
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+      const float z = (c ? z_od : z_ev)[t];
+      const float dn = FIRST ? z : fmaf(-beta, (c ? d_od : d_ev)[t], z);
+      const int i = 2 + 2 * x.m + ((x.j + x.k + c) & 1);
+      const unsigned q = ix32(d, i, x.j, x.k);
+      p[q] = fma(alpha, (double)dn, p[q]);
+    }
+  }
+}
+
 }  // namespace
 
 cudaError_t relax32_n(int n, float *u, float h2, const float *rhs, const float *a, const float *b, const float *c,
@@ -238,6 +434,40 @@ cudaError_t correct64(double *p, float *const e[2], Dims d, int init, cudaStream
 
 cudaError_t to32(float *dst, const double *src, size_t n, cudaStream_t st) {
   DSG_COUNT k_to32<<<flat_blocks(n), 256, 0, st>>>(dst, src, n);
+  return cudaGetLastError();
+}
+
+cudaError_t gcr_step(int first, int last, const GcrBufs &g, double *p, float *const z[2], float *const r[2],
+                     const float *cc, Dims d, float h2i, float r1, float r2, cudaStream_t st) {
+  const Split sp{(d.nx - 2) >> 1, d.ny - 2, d.nz - 2};
+  const int nb = kRedBlocks;
+  if (first) {
+    if (last)
+      DSG_COUNT k_gcr_apply<true, false><<<nb, kRedThreads, 0, st>>>(g.w[0], g.w[1], g.p1, z[0], z[1], r[0], r[1],
+                                                                    g.q[0], g.q[1], cc, d, sp, h2i, r1, r2);
+    else
+      DSG_COUNT k_gcr_apply<true, true><<<nb, kRedThreads, 0, st>>>(g.w[0], g.w[1], g.p1, z[0], z[1], r[0], r[1],
+                                                                   g.q[0], g.q[1], cc, d, sp, h2i, r1, r2);
+    DSG_COUNT k_gcr_fold<true><<<1, kRedThreads, 0, st>>>(g.p1, g.p2, g.coef, nb);
+    if (last)
+      DSG_COUNT k_gcr_final<true><<<nb, kRedThreads, 0, st>>>(p, z[0], z[1], g.d[0], g.d[1], g.coef, d, sp);
+    else
+      DSG_COUNT k_gcr_update<true><<<nb, kRedThreads, 0, st>>>(p, g.d[0], g.d[1], g.q[0], g.q[1], r[0], r[1], g.p2,
+                                                              z[0], z[1], g.w[0], g.w[1], g.coef, d, sp);
+  } else {
+    if (last)
+      DSG_COUNT k_gcr_apply<false, false><<<nb, kRedThreads, 0, st>>>(g.w[0], g.w[1], g.p1, z[0], z[1], r[0], r[1],
+                                                                     g.q[0], g.q[1], cc, d, sp, h2i, r1, r2);
+    else
+      DSG_COUNT k_gcr_apply<false, true><<<nb, kRedThreads, 0, st>>>(g.w[0], g.w[1], g.p1, z[0], z[1], r[0], r[1],
+                                                                    g.q[0], g.q[1], cc, d, sp, h2i, r1, r2);
+    DSG_COUNT k_gcr_fold<false><<<1, kRedThreads, 0, st>>>(g.p1, g.p2, g.coef, nb);
+    if (last)
+      DSG_COUNT k_gcr_final<false><<<nb, kRedThreads, 0, st>>>(p, z[0], z[1], g.d[0], g.d[1], g.coef, d, sp);
+    else
+      DSG_COUNT k_gcr_update<false><<<nb, kRedThreads, 0, st>>>(p, g.d[0], g.d[1], g.q[0], g.q[1], r[0], r[1], g.p2,
+                                                               z[0], z[1], g.w[0], g.w[1], g.coef, d, sp);
+  }
   return cudaGetLastError();
 }
 

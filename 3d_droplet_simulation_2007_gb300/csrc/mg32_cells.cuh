@@ -165,6 +165,37 @@ __device__ __forceinline__ void relax32_split_cell(float *__restrict__ self, con
   self[qs] = omega * temp + (1.f - omega) * uc;
 }
 
+// Operator of the finest-level FP32 correction equation at the colour-c cell of
+// split index (m, j, k) (qs its offset): sum_f a_f (z_f - z) over the six faces,
+// with the neighbours, virtual ghosts and face coefficients of
+// relax32_split_cell.  The residual of relax is rhs - lap / h^2.
+__device__ __forceinline__ float lap32_split_cell(const float *__restrict__ self, const float *__restrict__ other,
+                                                  const float *__restrict__ cc, Dims d, Split sp, int c, float r1,
+                                                  float r2, int m, int j, int k, unsigned qs) {
+  const int p = (j + k + c) & 1;
+  const int i = 2 + 2 * m + p;
+  const int row = sp.hx, plane = sp.hx * sp.ny2;
+  const float *o = other + qs;
+  const float uc = self[qs];
+  const float xm = (m == 0 && p == 0) ? uc : o[p - 1];
+  const float xp = (m == sp.hx - 1 && p == 1) ? 0.f : o[p];
+  const float ym = (j == 2) ? uc : o[-row];
+  const float yp = (j == d.ny - 1) ? uc : o[row];
+  const float zm = (k == 2) ? uc : o[-plane];
+  const float zp = (k == d.nz - 1) ? uc : o[plane];
+  const unsigned q = (unsigned)(i - 1) + (unsigned)d.nx * ((unsigned)(j - 1) + (unsigned)d.ny * (unsigned)(k - 1));
+  const float *cq = cc + q;
+  const int sy = d.nx, sz = d.nx * d.ny;
+  const float c0 = cq[0];
+  const float ae = face_coef(c0, cq[1], r1, r2);
+  const float aw = (i == 2) ? ae : face_coef(cq[-1], c0, r1, r2);
+  const float bn = face_coef(c0, cq[sy], r1, r2);
+  const float bs = face_coef(cq[-sy], c0, r1, r2);
+  const float ct = face_coef(c0, cq[sz], r1, r2);
+  const float cb = face_coef(cq[-sz], c0, r1, r2);
+  return ae * (xp - uc) + aw * (xm - uc) + bn * (yp - uc) + bs * (ym - uc) + ct * (zp - uc) + cb * (zm - uc);
+}
+
 // One colour pass on the finest level: each thread updates split indices m
 // and m + blockDim.x of its row (two independent cells in flight; 45.7 against
 // 47.2 us per pass with one).

@@ -110,6 +110,9 @@ typedef struct dsg_config {
   int fp64_exact;      /* DSG_MODE_TOL_FP64: 0 = sweeps, residuals and norm as fused multiply-adds (fewer
                           FP64 operations, results within ulps of the oracle), 1 = the reference's operation
                           order (bit-identical to the oracle).  DSG_MODE_REF_EXACT always keeps that order. */
+  int mg32_krylov;     /* mixed modes: 0 = the FP32 V-cycles between two FP64 defects iterate on one
+                          correction, 1 = each V-cycle preconditions one step of GCR (generalised conjugate
+                          residual keeping one previous direction; the step minimises the FP32 residual) */
 } dsg_config;
 
 /* Non-dimensional scalars and adaptive counters (COMMON /PHYSICS/, /DIFF/,

@@ -25,15 +25,17 @@ def _sync_state(gpu, ora):
     gpu.set_scalars(s)
 
 
-@pytest.mark.parametrize("n,prolong", [(16, 0), (32, 0), (32, 1)])
-def test_mixed_matches_fp64_oracle(gpu_lib, n, prolong):
-    """prolong 0: trilinear FP32 prolongation, 1: the reference's injection."""
+@pytest.mark.parametrize("n,prolong,krylov", [(16, 0, 0), (32, 0, 0), (32, 1, 0), (16, 0, 1), (32, 0, 1),
+                                               (32, 1, 1), (64, 0, 1)])
+def test_mixed_matches_fp64_oracle(gpu_lib, n, prolong, krylov):
+    """prolong 0: trilinear FP32 prolongation, 1: the reference's injection;
+    krylov 1: each V-cycle preconditions a GCR step."""
     dsg = gpu_lib
     from oracle import Oracle
     tol = 1e-10
     ora = Oracle(dsg.config.droplet(n, mode=dsg.config.MODE_TOL_FP64, tol=tol).as_dict())
-    gpu = dsg.Solver(dsg.config.droplet(n, mode=dsg.config.MODE_TOL_MIXED, tol=tol).replace(mg32_prolong=prolong),
-                     init=False)
+    gpu = dsg.Solver(dsg.config.droplet(n, mode=dsg.config.MODE_TOL_MIXED, tol=tol).replace(
+        mg32_prolong=prolong, mg32_krylov=krylov), init=False)
     for t in range(1, 6):
         _sync_state(gpu, ora)
         ora.step(t)
@@ -102,3 +104,26 @@ def test_mixed_generalised_grid(gpu_lib):
         assert st["converged"] == 1 and st["relres"] < tol, st
         for name in ("p", "u", "v", "w", "cc"):
             assert relerr(gpu.field(name), ora.field(name)) < 1e-7, (t, name)
+
+
+def test_gcr_cuts_vcycles_and_is_deterministic(gpu_lib):
+    """GCR over the FP32 V-cycle (mg32_krylov = 1) reaches the tolerance with
+    fewer V-cycles over eight steps than the V-cycles iterated alone, keeps the
+    liquid volume of the stationary run, and repeats its own bits."""
+    dsg = gpu_lib
+    base = dsg.config.droplet(64, mode=dsg.config.MODE_TOL_MIXED, tol=1e-10, impact_speed=3.0, noise_si=1e-4)
+    runs = {}
+    for key, kr in (("stationary", 0), ("gcr", 1), ("gcr_again", 1)):
+        with dsg.Solver(base.replace(mg32_krylov=kr)) as s:
+            sts = [s.step(t) for t in range(1, 9)]
+            assert all(st["converged"] == 1 and st["relres"] < 1e-10 for st in sts), sts
+            runs[key] = ([st["vcycles"] for st in sts], s.liquid_volume(),
+                         {f: s.field(f).copy() for f in ("p", "u", "v", "w", "cc")})
+    vs, vg = runs["stationary"][0], runs["gcr"][0]
+    assert sum(vg) < sum(vs), (vg, vs)
+    assert abs(runs["gcr"][1] - runs["stationary"][1]) / runs["stationary"][1] < 1e-9
+    assert runs["gcr"][0] == runs["gcr_again"][0]
+    for f in ("p", "u", "v", "w", "cc"):
+        assert np.array_equal(runs["gcr"][2][f], runs["gcr_again"][2][f]), f
+        assert relerr(runs["gcr"][2][f], runs["stationary"][2][f]) < 1e-5, f
+
