@@ -969,6 +969,8 @@ int batch_solve(BatchSolve *b, const std::vector<int> &active, std::vector<dsg_m
       e = dsg::diag_sum(c->diag64, L[4], L[5], L[6], c->fine(), c->stream);
       c->diag_fresh = true;
     }
+    // the member's own FP32 hierarchy (side stream) ends before the batch forms it again
+    if (e == cudaSuccess && c->coef32_async) e = cudaStreamWaitEvent(c->stream, c->coef_ev, 0);
     if (e == cudaSuccess) e = cudaEventRecord(b->ev_member[i], c->stream);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(b->st, b->ev_member[i], 0);
     if (e != cudaSuccess) return set_error(nullptr, DSG_E_CUDA, "batched solve: join: %s", cudaGetErrorString(e));

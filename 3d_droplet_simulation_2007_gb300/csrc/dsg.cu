@@ -397,9 +397,8 @@ bool graph_matches(const GraphRec &g, const int key[6]) {
 // FP32 hierarchy: cc in FP32 on the finest level (its relax forms the face
 // coefficients itself), coarse coefficients by acfromac from the FP64 fine
 // coefficients of abcei.
-int coef_hierarchy32(dsg_ctx *ctx) {
+int coef_hierarchy32(dsg_ctx *ctx, cudaStream_t st) {
   const int ng = ctx->ng;
-  cudaStream_t st = ctx->stream;
   double **F = ctx->lv[ng];
   DSG_CK(ctx, dsg::to32(ctx->lv32[ng][A32], F[0], ctx->fine().count(), st));
   if (ng >= 2) {
@@ -410,6 +409,26 @@ int coef_hierarchy32(dsg_ctx *ctx) {
     float **C = ctx->lv32[g], **Fi = ctx->lv32[g + 1];
     DSG_CK(ctx, dsg::acfromac32(C[A32], C[B32], C[C32], C[EI32], Fi[A32], Fi[B32], Fi[C32], ctx->level(g), st));
   }
+  return DSG_OK;
+}
+
+// In the mixed modes, the FP32 coefficient hierarchy of this step's abcei on
+// the side stream (it reads cc and the FP64 a, b, c, which nothing writes
+// before the solve): it overlaps the FP64-bound momentum kernels.
+int coef_hierarchy_side(dsg_ctx *ctx) {
+  ctx->coef32_async = false;
+  if (ctx->cfg.mode != DSG_MODE_TOL_MIXED && ctx->cfg.mode != DSG_MODE_LEARNED) return DSG_OK;
+  if (!ctx->side) {
+    DSG_CK(ctx, cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
+    DSG_CK(ctx, cudaEventCreateWithFlags(&ctx->side_start, cudaEventDisableTiming));
+    DSG_CK(ctx, cudaEventCreateWithFlags(&ctx->coef_ev, cudaEventDisableTiming));
+  }
+  DSG_CK(ctx, cudaEventRecord(ctx->side_start, ctx->stream));
+  DSG_CK(ctx, cudaStreamWaitEvent(ctx->side, ctx->side_start, 0));
+  int rc = coef_hierarchy32(ctx, ctx->side);
+  if (rc) return rc;
+  DSG_CK(ctx, cudaEventRecord(ctx->coef_ev, ctx->side));
+  ctx->coef32_async = true;
   return DSG_OK;
 }
 
@@ -468,9 +487,11 @@ int mixed_solve(dsg_ctx *ctx, dsg_mg_stats *s) {
   int key[6] = {pre32(ctx), post32(ctx), ctx->s.ntop, ctx->cfg.cycles, 0, ctx->prof ? 1 : 0};
   // start: FP32 coefficient hierarchy, FP32 FMG guess, first FP64 defect
   auto first = [&]() -> int {
-    int q = coef_hierarchy32(ctx);
-    if (q) return q;
-    q = fmg32(ctx);
+    if (!ctx->coef32_async) {
+      int q = coef_hierarchy32(ctx, st);
+      if (q) return q;
+    }
+    int q = fmg32(ctx);
     if (q) return q;
     return defect_launch(ctx);
   };
@@ -533,13 +554,16 @@ int mixed_solve(dsg_ctx *ctx, dsg_mg_stats *s) {
     DSG_CK(ctx, dsg::diag_sum(ctx->diag64, L[4], L[5], L[6], ctx->fine(), st));
     ctx->diag_fresh = true;
   }
+  if (ctx->coef32_async) DSG_CK(ctx, cudaStreamWaitEvent(st, ctx->coef_ev, 0));
   const bool learned = ctx->cfg.mode == DSG_MODE_LEARNED;
   if (learned && !ctx->net) return dsg::set_error(ctx, DSG_E_STATE, "learned mode without an attached network");
   if (ctx->net) dsg::nn::net_begin_solve(ctx->net);
   if (!learned && (ctx->cfg.warm_start == 1 || ctx->cfg.warm_start == 2)) {
     // previous-step pressure (1) or zero (2) as the initial guess
-    rc = coef_hierarchy32(ctx);
-    if (rc) return rc;
+    if (!ctx->coef32_async) {
+      rc = coef_hierarchy32(ctx, st);
+      if (rc) return rc;
+    }
     if (ctx->cfg.warm_start == 1)
       DSG_CK(ctx, cudaMemcpyAsync(ctx->lv[ng][1], ctx->f[DSG_F_PPREV], ctx->fine().count() * sizeof(double),
                                   cudaMemcpyDeviceToDevice, st));
@@ -548,7 +572,7 @@ int mixed_solve(dsg_ctx *ctx, dsg_mg_stats *s) {
     rc = defect_host(ctx, &r);
     if (rc) return rc;
   } else {
-    key[4] = 0;  // the start does not depend on the inner count
+    key[4] = ctx->coef32_async ? 1 : 0;  // the start with or without the coefficient hierarchy
     rc = run(ctx->g_first, first);
     if (rc) return rc;
     rc = defect_read(ctx, &r);
@@ -631,6 +655,7 @@ int mixed_solve(dsg_ctx *ctx, dsg_mg_stats *s) {
 // statistics, and DSG_E_NOT_CONVERGED when the cycle cap stopped it.
 int dsg::mixed_finish(dsg_ctx *ctx, dsg_mg_stats *s, dsg_mg_stats *stats) {
   ctx->diag_fresh = false;  // the next solve forms it again unless abcei does
+  ctx->coef32_async = false;
   int rc = record_pair(ctx);
   if (rc) return rc;
   ctx->s.last_vcycles = s->vcycles;
@@ -863,6 +888,12 @@ void dsg_destroy(dsg_ctx *ctx) {
     if (ctx->s_chunk_ev[q]) cudaEventDestroy(ctx->s_chunk_ev[q]);
   }
   if (ctx->xfer_start) cudaEventDestroy(ctx->xfer_start);
+  if (ctx->side) {
+    cudaStreamSynchronize(ctx->side);
+    cudaStreamDestroy(ctx->side);
+  }
+  if (ctx->side_start) cudaEventDestroy(ctx->side_start);
+  if (ctx->coef_ev) cudaEventDestroy(ctx->coef_ev);
   for (cudaEvent_t e : ctx->prof_ev) cudaEventDestroy(e);
   for (cudaEvent_t e : ctx->phase_ev) cudaEventDestroy(e);
   graph_release(ctx->g_first);
@@ -889,6 +920,12 @@ int64_t dsg_device_bytes(const dsg_ctx *ctx) { return ctx ? (int64_t)ctx->arena_
 
 int dsg_upload(dsg_ctx *ctx, int field, const double *host) {
   if (!ctx || !host || field < 0 || field >= DSG_NFIELDS) return dsg::set_error(ctx, DSG_E_ARG, "bad upload");
+  if (field == DSG_F_CC || field == DSG_F_A || field == DSG_F_B || field == DSG_F_C) {
+    // coefficients or volume fraction replaced: the next solve forms its
+    // diagonal and FP32 hierarchy from them
+    ctx->diag_fresh = false;
+    ctx->coef32_async = false;
+  }
   DSG_CK(ctx, cudaMemcpyAsync(ctx->f[field], host, ctx->fine().count() * sizeof(double), cudaMemcpyHostToDevice,
                               ctx->stream));
   DSG_CK(ctx, cudaStreamSynchronize(ctx->stream));
@@ -1161,6 +1198,8 @@ int dsg::solvelpres_pre(dsg_ctx *ctx) {
     // values as in the unsplit order.
     DSG_CK(ctx, dsg::abcei(a, b, c, ei, cc, rho_r1, rho_r2, d, st, ctx->diag64));
     ctx->diag_fresh = true;
+    int rc = coef_hierarchy_side(ctx);
+    if (rc) return rc;
     const int *K = ctx->s_chunk_k, n = ctx->s_chunks;
     auto lo = [&](int q) { return K[q] > 2 ? K[q] : 2; };
     auto hi = [&](int q) { return K[q + 1] < d.nz ? K[q + 1] : d.nz; };
@@ -1181,6 +1220,8 @@ int dsg::solvelpres_pre(dsg_ctx *ctx) {
     DSG_CK(ctx, dsg::bc_tensor(S.p, d, st));
     DSG_CK(ctx, dsg::abcei(a, b, c, ei, cc, rho_r1, rho_r2, d, st, ctx->diag64));
     ctx->diag_fresh = true;
+    int rc = coef_hierarchy_side(ctx);
+    if (rc) return rc;
     DSG_CK(ctx, dsg::predictor(w1, w2, w3, u, v, w, a, b, c, S.p, d, horgrav, stdgrav, st));
   }
   DSG_CK(ctx, dsg::bc_w(w1, w2, w3, u, v, w, ctx->red_partials, d, st));

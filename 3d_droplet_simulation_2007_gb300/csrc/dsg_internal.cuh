@@ -284,6 +284,13 @@ struct dsg_ctx {
   double *ccf;                // csf filtered volume fraction (local array of csf)
   double *diag64;             // sum of the six fine face coefficients (the mixed solve's defect)
   bool diag_fresh = false;    // diag64 was formed from the current coefficients (this step's abcei)
+  // The mixed solve's FP32 coefficient hierarchy, launched on `side` right
+  // after this step's abcei so that it overlaps the rest of the momentum
+  // phase; coef_ev marks its end, and the solve waits for it instead of
+  // forming the hierarchy itself.
+  cudaStream_t side = nullptr;
+  cudaEvent_t side_start = nullptr, coef_ev = nullptr;
+  bool coef32_async = false;
   double *red_partials;       // reduction partials (kRedBlocks * 4 doubles)
   double *gcr_partials;       // GCR block sums of the mixed solve (kRedBlocks * 6 doubles)
   double *gcr_coef;           // GCR step lengths and sums (16 doubles)
