@@ -50,7 +50,7 @@ class DsgConfig(C.Structure):
         ("mg32_prolong", C.c_int), ("mg32_fmg_cycles", C.c_int), ("mg32_fine_npre", C.c_int),
         ("mg32_fine_npost", C.c_int), ("mg32_mid_npre", C.c_int), ("mg32_mid_npost", C.c_int),
         ("mg32_small_npre", C.c_int), ("mg32_small_npost", C.c_int), ("fp64_exact", C.c_int),
-        ("mg32_krylov", C.c_int),
+        ("mg32_krylov", C.c_int), ("mg32_fmg_fine_cycles", C.c_int),
     ]
 
 

@@ -663,17 +663,12 @@ struct Planner {
       }
       prolong(out, top, 0, 0, 0);
       int cycles = 0;
-      for (size_t i = 0; i < n; i++) {
-        dsg_ctx *c = mp[i].c;
-        cycles = std::max(cycles, c->cfg.mg32_fmg_cycles > 0 ? c->cfg.mg32_fmg_cycles : c->cfg.cycles);
-      }
+      for (size_t i = 0; i < n; i++)
+        if (top[i]) cycles = std::max(cycles, mixed::fmg32_cycles(mp[i].c, top[i]));
       for (int cy = 0; cy < cycles; cy++) {
         std::vector<int> t2(top);
-        for (size_t i = 0; i < n; i++) {
-          dsg_ctx *c = mp[i].c;
-          const int ci = c->cfg.mg32_fmg_cycles > 0 ? c->cfg.mg32_fmg_cycles : c->cfg.cycles;
-          if (cy >= ci) t2[i] = 0;
-        }
+        for (size_t i = 0; i < n; i++)
+          if (top[i] && cy >= mixed::fmg32_cycles(mp[i].c, top[i])) t2[i] = 0;
         vcycle(out, t2, 0, 0);
       }
     }

@@ -448,7 +448,7 @@ int fmg32(dsg_ctx *ctx) {
       DSG_CK(ctx, dsg::prolong32_split(f.u, ctx->lv32[j - 1][U32], ctx->level(j), 0, tri32(ctx), st));
     else
       DSG_CK(ctx, dsg::prolong32(ctx->lv32[j][U32], ctx->lv32[j - 1][U32], ctx->level(j), 0, tri32(ctx), st));
-    const int cycles = ctx->cfg.mg32_fmg_cycles > 0 ? ctx->cfg.mg32_fmg_cycles : ctx->cfg.cycles;
+    const int cycles = fmg32_cycles(ctx, j);
     for (int c = 0; c < cycles; c++) {
       int rc = vcycle32(ctx, j);
       if (rc) return rc;

@@ -400,6 +400,13 @@ inline int post32(const dsg_ctx *ctx, int l) {
 
 // Prolongation of the FP32 V-cycles and FMG start: trilinear unless the
 // configuration asks for the reference's injection.
+// V-cycles of the FP32 FMG start at level l (its own count on the finest
+// level when mg32_fmg_fine_cycles > 0).
+inline int fmg32_cycles(const dsg_ctx *ctx, int l) {
+  if (l == ctx->ng && ctx->cfg.mg32_fmg_fine_cycles > 0) return ctx->cfg.mg32_fmg_fine_cycles;
+  return ctx->cfg.mg32_fmg_cycles > 0 ? ctx->cfg.mg32_fmg_cycles : ctx->cfg.cycles;
+}
+
 inline int tri32(const dsg_ctx *ctx) { return ctx->cfg.mg32_prolong == 1 ? 0 : 1; }
 
 inline float level_h2(dsg_ctx *ctx, int l) {

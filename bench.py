@@ -70,6 +70,8 @@ def parse():
                     help="pre,post sweeps of the FP32 V-cycles on the level below the finest")
     ap.add_argument("--krylov", type=int, default=None,
                     help="mixed modes: 1 GCR over the FP32 V-cycle, 0 V-cycles alone (default: the configuration's)")
+    ap.add_argument("--fmg32-fine", type=int, default=None,
+                    help="V-cycles of the FP32 FMG start on the finest level (default: as on the others)")
     ap.add_argument("--tail-nodes", type=int, default=0,
                     help="largest FP32 level (nodes) of the single-block coarse tail (0: default, -1: off)")
     ap.add_argument("--e2e-steps", type=int, default=6)
@@ -98,7 +100,8 @@ def dist_env():
 
 
 def workload(dsg, n, mode, tol, inner=0, graphs=True, tail_nodes=0, omega32=None, start=None, sweeps32=None,
-             prolong32=None, fmg32=None, fine_sweeps32=None, mid_sweeps32=None, small_sweeps32=None, krylov=None):
+             prolong32=None, fmg32=None, fine_sweeps32=None, mid_sweeps32=None, small_sweeps32=None, krylov=None,
+             fmg32_fine=None):
     cfg = dsg.config
     inp = cfg.droplet(n, steps=1000, impact_speed=3.0, noise_si=1e-4, mode=mode, tol=tol,
                       npre=4, npost=4, ntop=4).replace(inner_vcycles=inner, use_graphs=1 if graphs else 0,
@@ -108,6 +111,7 @@ def workload(dsg, n, mode, tol, inner=0, graphs=True, tail_nodes=0, omega32=None
     inp = inp if prolong32 is None else inp.replace(mg32_prolong=prolong32)
     inp = inp if fmg32 is None else inp.replace(mg32_fmg_cycles=fmg32)
     inp = inp if krylov is None else inp.replace(mg32_krylov=krylov)
+    inp = inp if fmg32_fine is None else inp.replace(mg32_fmg_fine_cycles=fmg32_fine)
     if small_sweeps32:
         a, b = (int(x) for x in small_sweeps32.split(","))
         inp = inp.replace(mg32_small_npre=a, mg32_small_npost=b)
@@ -128,8 +132,10 @@ def schedule(inp, mode, dsg):
     m = dsg.config.MODE_NAMES
     if mode in (m["tol_mixed"], m["learned"]):
         fine = (inp.mg32_fine_npre or inp.mg32_npre, inp.mg32_fine_npost or inp.mg32_npost)
-        start = "FP32 full-multigrid start with the guarded learned correction" if mode == m["learned"] else \
-            {0: "FP32 full multigrid", 1: "previous-step pressure", 2: "zero"}[inp.warm_start]
+        fmg = "FP32 full multigrid (%d V-cycle(s) per level below the finest, %d on the finest)" % (
+            inp.mg32_fmg_cycles or inp.cycles, inp.mg32_fmg_fine_cycles or inp.mg32_fmg_cycles or inp.cycles)
+        start = fmg + " with the guarded learned correction" if mode == m["learned"] else \
+            {0: fmg, 1: "previous-step pressure", 2: "zero"}[inp.warm_start]
         return ("FP64 defect correction (FP64 residual, correction and projection) around FP32 V-cycles%s: "
                 "%s start, V(%d,%d) on the finest level and V(%d,%d) below, omega %.2f, %s prolongation, "
                 "red-black Gauss-Seidel, to %.0e relative residual"
@@ -384,7 +390,7 @@ def run_gb300(args):
     mode = mode_of(dsg, args.mode)
     inp = workload(dsg, args.n, mode, args.tol, args.inner, not args.no_graphs, args.tail_nodes, args.omega32,
                    args.start, args.sweeps32, args.prolong32, args.fmg32, args.fine_sweeps32,
-                   args.mid_sweeps32, args.small_sweeps32, args.krylov)
+                   args.mid_sweeps32, args.small_sweeps32, args.krylov, args.fmg32_fine)
     solver = dsg.Solver(inp)
     solver.set_stream(torch.cuda.current_stream().cuda_stream)
     for t in range(1, args.warmup + 1):

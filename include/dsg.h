@@ -113,6 +113,7 @@ typedef struct dsg_config {
   int mg32_krylov;     /* mixed modes: 0 = the FP32 V-cycles between two FP64 defects iterate on one
                           correction, 1 = each V-cycle preconditions one step of GCR (generalised conjugate
                           residual keeping one previous direction; the step minimises the FP32 residual) */
+  int mg32_fmg_fine_cycles; /* V-cycles of the FP32 FMG start on the finest level (<= 0: as on the others) */
 } dsg_config;
 
 /* Non-dimensional scalars and adaptive counters (COMMON /PHYSICS/, /DIFF/,

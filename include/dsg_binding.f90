@@ -33,6 +33,7 @@ module dsg_binding
     integer(c_int) :: mg32_small_npre, mg32_small_npost
     integer(c_int) :: fp64_exact
     integer(c_int) :: mg32_krylov
+    integer(c_int) :: mg32_fmg_fine_cycles
   end type
   interface
     integer(c_int) function dsg_create(cfg, ctx) bind(C, name='dsg_create')
