@@ -127,3 +127,19 @@ def test_gcr_cuts_vcycles_and_is_deterministic(gpu_lib):
         assert np.array_equal(runs["gcr"][2][f], runs["gcr_again"][2][f]), f
         assert relerr(runs["gcr"][2][f], runs["stationary"][2][f]) < 1e-5, f
 
+
+
+@pytest.mark.parametrize("start", [1, 2])
+def test_mixed_other_starts_reach_the_same_solution(gpu_lib, start):
+    """The mixed solve from the previous-step pressure (1) or from zero (2)
+    reaches the tolerance and the same step as from the FP32 FMG start."""
+    dsg = gpu_lib
+    base = dsg.config.droplet(32, mode=dsg.config.MODE_TOL_MIXED, tol=1e-10, impact_speed=3.0, noise_si=1e-4)
+    runs = {}
+    for key, ws in (("fmg", 0), ("other", start)):
+        with dsg.Solver(base.replace(warm_start=ws)) as s:
+            sts = [s.step(t) for t in range(1, 5)]
+            assert all(st["converged"] == 1 and st["relres"] < 1e-10 for st in sts), sts
+            runs[key] = {f: s.field(f).copy() for f in ("p", "u", "v", "w", "cc")}
+    for f in ("p", "u", "v", "w", "cc"):
+        assert relerr(runs["other"][f], runs["fmg"][f]) < 1e-6, f
