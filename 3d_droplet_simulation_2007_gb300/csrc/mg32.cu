@@ -121,13 +121,35 @@ inline int flat_blocks(size_t n) { return (int)((n + 255) / 256 < 8192 ? (n + 25
 // FP64 in a fixed order, and folded by one block: the results are
 // deterministic.
 
-// Index t's split coordinates.
+// Division by a divisor d >= 1 fixed at launch as a multiply-high, an add and
+// a shift (the round-up method of Granlund and Montgomery, 1994): with
+// s = ceil(log2 d) and m = floor(2^32 (2^s - d) / d) + 1,
+// n / d = (umulhi(n, m) + n) >> s for every 32-bit n (the sum taken in 64
+// bits).  It replaces the two integer divisions of each index decode.
+struct FastDiv {
+  unsigned d, m, s;
+};
+
+FastDiv fast_div(unsigned d) {
+  unsigned s = 0;
+  while ((1ull << s) < d) s++;
+  return FastDiv{d, (unsigned)((((1ull << 32) * ((1ull << s) - d)) / d) + 1), s};
+}
+
+__device__ __forceinline__ unsigned fdiv(unsigned n, const FastDiv &f) {
+  return (unsigned)(((unsigned long long)__umulhi(n, f.m) + n) >> f.s);
+}
+
+// Index t's split coordinates (hx and ny2 divisors of the split layout).
 struct SplitIx {
   int m, j, k;
 };
-__device__ __forceinline__ SplitIx split_ix(unsigned t, Split sp) {
-  const unsigned rem = t / (unsigned)sp.hx, kk = rem / (unsigned)sp.ny2;
-  return SplitIx{(int)(t - rem * (unsigned)sp.hx), (int)(rem - kk * (unsigned)sp.ny2) + 2, (int)kk + 2};
+struct SplitDiv {
+  FastDiv hx, ny2;
+};
+__device__ __forceinline__ SplitIx split_ix(unsigned t, const SplitDiv &sd) {
+  const unsigned rem = fdiv(t, sd.hx), kk = fdiv(rem, sd.ny2);
+  return SplitIx{(int)(t - rem * sd.hx.d), (int)(rem - kk * sd.ny2.d) + 2, (int)kk + 2};
 }
 
 // NS FP64 sums of the block (thread 0 holds them afterwards) written to
@@ -167,11 +189,12 @@ __global__ void __launch_bounds__(kRedThreads) k_gcr_apply(float *__restrict__ w
                                                            const float *__restrict__ r_od,
                                                            const float *__restrict__ q_ev,
                                                            const float *__restrict__ q_od, const float *__restrict__ cc,
-                                                           Dims d, Split sp, float h2i, float r1, float r2) {
+                                                           Dims d, Split sp, SplitDiv sd, float h2i, float r1,
+                                                           float r2) {
   const unsigned n = (unsigned)sp.hx * (unsigned)sp.ny2 * (unsigned)sp.nz2;
   float ww = 0.f, rw = 0.f, wq = 0.f, rq = 0.f;
   for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-    const SplitIx x = split_ix(t, sp);
+    const SplitIx x = split_ix(t, sd);
 #pragma unroll
     for (int c = 0; c < 2; c++) {
       const float w = h2i * lap32_split_cell(c ? z_od : z_ev, c ? z_ev : z_od, cc, d, sp, c, r1, r2, x.m, x.j, x.k, t);
@@ -257,13 +280,14 @@ __global__ void __launch_bounds__(kRedThreads) k_gcr_update(double *__restrict__
                                                             const float *__restrict__ z_od,
                                                             const float *__restrict__ w_ev,
                                                             const float *__restrict__ w_od,
-                                                            const double *__restrict__ coef, Dims d, Split sp) {
+                                                            const double *__restrict__ coef, Dims d, Split sp,
+                                                            SplitDiv sd) {
   const double alpha = coef[0];
   const float alpha32 = (float)alpha, beta = (float)coef[1];
   const unsigned n = (unsigned)sp.hx * (unsigned)sp.ny2 * (unsigned)sp.nz2;
   float qq = 0.f, rr = 0.f;
   for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-    const SplitIx x = split_ix(t, sp);
+    const SplitIx x = split_ix(t, sd);
 #pragma unroll
     for (int c = 0; c < 2; c++) {
       float *dc = c ? d_od : d_ev, *qc = c ? q_od : q_ev, *rc = c ? r_od : r_ev;
@@ -291,12 +315,13 @@ __global__ void __launch_bounds__(kRedThreads) k_gcr_final(double *__restrict__ 
                                                            const float *__restrict__ z_od,
                                                            const float *__restrict__ d_ev,
                                                            const float *__restrict__ d_od,
-                                                           const double *__restrict__ coef, Dims d, Split sp) {
+                                                           const double *__restrict__ coef, Dims d, Split sp,
+                                                           SplitDiv sd) {
   const double alpha = coef[0];
   const float beta = (float)coef[1];
   const unsigned n = (unsigned)sp.hx * (unsigned)sp.ny2 * (unsigned)sp.nz2;
   for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-    const SplitIx x = split_ix(t, sp);
+    const SplitIx x = split_ix(t, sd);
 #pragma unroll
     for (int c = 0; c < 2; c++) {
       const float z = (c ? z_od : z_ev)[t];
@@ -440,33 +465,34 @@ cudaError_t to32(float *dst, const double *src, size_t n, cudaStream_t st) {
 cudaError_t gcr_step(int first, int last, const GcrBufs &g, double *p, float *const z[2], float *const r[2],
                      const float *cc, Dims d, float h2i, float r1, float r2, cudaStream_t st) {
   const Split sp{(d.nx - 2) >> 1, d.ny - 2, d.nz - 2};
+  const SplitDiv sd{fast_div((unsigned)sp.hx), fast_div((unsigned)sp.ny2)};
   const int nb = kRedBlocks;
   if (first) {
     if (last)
       DSG_COUNT k_gcr_apply<true, false><<<nb, kRedThreads, 0, st>>>(g.w[0], g.w[1], g.p1, z[0], z[1], r[0], r[1],
-                                                                    g.q[0], g.q[1], cc, d, sp, h2i, r1, r2);
+                                                                    g.q[0], g.q[1], cc, d, sp, sd, h2i, r1, r2);
     else
       DSG_COUNT k_gcr_apply<true, true><<<nb, kRedThreads, 0, st>>>(g.w[0], g.w[1], g.p1, z[0], z[1], r[0], r[1],
-                                                                   g.q[0], g.q[1], cc, d, sp, h2i, r1, r2);
+                                                                   g.q[0], g.q[1], cc, d, sp, sd, h2i, r1, r2);
     DSG_COUNT k_gcr_fold<true><<<1, kRedThreads, 0, st>>>(g.p1, g.p2, g.coef, nb);
     if (last)
-      DSG_COUNT k_gcr_final<true><<<nb, kRedThreads, 0, st>>>(p, z[0], z[1], g.d[0], g.d[1], g.coef, d, sp);
+      DSG_COUNT k_gcr_final<true><<<nb, kRedThreads, 0, st>>>(p, z[0], z[1], g.d[0], g.d[1], g.coef, d, sp, sd);
     else
       DSG_COUNT k_gcr_update<true><<<nb, kRedThreads, 0, st>>>(p, g.d[0], g.d[1], g.q[0], g.q[1], r[0], r[1], g.p2,
-                                                              z[0], z[1], g.w[0], g.w[1], g.coef, d, sp);
+                                                              z[0], z[1], g.w[0], g.w[1], g.coef, d, sp, sd);
   } else {
     if (last)
       DSG_COUNT k_gcr_apply<false, false><<<nb, kRedThreads, 0, st>>>(g.w[0], g.w[1], g.p1, z[0], z[1], r[0], r[1],
-                                                                     g.q[0], g.q[1], cc, d, sp, h2i, r1, r2);
+                                                                     g.q[0], g.q[1], cc, d, sp, sd, h2i, r1, r2);
     else
       DSG_COUNT k_gcr_apply<false, true><<<nb, kRedThreads, 0, st>>>(g.w[0], g.w[1], g.p1, z[0], z[1], r[0], r[1],
-                                                                    g.q[0], g.q[1], cc, d, sp, h2i, r1, r2);
+                                                                    g.q[0], g.q[1], cc, d, sp, sd, h2i, r1, r2);
     DSG_COUNT k_gcr_fold<false><<<1, kRedThreads, 0, st>>>(g.p1, g.p2, g.coef, nb);
     if (last)
-      DSG_COUNT k_gcr_final<false><<<nb, kRedThreads, 0, st>>>(p, z[0], z[1], g.d[0], g.d[1], g.coef, d, sp);
+      DSG_COUNT k_gcr_final<false><<<nb, kRedThreads, 0, st>>>(p, z[0], z[1], g.d[0], g.d[1], g.coef, d, sp, sd);
     else
       DSG_COUNT k_gcr_update<false><<<nb, kRedThreads, 0, st>>>(p, g.d[0], g.d[1], g.q[0], g.q[1], r[0], r[1], g.p2,
-                                                               z[0], z[1], g.w[0], g.w[1], g.coef, d, sp);
+                                                               z[0], z[1], g.w[0], g.w[1], g.coef, d, sp, sd);
   }
   return cudaGetLastError();
 }

@@ -112,7 +112,8 @@ typedef struct dsg_config {
                           order (bit-identical to the oracle).  DSG_MODE_REF_EXACT always keeps that order. */
   int mg32_krylov;     /* mixed modes: 0 = the FP32 V-cycles between two FP64 defects iterate on one
                           correction, 1 = each V-cycle preconditions one step of GCR (generalised conjugate
-                          residual keeping one previous direction; the step minimises the FP32 residual) */
+                          residual keeping one previous direction; the step minimises the FP32 residual;
+                          an option for tolerances of 1e-9 and below) */
   int mg32_fmg_fine_cycles; /* V-cycles of the FP32 FMG start on the finest level (<= 0: as on the others) */
 } dsg_config;
 
